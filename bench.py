@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Headline benchmark: LETKF analysis throughput (grid columns per second) of
+the GB300 library on the 720x360x40 ocean workload (k=40, T/S/SSH = 81 slabs,
+3,000 T/S profiles + 200,000 SSH/SST swath observations, loc_novrt 800 km ->
+200 km), synthetic seeded inputs.
+
+One step = one complete analysis (observation index build, search,
+localisation, Gram, eigensolve, transform and update epilogue) over every
+ocean column, inputs resident in HBM; the L2 is flushed (256 MB write)
+between timed steps.  `e2e` repeats the step through the public C ABI with
+host buffers: the state and observations are copied in from page-locked host
+memory and the analysis is copied back every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the
+oracle, FP32 arithmetic of the reference) on the host cores, on a bounded
+column sample of the same workload.  With N > 1 (torchrun) every rank runs
+an independent replica on its own GPU (weak scaling, no collectives on the
+data path); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "umd-letkf_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "gridpoints/s on 1 GB300: batched+learned vs plain LETKF at fixed analysis error"
+UNIT = "gridpoints/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            td.init_process_group(backend)
+            self.td, self.torch = td, torch
+            self.dev = torch.device("cuda", self.local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device=self.dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/lgpu_clocks.csv"
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu), "--query-gpu=" + q, "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax = float(parts[2].split()[0])
+            except Exception:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_problem(name, nthreads=0):
+    from letkf_gb300 import synth
+    from letkf_gb300.workloads import WORKLOADS
+    cfg = WORKLOADS[name]
+    gen = dict(cfg["gen"])
+    w = gen.pop("workload")
+    prob = synth.generate(w, nthreads=nthreads, **gen)
+    return prob, cfg
+
+
+def cpu_rate(prob, cfg, target_s=15.0, max_cols=20000, nthreads=0):
+    """Oracle (FP32 restatement of the reference) on a bounded, evenly spread
+    sample of ocean columns; returns (columns/s, sample size, threads)."""
+    from letkf_gb300 import normalize_loc, normalize_solver
+    from oracle import oracle as O
+    inf = normalize_solver(cfg["solver"])
+    o = O.Oracle(prob, normalize_loc(cfg["localization"], prob.vars), rtps=inf["rtps"], rtpp=inf["rtpp"],
+                 mul=inf["mul"])
+    active = np.nonzero(prob.mask == 0)[0]
+    nth = nthreads or os.cpu_count() or 1
+    probe = active[:: max(1, len(active) // (4 * nth))][: 4 * nth]
+    t0 = time.perf_counter()
+    o.run(32, cols=probe, nthreads=nth)
+    dt = time.perf_counter() - t0
+    rate = len(probe) / max(dt, 1e-9)
+    n = int(min(max_cols, max(4 * nth, rate * target_s)))
+    sample = active[:: max(1, len(active) // n)][:n]
+    t0 = time.perf_counter()
+    o.run(32, cols=sample, nthreads=nth)
+    dt = time.perf_counter() - t0
+    o.close()
+    return len(sample) / dt, len(sample), nth, dt
+
+
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return 0
+    prob, cfg = make_problem(args.workload)
+    from letkf_gb300 import normalize_loc, normalize_solver
+    from oracle import oracle as O
+    inf = normalize_solver(cfg["solver"])
+    o = O.Oracle(prob, normalize_loc(cfg["localization"], prob.vars), rtps=inf["rtps"], rtpp=inf["rtpp"],
+                 mul=inf["mul"])
+    active = np.nonzero(prob.mask == 0)[0]
+    nth = os.cpu_count() or 1
+    # size one step to about 10 s of host work
+    probe = active[:: max(1, len(active) // (4 * nth))][: 4 * nth]
+    t0 = time.perf_counter()
+    o.run(32, cols=probe, nthreads=nth)
+    rate = len(probe) / max(time.perf_counter() - t0, 1e-9)
+    n = int(min(len(active), max(4 * nth, rate * 10.0)))
+    sample = active[:: max(1, len(active) // n)][:n]
+    for _ in range(args.warmup):
+        o.run(32, cols=sample[: max(nth, n // 8)], nthreads=nth)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.run(32, cols=sample, nthreads=nth)
+        times.append(time.perf_counter() - t0)
+    o.close()
+    ms = 1000.0 * statistics.mean(times)
+    value = len(sample) / (ms / 1000.0)
+    desc = ("%d of %d ocean columns (evenly spaced) per step, C restatement of the reference algorithm in "
+            "FP32 (oracle/letkf_oracle.c), OpenMP over columns" % (len(sample), len(active)))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args, prob, cfg),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(args, prob, cfg):
+    nact = int(np.sum(prob.mask == 0))
+    return {"workload": "%s: ocean %dx%dx%d grid, T/S/SSH (%d slabs), k=%d, %d obs (T/S profiles + SSH/SST swaths), "
+                        "loc_novrt 800 km (equator) -> 200 km (poles)" % (args.workload, prob.nx, prob.ny, prob.nz,
+                                                                         prob.ns, prob.k, prob.nobs),
+            "columns_total": int(prob.ncol), "columns_active": nact, "ensemble": int(prob.k), "slabs": int(prob.ns),
+            "observations": int(prob.nobs), "l2": "flushed (256 MB device write) before every timed step; "
+                                                  "state in+out 6.7 GB per step also exceeds L2",
+            "parallelism": "replicas" if args.gpus > 1 else "single"}
+
+
+def gpu_arm(args, dist):
+    from letkf_gb300 import PinnedArray, Solver
+    prob, cfg = make_problem(args.workload)
+    hbm, bf16, peak_kind = peaks()
+    dev = dist.local if dist.world > 1 else 0
+    s = Solver(dev)
+    s.solver_init(cfg["solver"])
+    s.loc_init(cfg["localization"], prob.vars, prob.lev_depth)
+    s.set_problem(prob)
+    nact = int(np.sum(prob.mask == 0))
+    # ---- device-resident steps
+    for _ in range(max(args.warmup, 3)):
+        s.run()
+    dist.barrier()
+    clocks = Clocks(dev)
+    tims = []
+    for _ in range(args.steps):
+        s.flush_l2(256 << 20)
+        s.run()
+        tims.append(s.timings())
+    dist.barrier()
+    ck = clocks.stop()
+    ms = statistics.mean(t["total_ms"] for t in tims)
+    ms_max = dist.max(ms)
+    value = dist.world * nact / (ms_max / 1000.0)
+    stage = {k: statistics.mean(t[k] for t in tims) for k in ("index_ms", "prep_ms", "gram_ms", "eig_ms", "update_ms")}
+    launches = tims[-1]["launches"]
+    diag = s.get_diag()
+    kept = float(np.sum(diag["lg_obscount"], dtype=np.float64))
+    cand = float(np.sum(diag["obscount"], dtype=np.float64))
+    k, ns, ncol = prob.k, prob.ns, prob.ncol
+    units = tims[-1]["units"]
+    # algorithmic work: Gram + RHS 2k(k+1) flop per kept obs;
+    # eigensolve ~9k^3 + transform 4k^3 per unit; update 2k^2 per slab and the
+    # state read + analysis write.
+    gram_flop = 2.0 * k * (k + 1) * kept
+    eig_flop = 13.0 * k ** 3 * units
+    upd_bytes = 2.0 * ncol * ns * k * 4 + 4.0 * ncol * ns * 4
+    stages = {
+        "gram": {"ms": stage["gram_ms"], "tflops": gram_flop / (stage["gram_ms"] * 1e-3) / 1e12},
+        "eig": {"ms": stage["eig_ms"], "tflops": eig_flop / (stage["eig_ms"] * 1e-3) / 1e12},
+        "update": {"ms": stage["update_ms"], "gbs": upd_bytes / (stage["update_ms"] * 1e-3) / 1e9},
+        "index": {"ms": stage["index_ms"]}, "prep": {"ms": stage["prep_ms"]},
+        "kept_pairs": kept, "candidate_pairs": cand}
+    dom = max(("gram", "eig", "update"), key=lambda n: stage[n + "_ms"])
+    traffic = read_traffic(dom)
+    if dom == "update":
+        ach = upd_bytes / (stage["update_ms"] * 1e-3) / 1e9
+        roof = {"kernel": "k_update", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "traffic": traffic, "peak_source": peak_kind + " hbm_gbs (burst)"}
+    else:
+        fl = gram_flop if dom == "gram" else eig_flop
+        ach = fl / (stage[dom + "_ms"] * 1e-3) / 1e12
+        roof = {"kernel": "k_" + dom, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": ach / bf16, "traffic": traffic,
+                "peak_source": peak_kind + " bf16_tflops (burst); this kernel computes in FP32 on CUDA cores"}
+    # ---- end to end through the C ABI with page-locked host buffers
+    pin = {n: PinnedArray(getattr(prob, n).shape, getattr(prob, n).dtype) for n in
+           ("state", "mean", "sprd", "olat", "olon", "oz", "otime", "oval", "oerr", "oobsid", "oplatid", "hx",
+            "hx_mean")}
+    for n, p in pin.items():
+        p.array[...] = getattr(prob, n)
+    outp = [PinnedArray(prob.state.shape), PinnedArray(prob.mean.shape), PinnedArray(prob.sprd.shape)]
+    h2d = sum(p.array.nbytes for p in pin.values())
+    d2h = sum(p.array.nbytes for p in outp)
+
+    def e2e_step():
+        s.set_state(pin["state"].array, pin["mean"].array, pin["sprd"].array, prob.vars)
+        s.set_obs(pin["olat"].array, pin["olon"].array, pin["oz"].array, pin["otime"].array, pin["oval"].array,
+                  pin["oerr"].array, pin["oobsid"].array, pin["oplatid"].array, pin["hx"].array,
+                  pin["hx_mean"].array)
+        s.run()
+        s.get_state(tuple(p.array for p in outp))
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_step()
+    dist.barrier()
+    et = []
+    for _ in range(args.steps):
+        s.flush_l2(256 << 20)
+        t0 = time.perf_counter()
+        e2e_step()
+        et.append(time.perf_counter() - t0)
+    dist.barrier()
+    e2e_ms = dist.max(1000.0 * statistics.mean(et))
+    e2e_val = dist.world * nact / (e2e_ms / 1000.0)
+    ok = bool(np.all(np.isfinite(outp[1].array)))
+    for p in list(pin.values()) + outp:
+        p.free()
+    s.close()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no public dataset)",
+            "config": workload_config(args, prob, cfg), "clocks": ck, "gpu_launches": launches * args.steps,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": e2e_ms},
+            "roofline": roof, "stages": stages, "analysis_finite": ok}
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        rate, n, nth, dt = cpu_rate(prob, cfg)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
+                                "sample": "%d of %d ocean columns (evenly spaced), %.1f s, FP32 C restatement of "
+                                          "the reference algorithm (oracle/letkf_oracle.c)" % (n, nact, dt)}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/<kernel>_c2.md, line 'traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", "k_%s_c2.md" % kernel)
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return reference_arm(args, dist)
+        return gpu_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

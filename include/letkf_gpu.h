@@ -1,0 +1,192 @@
+/*
+ * letkf_gpu.h -- C ABI of the GB300 (sm_103a) LETKF per-gridpoint analysis.
+ *
+ * This library replaces the analysis path of UMD-LETKF: the local
+ * observation search, Gaspari-Cohn localisation, the LETKF core solve and
+ * the ensemble update with its relaxation/inflation/bounds epilogue.  It is
+ * called from the host exactly where the reference calls its solver module:
+ *
+ *   reference (Fortran module letkf_solver)        this ABI
+ *   ------------------------------------------    ----------------------------
+ *   letkf_solver_init(config)                      lgpu_solver_init
+ *     src/letkf_solver.F90:73-142
+ *   letkf_loc_init(config) + plugin %init          lgpu_loc_init
+ *     src/letkf_loc.F90:164-210, plugin init
+ *   module globals lat_ij/lon_ij/mask_ij           lgpu_set_grid
+ *     src/letkf_state.F90:166-173
+ *   module globals state_ij/state_mean_ij/         lgpu_set_state
+ *     state_sprd_ij, statevars
+ *     src/letkf_state.F90:176-208, :83-98
+ *   module globals obs_def/obs_hx/obs_hx_mean      lgpu_set_obs
+ *     src/letkf_obs.F90:57-68, :164-171
+ *   letkf_solver_run()                             lgpu_solver_run
+ *     src/letkf_solver.F90:150-389
+ *   in-place update of the state module arrays     lgpu_get_state
+ *     src/letkf_solver.F90:288,299-379
+ *   diagnostics written by letkf_solver_final      lgpu_get_diag
+ *     src/letkf_solver.F90:131-140,212,220,265-268
+ *   letkf_solver_final()                           lgpu_solver_final
+ *     src/letkf_solver.F90:397-527
+ *
+ * Conventions
+ *   - Plain C types and host pointers only; the library owns every device
+ *     buffer behind the opaque handle.  Host arrays are borrowed for the
+ *     duration of a call.
+ *   - Layouts are the reference's Fortran column-major arrays read as C:
+ *       state[ij][slab][member]   (state_ij(k, ns, ij))
+ *       mean[ij][slab], sprd[ij][slab]
+ *       hx[obs][member]           (obs_hx(k, nobs))
+ *       lg_obscount[group][ij]    (diag_lg_obscount(ij, maxgroups))
+ *     Indices (slabs, groups, observation indices) are 0-based.
+ *   - Every call returns an lgpu_status; on failure lgpu_last_error() holds a
+ *     message.  The reference aborts the MPI job in these cases
+ *     (letkf_mpi_abort, src/letkf_mpi.F90:159-169); the caller decides.
+ *   - One host thread per handle; calls on a handle are not re-entrant.
+ *   - There is no CPU fallback: without a usable sm_103a device every call
+ *     that needs it fails with LGPU_ERR_CUDA.
+ */
+#ifndef LETKF_GPU_H
+#define LETKF_GPU_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lgpu_handle lgpu_handle;
+
+typedef enum lgpu_status {
+  LGPU_OK = 0,
+  LGPU_ERR_ARG = 1,                   /* bad argument (NULL, size, range) */
+  LGPU_ERR_CUDA = 2,                  /* CUDA runtime error / no device */
+  LGPU_ERR_NOMEM = 3,                 /* device allocation failed */
+  LGPU_ERR_UNSUPPORTED_LOCALIZER = 4, /* localization.class not registered */
+  LGPU_ERR_CONFIG = 5,                /* invalid solver / localizer settings */
+  LGPU_ERR_ORDER = 6,                 /* call made before its inputs were set */
+  LGPU_ERR_CAPACITY = 7,              /* a static limit was exceeded */
+  LGPU_ERR_NONFINITE = 8,             /* non-finite analysis produced */
+  LGPU_ERR_EIG = 9,                   /* eigensolver did not converge */
+  LGPU_ERR_UNSUPPORTED = 10           /* size outside what this build supports */
+} lgpu_status;
+
+#define LGPU_MAX_INTERP 16   /* linearinterp_lat points per table */
+#define LGPU_MAX_IDS 32      /* sat_obs / sat_plats list entries */
+#define LGPU_MAX_LEVELS 128  /* loc_vtgc level groups */
+#define LGPU_MAX_K 64        /* ensemble size supported by this build */
+
+/* Solver settings: the keys letkf_solver_init reads (src/letkf_solver.F90:86-101).
+ * Validation matches :113-125 (0<=rtps<=1, 0<=rtpp<=1, not both, mul>=1). */
+typedef struct lgpu_solver_config {
+  float rtps;      /* solver.inflation.rtps, default 0 */
+  float rtpp;      /* solver.inflation.rtpp, default 0 */
+  float mul;       /* solver.inflation.mul, default 1 */
+  int save_diag;   /* solver.save_diag, default 1 */
+} lgpu_solver_config;
+
+/* One {lat, radius} entry of a linearinterp_lat table (src/letkf_loc.F90:251-294). */
+typedef struct lgpu_interp_point { float lat; float radius; } lgpu_interp_point;
+
+/* Localizer selection and parameters (localization: section).
+ *   cls = "loc_novrt"  (src/subclass.letkf_localizer/letkf_loc_novrt.F90)
+ *         uses hz (localization.hzloc.value)
+ *   cls = "loc_ocean"  (src/subclass.letkf_localizer/letkf_loc_ocean.F90)
+ *         uses hz (hzloc_prof), hz_sat (hzloc_sat), tloc_prof, tloc_sat,
+ *         sat_obs, sat_plats, vtloc_surf (0 none, 1 bkg_t), bkg_t_delta,
+ *         bkg_t_var (index into the statevars given to lgpu_set_state)
+ *   cls = "loc_vtgc"   horizontal GC times vertical GC with one group per
+ *         level (a plugin added by this project for depth localisation)
+ *         uses hz, vtloc (metres), nlev + lev_depth (vertical grid)
+ * The class name is matched case-insensitively, as letkf_loc_init does. */
+typedef struct lgpu_loc_config {
+  const char *cls;
+  int n_hz; const lgpu_interp_point *hz;
+  int n_hz_sat; const lgpu_interp_point *hz_sat;
+  float tloc_prof, tloc_sat;          /* <= 0 disables (default -1) */
+  int vtloc_surf;
+  float bkg_t_delta;
+  int bkg_t_var;
+  int n_sat_obs; const int *sat_obs;
+  int n_sat_plats; const int *sat_plats;
+  float vtloc;
+  int nlev; const float *lev_depth;
+} lgpu_loc_config;
+
+/* letkf_statevar_spec (src/letkf_state.F90:83-98), 0-based grid_s_idx. */
+typedef struct lgpu_statevar {
+  int grid_s_idx;
+  int levels;
+  float ana_inc_max;      /* default 9.99e36 */
+  float ana_bounds[2];    /* default {-9.99e36, 9.99e36} */
+} lgpu_statevar;
+
+/* letkf_observation (src/letkf_obs.F90:57-68) as structure-of-arrays, after
+ * the reference's QC compaction (only qc == 0 observations). */
+typedef struct lgpu_obs {
+  const float *lat, *lon, *zdim, *time, *val, *err;
+  const int *obsid, *platid;
+} lgpu_obs;
+
+/* Device time of the last lgpu_solver_run, from CUDA events on the
+ * library's stream. */
+typedef struct lgpu_timings {
+  float total_ms;    /* whole run */
+  float index_ms;    /* observation preparation + spatial index */
+  float prep_ms;     /* per-column localisation parameters */
+  float gram_ms;     /* search + localisation + Gram/RHS */
+  float eig_ms;      /* eigensolve + transform */
+  float update_ms;   /* X_b * T + relaxation/inflation/bounds epilogue */
+  int launches;      /* kernels launched by the run */
+  int units;         /* (column, group) solve units */
+  long long kept_pairs;   /* sum over units of kept local observations (only when counted) */
+} lgpu_timings;
+
+int lgpu_create(int device, lgpu_handle **out);
+void lgpu_destroy(lgpu_handle *h);
+const char *lgpu_last_error(const lgpu_handle *h);
+
+int lgpu_solver_init(lgpu_handle *h, const lgpu_solver_config *cfg);
+int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *cfg);
+int lgpu_loc_maxgroups(const lgpu_handle *h);
+
+int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, const int *mask);
+int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean,
+                   const float *sprd, int nvars, const lgpu_statevar *vars);
+int lgpu_set_obs(lgpu_handle *h, int nobs, const lgpu_obs *obs, const float *hx, const float *hx_mean);
+
+int lgpu_solver_run(lgpu_handle *h);
+
+int lgpu_get_state(lgpu_handle *h, float *state, float *mean, float *sprd);
+int lgpu_get_diag(lgpu_handle *h, float *maxhz, float *obscount, float *lg_obscount, float *lg_obsloc);
+int lgpu_get_timings(const lgpu_handle *h, lgpu_timings *t);
+int lgpu_solver_final(lgpu_handle *h);
+
+/* Verification: the local observation list of (ij, group) in canonical order
+ * (ascending observation index) with its localisation weights; *n receives
+ * the full count (entries beyond cap are not written), *ncand the number of
+ * search candidates (diag_obscount).  Needs a prior lgpu_solver_run. */
+int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
+                     int *n, int *ncand);
+
+/* Verification: evaluate the library's distance metric and Gaspari-Cohn
+ * weights on the device.  dist[i] = distance (m) between points
+ * (lat1[i], lon1[i]) and (lat2[i], lon2[i]).  gc must hold 2n floats:
+ * gc[i] = the fast single-precision weight used in the search loop and
+ * gc[n + i] = letkf_loc_gc(z[i], L[i]) evaluated exactly as the reference
+ * does (REAL(8), rounded to REAL). */
+/* Page-locked host memory for callers that stream state in and out every
+ * analysis (host<->device copies run at full link speed from it). */
+int lgpu_host_alloc(size_t bytes, void **ptr);
+int lgpu_host_free(void *ptr);
+
+/* Benchmark hygiene: overwrite `bytes` of device scratch memory (owned by the
+ * handle) on the library's stream so the next run starts with a cold L2. */
+int lgpu_flush_l2(lgpu_handle *h, size_t bytes);
+
+int lgpu_debug_metric(lgpu_handle *h, int n, const float *lat1, const float *lon1,
+                      const float *lat2, const float *lon2, float *dist);
+int lgpu_debug_gc(lgpu_handle *h, int n, const float *z, const float *L, float *gc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

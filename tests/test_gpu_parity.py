@@ -1,0 +1,226 @@
+"""GPU parity: the CUDA library through its C ABI against the CPU oracle.
+
+Bars (written here, checked per variable and level):
+  - distances, local observation lists (indices and canonical order),
+    search-candidate counts and maxhz: bit-exact;
+  - localisation weights: |r_gpu - r_oracle| <= 4e-7 (one GC factor) /
+    1e-6 (products), keep/drop decisions exact;
+  - analysis perturbations and analysis mean: relative L2 <= 1e-5 per slab
+    against the FP32 oracle (reference arithmetic) and the FP64 oracle,
+    for slabs whose perturbation norm is not negligible;
+  - mean increment: reported; relative L2 <= 2e-3 per slab (FP32 Gram
+    accumulation error of ill-conditioned columns, shared by the
+    reference's own FP32 path).
+"""
+import numpy as np
+import pytest
+
+from conftest import workload
+from helpers import compare, gpu_run, oracle_for, workload_cfg
+
+pytestmark = pytest.mark.gpu
+
+PERT_TOL = 1e-5
+MEAN_TOL = 1e-5
+INC_TOL = 2e-3
+
+
+@pytest.fixture(scope="module")
+def solver():
+    from letkf_gb300 import Solver
+    s = Solver(0)
+    yield s
+    s.close()
+
+
+def test_metric_bitexact(solver):
+    from oracle import oracle as O
+    rng = np.random.default_rng(7)
+    n = 20000
+    la1 = rng.uniform(-90, 90, n).astype(np.float32)
+    lo1 = rng.uniform(-180, 360, n).astype(np.float32)
+    la2 = np.clip(la1 + rng.normal(0, 20, n), -90, 90).astype(np.float32)
+    lo2 = (lo1 + rng.normal(0, 30, n)).astype(np.float32)
+    got = solver.debug_metric(la1, lo1, la2, lo2)
+    ref = np.array([O.dist(O.unitvec(a, b), O.unitvec(c, d)) for a, b, c, d in zip(la1, lo1, la2, lo2)], np.float32)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_gc_fast_and_exact(solver):
+    from oracle import oracle as O
+    rng = np.random.default_rng(8)
+    n = 200000
+    L = rng.choice(np.array([50e3, 200e3, 500e3, 800e3, 200.0], np.float32), n)
+    z = (rng.random(n) * 2.05 * L / np.sqrt(0.3)).astype(np.float32)
+    fast, exact = solver.debug_gc(z, L)
+    assert np.max(np.abs(fast.astype(np.float64) - exact)) <= 4e-7
+    ref = np.array([O.gc(a, b) for a, b in zip(z[:20000], L[:20000])], np.float32)
+    assert np.array_equal(exact[:20000].view(np.uint32), ref.view(np.uint32))
+
+
+LIST_CASES = [("simple3d", None), ("ocean", None), ("c1", None), ("c2small", 150), ("c3small", 150)]
+
+
+@pytest.mark.parametrize("name,nsample", LIST_CASES)
+def test_obslists_bitexact(name, nsample):
+    cfg = workload_cfg(name)
+    prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
+    res = gpu_run(prob, cfg["localization"], cfg["solver"], keep_open=True)
+    s = res["solver"]
+    o = oracle_for(prob, cfg["localization"], cfg["solver"])
+    rng = np.random.default_rng(1)
+    active = np.nonzero(prob.mask == 0)[0]
+    if nsample is None:
+        # every column near an observation plus a random sample
+        cols = rng.choice(active, size=min(200, len(active)), replace=False)
+        near = []
+        for la, lo in zip(prob.olat[:50], prob.olon[:50]):
+            d = (prob.lat - la) ** 2 + ((prob.lon - lo + 180) % 360 - 180) ** 2
+            near.append(int(np.argmin(d)))
+        cols = np.unique(np.concatenate([cols, near]))
+    else:
+        cols = rng.choice(active, size=nsample, replace=False)
+    G = s.maxgroups
+    groups = range(G) if G <= 2 else [0, G // 2, G - 1]
+    nonempty = 0
+    for c in cols:
+        for g in groups:
+            gi, gr, gn = s.obslist(int(c), g)
+            oi, orr, on = o.obslist(int(c), g)
+            assert gn == on, (c, g)
+            assert np.array_equal(gi, oi), (c, g, len(gi), len(oi))
+            tol = 1e-6 if (name == "c1") else 4e-7
+            assert np.all(np.abs(gr.astype(np.float64) - orr) <= tol), (c, g)
+            nonempty += len(gi) > 0
+    assert nonempty > 0
+    # diagnostics: maxhz and candidate counts bit-exact, kept counts exact
+    ref = o.run(32, cols=cols)
+    d = res["diag"]
+    assert np.array_equal(d["maxhz"][cols], ref["maxhz"])
+    assert np.array_equal(d["obscount"][cols], ref["obscount"])
+    assert np.array_equal(d["lg_obscount"][:, cols].T, ref["lg_obscount"])
+    assert np.allclose(d["lg_obsloc"][:, cols].T, ref["lg_obsloc"], rtol=2e-5, atol=1e-5)
+    s.close()
+    o.close()
+
+
+def _check_analysis(prob, cfg_loc, cfg_solver, cols, variables=None, label=""):
+    gpu = gpu_run(prob, cfg_loc, cfg_solver, variables=variables)
+    o = oracle_for(prob, cfg_loc, cfg_solver, variables=variables)
+    for prec in (32, 64):
+        ref = o.run(prec, cols=cols)
+        cmp = compare(prob, gpu, ref, cols)
+        # slabs with negligible perturbations (e.g. fully clipped) are skipped
+        pr = ref["state"] - ref["mean"][:, :, None]
+        pn = np.sqrt(np.sum(pr.astype(np.float64) ** 2, axis=(0, 2)))
+        ok = pn > 1e-6 * max(pn.max(), 1e-30)
+        assert np.all(cmp["pert"][ok] <= PERT_TOL), (label, prec, cmp["pert"].max(), np.argmax(cmp["pert"]))
+        assert np.all(cmp["mean"] <= MEAN_TOL), (label, prec, cmp["mean"].max())
+        big = cmp["inc_norm"] > 1e-3 * max(cmp["inc_norm"].max(), 1e-30)
+        assert np.all(cmp["inc"][big] <= INC_TOL), (label, prec, cmp["inc"][big].max())
+    # masked columns keep the background exactly (src/letkf_solver.F90:207)
+    mc = np.nonzero(prob.mask)[0]
+    if len(mc):
+        assert np.array_equal(gpu["state"][mc], prob.state[mc])
+        assert np.array_equal(gpu["mean"][mc], prob.mean[mc])
+        assert np.array_equal(gpu["sprd"][mc], prob.sprd[mc])
+    assert np.all(np.isfinite(gpu["state"]))
+    o.close()
+    return gpu
+
+
+@pytest.mark.parametrize("variant", ["default", "bounds_check", "inflation_rtps", "inflation_rtpp", "inflation_mul"])
+def test_simple3d_variants(variant):
+    from letkf_gb300.workloads import SIMPLE3D_VARIANTS, apply_bounds
+    cfg = workload_cfg("simple3d")
+    prob = workload("simple3d")
+    v = SIMPLE3D_VARIANTS[variant]
+    variables = apply_bounds(prob.vars, v["bounds"])
+    cols = np.arange(prob.ncol)[::3]
+    _check_analysis(prob, cfg["localization"], v["solver"], cols, variables=variables, label=variant)
+
+
+@pytest.mark.parametrize("name", ["ocean", "c1", "c2small", "c3small"])
+def test_analysis_parity(name):
+    cfg = workload_cfg(name)
+    prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
+    active = np.nonzero(prob.mask == 0)[0]
+    rng = np.random.default_rng(2)
+    cols = np.sort(rng.choice(active, size=min(600, len(active)), replace=False))
+    _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label=name)
+
+
+def test_single_observation_closed_form():
+    """One obs, one column in range: the GPU mean increment at the observed
+    slab equals the scalar Kalman update."""
+    prob = workload("simple3d")
+    cfg = workload_cfg("simple3d")
+    gpu = gpu_run(prob, cfg["localization"], {})
+    o = oracle_for(prob, cfg["localization"], {})
+    col = int(np.argmin((prob.lat - 41.0) ** 2 + (prob.lon - 221.0) ** 2))
+    idx, rr, _ = o.obslist(col, 0)
+    assert list(idx) == [0]
+    y = prob.hx[0].astype(np.float64)
+    s2 = y @ y / (prob.k - 1)
+    d = float(prob.oval[0]) - float(prob.hx_mean[0])
+    expect = d * s2 / (s2 + float(prob.oerr[0]) / float(rr[0]))
+    inc = float(gpu["mean"][col, 0]) - float(prob.mean[col, 0])
+    assert abs(inc - expect) < 2e-5 * max(1.0, abs(expect))
+    o.close()
+
+
+def test_edge_cases():
+    """No observations; every column masked; ensemble sizes 2 and odd."""
+    from dataclasses import replace
+    cfg = workload_cfg("simple3d")
+    prob = workload("simple3d")
+    empty = replace(prob, olat=prob.olat[:0], olon=prob.olon[:0], oz=prob.oz[:0], otime=prob.otime[:0],
+                    oval=prob.oval[:0], oerr=prob.oerr[:0], oobsid=prob.oobsid[:0], oplatid=prob.oplatid[:0],
+                    hx=prob.hx[:0], hx_mean=prob.hx_mean[:0])
+    g = gpu_run(empty, cfg["localization"], {})
+    full_b = prob.state + prob.mean[:, :, None]
+    assert np.allclose(g["state"], full_b, atol=3e-6)
+    assert np.all(g["diag"]["obscount"] == 0)
+    masked = replace(prob, mask=np.ones_like(prob.mask))
+    g = gpu_run(masked, cfg["localization"], {})
+    assert np.array_equal(g["state"], prob.state)
+    for k in (2, 7, 33):
+        p = workload("c1", k=k)
+        c1 = workload_cfg("c1")
+        cols = np.arange(0, p.ncol, 37)
+        _check_analysis(p, c1["localization"], c1["solver"], cols, label="k=%d" % k)
+
+
+def test_errors_and_validation():
+    from letkf_gb300 import LgpuError, Solver
+    with Solver(0) as s:
+        for bad in ({"inflation": {"rtps": 1.5}}, {"inflation": {"rtpp": -0.1}},
+                    {"inflation": {"rtps": 0.5, "rtpp": 0.5}}, {"inflation": {"mul": 0.9}}):
+            with pytest.raises(LgpuError) as e:
+                s.solver_init(bad)
+            assert e.value.code == 5
+        with pytest.raises(LgpuError) as e:
+            s.loc_init({"class": "loc_nosuch", "hzloc": [(0.0, 1e5)]})
+        assert e.value.code == 4 and "LOC_NOSUCH not found" in e.value.msg
+        with pytest.raises(LgpuError) as e:
+            s.run()
+        assert e.value.code == 6
+        prob = workload("simple3d")
+        s.solver_init({})
+        s.loc_init(workload_cfg("simple3d")["localization"], prob.vars)
+        with pytest.raises(LgpuError) as e:
+            s.set_state(prob.state, prob.mean, prob.sprd, prob.vars)
+        assert e.value.code == 6          # state before grid
+        s.set_grid(prob.lat, prob.lon, prob.mask)
+        big = np.zeros((prob.ncol, 1, 65), np.float32)
+        with pytest.raises(LgpuError) as e:
+            s.set_state(big, np.zeros((prob.ncol, 1), np.float32), np.zeros((prob.ncol, 1), np.float32),
+                        [dict(grid_s_idx=0, levels=1)])
+        assert e.value.code == 10
+        s.set_state(prob.state, prob.mean, prob.sprd, prob.vars)
+        bad_err = prob.oerr.copy()
+        bad_err[0] = 0.0
+        with pytest.raises(LgpuError) as e:
+            s.set_obs(prob.olat, prob.olon, prob.oz, prob.otime, prob.oval, bad_err, prob.oobsid, prob.oplatid,
+                      prob.hx, prob.hx_mean)
+        assert e.value.code == 1

@@ -1,0 +1,681 @@
+// lgpu_api.cu -- the C ABI (include/letkf_gpu.h): handle, validation that
+// mirrors the reference's solver/localizer initialisation, uploads, the run
+// orchestration on one CUDA stream, timings and verification helpers.
+#include <algorithm>
+#include <cctype>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <cmath>
+
+#include "lgpu_internal.cuh"
+
+using namespace lgpu;
+
+namespace lgpu {
+size_t gram_smem_bytes(int k);
+}
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) cap = bytes ? bytes : 16;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+enum {
+  B_LAT, B_LON, B_MASK, B_COL2ACT, B_ACTIVE,
+  B_BKG, B_MEANB, B_SPRDB, B_ANA, B_MEANA, B_SPRDA, B_SLABVAR, B_SLABLEV, B_VARINC, B_VARLB, B_VARUB,
+  B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID, B_HX, B_HXM, B_SATOBS, B_SATPLATS,
+  B_GEOM, B_CELL, B_COUNT, B_FILL, B_POSTMP, B_ORDER, B_ATMP, B_BTMP, B_SA, B_SB, B_SHX, B_SIDX, B_CSTART,
+  B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
+  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH,
+  B_COUNT_ALL
+};
+
+}  // namespace
+
+struct lgpu_handle {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[8] = {};
+  std::string err;
+  bool solver_ok = false, loc_ok = false, grid_ok = false, state_ok = false, obs_ok = false, ran = false;
+  lgpu_solver_config scfg{0.0f, 0.0f, 1.0f, 1};
+  DevLoc loc{};
+  std::vector<int> sat_obs, sat_plats;
+  std::vector<float> lev_depth;
+  int bkg_t_var = -1;
+  int ncol = 0, nact = 0;
+  std::vector<int> h_col2act;
+  int k = 0, ns = 0, kp = 0;
+  std::vector<lgpu_statevar> vars;
+  int nobs = 0;
+  IndexGeom geom{};
+  int ncell = 0;
+  int nunits = 0;
+  DevBuf buf[B_COUNT_ALL];
+  lgpu_timings tim{};
+};
+
+namespace {
+
+int fail(lgpu_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(lgpu_handle *h, cudaError_t e, const char *what) {
+  return fail(h, e == cudaErrorMemoryAllocation ? LGPU_ERR_NOMEM : LGPU_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                   \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return cuda_fail(h, _e, what); \
+  } while (0)
+
+std::string upper(const char *s) {
+  std::string r(s ? s : "");
+  for (auto &c : r) c = (char)std::toupper((unsigned char)c);
+  return r;
+}
+
+// linearinterp_lat_init (src/letkf_loc.F90:251-294): pad with a 0-degree
+// point carrying the first radius and a 90-degree point carrying the last.
+int build_interp(lgpu_handle *h, Interp &t, int n, const lgpu_interp_point *pts, const char *name) {
+  std::memset(&t, 0, sizeof(t));
+  if (n <= 0 || !pts) return fail(h, LGPU_ERR_CONFIG, std::string("localizer needs a non-empty ") + name + " table");
+  if (n > LGPU_MAX_INTERP) return fail(h, LGPU_ERR_CAPACITY, std::string(name) + " has more than 16 points");
+  float last_lat = 0.0f, last_r = 0.0f;
+  for (int i = 0; i < n; i++) {
+    if (!(pts[i].radius > 0.0f)) return fail(h, LGPU_ERR_CONFIG, std::string(name) + " radius must be > 0");
+    if (pts[i].lat > 0.0f && t.n == 0) { t.lat[0] = 0.0f; t.dist[0] = pts[i].radius; t.n = 1; }
+    t.lat[t.n] = pts[i].lat;
+    t.dist[t.n] = pts[i].radius;
+    t.n++;
+    last_lat = pts[i].lat;
+    last_r = pts[i].radius;
+  }
+  if (last_lat < 90.0f) { t.lat[t.n] = 90.0f; t.dist[t.n] = last_r; t.n++; }
+  return LGPU_OK;
+}
+
+void build_geom(IndexGeom &g, int &ncell) {
+  int off = 0;
+  for (int b = 0; b < kNB; b++) {
+    const double lat0 = -90.0 + b, lat1 = lat0 + 1.0;
+    const double pole = std::max(std::fabs(lat0), std::fabs(lat1));
+    int n = (int)std::floor(360.0 * std::cos(pole * 3.14159265358979323846 / 180.0));
+    if (n < 1) n = 1;
+    g.nlon[b] = n;
+    g.off[b] = off;
+    off += n;
+  }
+  g.off[kNB] = off;
+  ncell = off;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgpu_create(int device, lgpu_handle **out) {
+  if (!out) return LGPU_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n <= 0) return LGPU_ERR_CUDA;
+  if (device < 0 || device >= n) return LGPU_ERR_ARG;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return LGPU_ERR_CUDA;
+  lgpu_handle *h = new lgpu_handle();
+  h->device = device;
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  build_geom(h->geom, h->ncell);
+  if (h->buf[B_GEOM].ensure(sizeof(IndexGeom)) != cudaSuccess ||
+      cudaMemcpy(h->buf[B_GEOM].p, &h->geom, sizeof(IndexGeom), cudaMemcpyHostToDevice) != cudaSuccess) {
+    delete h;
+    return LGPU_ERR_CUDA;
+  }
+  *out = h;
+  return LGPU_OK;
+}
+
+void lgpu_destroy(lgpu_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (auto &b : h->buf) b.release();
+  for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+const char *lgpu_last_error(const lgpu_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+// letkf_solver_init (src/letkf_solver.F90:73-142)
+int lgpu_solver_init(lgpu_handle *h, const lgpu_solver_config *c) {
+  if (!h || !c) return LGPU_ERR_ARG;
+  if (c->rtps > 1.0f || c->rtps < 0.0f)
+    return fail(h, LGPU_ERR_CONFIG, "illegal value for infl_rtps (should be <1.0 and >0.0).");
+  if (c->rtpp > 1.0f || c->rtpp < 0.0f)
+    return fail(h, LGPU_ERR_CONFIG, "illegal value for infl_rtpp (should be <1.0 and >0.0).");
+  if (c->rtpp != 0.0f && c->rtps != 0.0f)
+    return fail(h, LGPU_ERR_CONFIG, "cannot have both RTPS and RTPP enabled at the same time. ");
+  if (c->mul < 1.0f) return fail(h, LGPU_ERR_CONFIG, "infl_mul must be >=1.0.");
+  h->scfg = *c;
+  h->solver_ok = true;
+  return LGPU_OK;
+}
+
+// letkf_loc_init (src/letkf_loc.F90:164-210) + the plugin's init
+int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *c) {
+  if (!h || !c) return LGPU_ERR_ARG;
+  h->loc_ok = false;
+  const std::string cls = upper(c->cls);
+  DevLoc L{};
+  L.tloc_prof = -1.0f;
+  L.tloc_sat = -1.0f;
+  int rc;
+  h->sat_obs.clear();
+  h->sat_plats.clear();
+  h->lev_depth.clear();
+  h->bkg_t_var = -1;
+  if (cls == "LOC_NOVRT") {
+    L.cls = LOC_NOVRT;
+    if ((rc = build_interp(h, L.hz, c->n_hz, c->hz, "hzloc")) != LGPU_OK) return rc;
+    L.groups = 1;
+  } else if (cls == "LOC_OCEAN") {
+    L.cls = LOC_OCEAN;
+    if ((rc = build_interp(h, L.hz, c->n_hz, c->hz, "hzloc_prof")) != LGPU_OK) return rc;
+    if ((rc = build_interp(h, L.hz_sat, c->n_hz_sat, c->hz_sat, "hzloc_sat")) != LGPU_OK) return rc;
+    L.tloc_prof = c->tloc_prof;
+    L.tloc_sat = c->tloc_sat;
+    if (c->n_sat_obs < 0 || c->n_sat_obs > LGPU_MAX_IDS || c->n_sat_plats < 0 || c->n_sat_plats > LGPU_MAX_IDS)
+      return fail(h, LGPU_ERR_CAPACITY, "sat_obs / sat_plats lists hold at most 32 ids");
+    if (c->n_sat_obs > 0 && !c->sat_obs) return LGPU_ERR_ARG;
+    if (c->n_sat_plats > 0 && !c->sat_plats) return LGPU_ERR_ARG;
+    h->sat_obs.assign(c->sat_obs, c->sat_obs + c->n_sat_obs);
+    h->sat_plats.assign(c->sat_plats, c->sat_plats + c->n_sat_plats);
+    if (c->vtloc_surf == 0) {
+      L.groups = 1;
+    } else if (c->vtloc_surf == 1) {
+      if (!(c->bkg_t_delta >= 0.0f)) return fail(h, LGPU_ERR_CONFIG, "vtloc_surf.bkg_t_delta must be >= 0");
+      L.groups = 2;
+      L.vtloc_surf = 1;
+      L.bkg_t_delta = c->bkg_t_delta;
+      h->bkg_t_var = c->bkg_t_var;
+    } else {
+      return fail(h, LGPU_ERR_CONFIG, "illegal vtloc_surf 'type' given: " + std::to_string(c->vtloc_surf));
+    }
+  } else if (cls == "LOC_VTGC") {
+    L.cls = LOC_VTGC;
+    if ((rc = build_interp(h, L.hz, c->n_hz, c->hz, "hzloc")) != LGPU_OK) return rc;
+    if (!(c->vtloc > 0.0f)) return fail(h, LGPU_ERR_CONFIG, "loc_vtgc needs vtloc > 0");
+    if (c->nlev <= 0 || !c->lev_depth) return fail(h, LGPU_ERR_CONFIG, "loc_vtgc needs the level depths");
+    if (c->nlev > LGPU_MAX_LEVELS) return fail(h, LGPU_ERR_CAPACITY, "loc_vtgc supports at most 128 levels");
+    L.vloc = c->vtloc;
+    h->lev_depth.assign(c->lev_depth, c->lev_depth + c->nlev);
+    L.groups = c->nlev;
+  } else {
+    return fail(h, LGPU_ERR_UNSUPPORTED_LOCALIZER, "localizer class " + cls + " not found.");
+  }
+  if (L.groups <= 0) return fail(h, LGPU_ERR_CONFIG, "localizer class needs to properly define 'maxgroups'");
+  h->loc = L;
+  h->loc_ok = true;
+  h->ran = false;
+  return LGPU_OK;
+}
+
+int lgpu_loc_maxgroups(const lgpu_handle *h) { return (h && h->loc_ok) ? h->loc.groups : -1; }
+
+int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, const int *mask) {
+  if (!h) return LGPU_ERR_ARG;
+  if (nij <= 0 || !lat || !lon) return fail(h, LGPU_ERR_ARG, "set_grid: bad arguments");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  std::vector<int> m(nij, 0), c2a(nij, -1), act;
+  act.reserve(nij);
+  for (int i = 0; i < nij; i++) {
+    if (!std::isfinite(lat[i]) || !std::isfinite(lon[i]) || lat[i] < -90.0f || lat[i] > 90.0f)
+      return fail(h, LGPU_ERR_ARG, "set_grid: latitude out of range at ij=" + std::to_string(i));
+    m[i] = mask ? (mask[i] != 0) : 0;
+    if (!m[i]) { c2a[i] = (int)act.size(); act.push_back(i); }
+  }
+  CK(h->buf[B_LAT].ensure(sizeof(float) * nij), "alloc lat");
+  CK(h->buf[B_LON].ensure(sizeof(float) * nij), "alloc lon");
+  CK(h->buf[B_MASK].ensure(sizeof(int) * nij), "alloc mask");
+  CK(h->buf[B_COL2ACT].ensure(sizeof(int) * nij), "alloc col2act");
+  CK(h->buf[B_ACTIVE].ensure(sizeof(int) * std::max<size_t>(1, act.size())), "alloc active");
+  CK(cudaMemcpyAsync(h->buf[B_LAT].p, lat, sizeof(float) * nij, cudaMemcpyHostToDevice, h->st), "H2D lat");
+  CK(cudaMemcpyAsync(h->buf[B_LON].p, lon, sizeof(float) * nij, cudaMemcpyHostToDevice, h->st), "H2D lon");
+  CK(cudaMemcpyAsync(h->buf[B_MASK].p, m.data(), sizeof(int) * nij, cudaMemcpyHostToDevice, h->st), "H2D mask");
+  CK(cudaMemcpyAsync(h->buf[B_COL2ACT].p, c2a.data(), sizeof(int) * nij, cudaMemcpyHostToDevice, h->st), "H2D c2a");
+  if (!act.empty())
+    CK(cudaMemcpyAsync(h->buf[B_ACTIVE].p, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, h->st), "H2D act");
+  CK(cudaStreamSynchronize(h->st), "set_grid sync");
+  h->ncol = nij;
+  h->nact = (int)act.size();
+  h->h_col2act = c2a;
+  h->grid_ok = true;
+  h->ran = false;
+  return LGPU_OK;
+}
+
+int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean, const float *sprd, int nvars,
+                   const lgpu_statevar *vars) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->grid_ok) return fail(h, LGPU_ERR_ORDER, "set_state before set_grid");
+  if (!state || !mean || !sprd || !vars || nvars <= 0 || ns <= 0) return fail(h, LGPU_ERR_ARG, "set_state: bad arguments");
+  if (k < 2) return fail(h, LGPU_ERR_ARG, "ensemble size must be >= 2");
+  if (k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "ensemble size > 64 is not supported by this build");
+  // slab -> (variable, level); every slab must belong to exactly one variable
+  std::vector<int> sv(ns, -1), sl(ns, -1);
+  std::vector<float> inc(nvars), lb(nvars), ub(nvars);
+  for (int v = 0; v < nvars; v++) {
+    const auto &x = vars[v];
+    if (x.levels <= 0 || x.grid_s_idx < 0 || x.grid_s_idx + x.levels > ns)
+      return fail(h, LGPU_ERR_ARG, "set_state: variable " + std::to_string(v) + " slab range outside [0, ns)");
+    for (int l = 0; l < x.levels; l++) {
+      if (sv[x.grid_s_idx + l] >= 0) return fail(h, LGPU_ERR_ARG, "set_state: overlapping variable slabs");
+      sv[x.grid_s_idx + l] = v;
+      sl[x.grid_s_idx + l] = l;
+    }
+    inc[v] = x.ana_inc_max;
+    lb[v] = x.ana_bounds[0];
+    ub[v] = x.ana_bounds[1];
+  }
+  for (int s = 0; s < ns; s++)
+    if (sv[s] < 0) return fail(h, LGPU_ERR_ARG, "set_state: slab " + std::to_string(s) + " belongs to no variable");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t nx = (size_t)h->ncol * ns * k, nm = (size_t)h->ncol * ns;
+  CK(h->buf[B_BKG].ensure(nx * 4), "alloc state");
+  CK(h->buf[B_ANA].ensure(nx * 4), "alloc analysis");
+  CK(h->buf[B_MEANB].ensure(nm * 4), "alloc mean");
+  CK(h->buf[B_SPRDB].ensure(nm * 4), "alloc sprd");
+  CK(h->buf[B_MEANA].ensure(nm * 4), "alloc mean_a");
+  CK(h->buf[B_SPRDA].ensure(nm * 4), "alloc sprd_a");
+  CK(h->buf[B_SLABVAR].ensure(ns * 4), "alloc slabvar");
+  CK(h->buf[B_SLABLEV].ensure(ns * 4), "alloc slablev");
+  CK(h->buf[B_VARINC].ensure(nvars * 4), "alloc varinc");
+  CK(h->buf[B_VARLB].ensure(nvars * 4), "alloc varlb");
+  CK(h->buf[B_VARUB].ensure(nvars * 4), "alloc varub");
+  CK(cudaMemcpyAsync(h->buf[B_BKG].p, state, nx * 4, cudaMemcpyHostToDevice, h->st), "H2D state");
+  CK(cudaMemcpyAsync(h->buf[B_MEANB].p, mean, nm * 4, cudaMemcpyHostToDevice, h->st), "H2D mean");
+  CK(cudaMemcpyAsync(h->buf[B_SPRDB].p, sprd, nm * 4, cudaMemcpyHostToDevice, h->st), "H2D sprd");
+  CK(cudaMemcpyAsync(h->buf[B_SLABVAR].p, sv.data(), ns * 4, cudaMemcpyHostToDevice, h->st), "H2D sv");
+  CK(cudaMemcpyAsync(h->buf[B_SLABLEV].p, sl.data(), ns * 4, cudaMemcpyHostToDevice, h->st), "H2D sl");
+  CK(cudaMemcpyAsync(h->buf[B_VARINC].p, inc.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D inc");
+  CK(cudaMemcpyAsync(h->buf[B_VARLB].p, lb.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D lb");
+  CK(cudaMemcpyAsync(h->buf[B_VARUB].p, ub.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D ub");
+  CK(cudaStreamSynchronize(h->st), "set_state sync");
+  h->k = k;
+  h->ns = ns;
+  h->kp = (k + 3) & ~3;
+  h->vars.assign(vars, vars + nvars);
+  h->state_ok = true;
+  h->ran = false;
+  return LGPU_OK;
+}
+
+int lgpu_set_obs(lgpu_handle *h, int nobs, const lgpu_obs *o, const float *hx, const float *hx_mean) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->state_ok) return fail(h, LGPU_ERR_ORDER, "set_obs before set_state (the ensemble size is needed)");
+  if (nobs < 0 || (nobs > 0 && (!o || !hx || !hx_mean || !o->lat || !o->lon || !o->zdim || !o->time || !o->val ||
+                                 !o->err || !o->obsid || !o->platid)))
+    return fail(h, LGPU_ERR_ARG, "set_obs: bad arguments");
+  for (int i = 0; i < nobs; i++)
+    if (!(o->err[i] > 0.0f)) return fail(h, LGPU_ERR_ARG, "set_obs: observation error must be > 0 at obs " + std::to_string(i));
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t n = std::max(nobs, 1), k = h->k;
+  int bi[8] = {B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID};
+  const void *src[8] = {o ? o->lat : nullptr, o ? o->lon : nullptr, o ? o->zdim : nullptr, o ? o->time : nullptr,
+                        o ? o->val : nullptr, o ? o->err : nullptr, o ? o->obsid : nullptr, o ? o->platid : nullptr};
+  for (int q = 0; q < 8; q++) {
+    CK(h->buf[bi[q]].ensure(n * 4), "alloc obs");
+    if (nobs > 0) CK(cudaMemcpyAsync(h->buf[bi[q]].p, src[q], (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D obs");
+  }
+  CK(h->buf[B_HX].ensure(n * k * 4), "alloc hx");
+  CK(h->buf[B_HXM].ensure(n * 4), "alloc hx_mean");
+  if (nobs > 0) {
+    CK(cudaMemcpyAsync(h->buf[B_HX].p, hx, (size_t)nobs * k * 4, cudaMemcpyHostToDevice, h->st), "H2D hx");
+    CK(cudaMemcpyAsync(h->buf[B_HXM].p, hx_mean, (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D hxm");
+  }
+  CK(cudaStreamSynchronize(h->st), "set_obs sync");
+  h->nobs = nobs;
+  h->obs_ok = true;
+  h->ran = false;
+  return LGPU_OK;
+}
+
+// letkf_solver_run (src/letkf_solver.F90:150-389)
+int lgpu_solver_run(lgpu_handle *h) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->solver_ok) return fail(h, LGPU_ERR_ORDER, "solver_run before solver_init");
+  if (!h->loc_ok) return fail(h, LGPU_ERR_ORDER, "solver_run before loc_init");
+  if (!h->grid_ok || !h->state_ok || !h->obs_ok) return fail(h, LGPU_ERR_ORDER, "solver_run before grid/state/obs were set");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const int k = h->k, kp = h->kp, ns = h->ns, G = h->loc.groups;
+  if (h->loc.cls == LOC_OCEAN && h->loc.vtloc_surf == 1) {
+    if (h->bkg_t_var < 0 || h->bkg_t_var >= (int)h->vars.size())
+      return fail(h, LGPU_ERR_CONFIG, "vtloc_surf.bkg_t_var does not name a state variable");
+    h->loc.bkg_t_idx = h->vars[h->bkg_t_var].grid_s_idx;
+    h->loc.bkg_t_len = h->vars[h->bkg_t_var].levels;
+  }
+  if (h->loc.cls == LOC_VTGC) {
+    int maxlev = 0;
+    for (auto &v : h->vars) maxlev = std::max(maxlev, v.levels);
+    if (maxlev > G) return fail(h, LGPU_ERR_CONFIG, "loc_vtgc: a variable has more levels than level depths given");
+    CK(h->buf[B_LEVDEPTH].ensure(sizeof(float) * G), "alloc lev");
+    CK(cudaMemcpyAsync(h->buf[B_LEVDEPTH].p, h->lev_depth.data(), sizeof(float) * G, cudaMemcpyHostToDevice, h->st), "H2D lev");
+    h->loc.lev_depth = h->buf[B_LEVDEPTH].as<float>();
+  }
+  const size_t nobs = std::max(h->nobs, 1);
+  const long long units = (long long)h->nact * G;
+  if (units > 0x7fffffffLL) return fail(h, LGPU_ERR_CAPACITY, "too many (column, group) units");
+  h->nunits = (int)units;
+  // ---- buffers
+  CK(h->buf[B_SATOBS].ensure(sizeof(int) * std::max<size_t>(1, h->sat_obs.size())), "alloc");
+  CK(h->buf[B_SATPLATS].ensure(sizeof(int) * std::max<size_t>(1, h->sat_plats.size())), "alloc");
+  if (!h->sat_obs.empty())
+    CK(cudaMemcpyAsync(h->buf[B_SATOBS].p, h->sat_obs.data(), 4 * h->sat_obs.size(), cudaMemcpyHostToDevice, h->st), "H2D");
+  if (!h->sat_plats.empty())
+    CK(cudaMemcpyAsync(h->buf[B_SATPLATS].p, h->sat_plats.data(), 4 * h->sat_plats.size(), cudaMemcpyHostToDevice, h->st), "H2D");
+  CK(h->buf[B_CELL].ensure(4 * nobs), "alloc");
+  CK(h->buf[B_COUNT].ensure(4 * (size_t)h->ncell), "alloc");
+  CK(h->buf[B_FILL].ensure(4 * (size_t)h->ncell), "alloc");
+  CK(h->buf[B_POSTMP].ensure(4 * nobs), "alloc");
+  CK(h->buf[B_ORDER].ensure(4 * nobs), "alloc");
+  CK(h->buf[B_ATMP].ensure(16 * nobs), "alloc");
+  CK(h->buf[B_BTMP].ensure(16 * nobs), "alloc");
+  CK(h->buf[B_SA].ensure(16 * nobs), "alloc");
+  CK(h->buf[B_SB].ensure(16 * nobs), "alloc");
+  CK(h->buf[B_SHX].ensure(4 * nobs * kp), "alloc sorted hx");
+  CK(h->buf[B_SIDX].ensure(4 * nobs), "alloc");
+  CK(h->buf[B_CSTART].ensure(4 * ((size_t)h->ncell + 1)), "alloc");
+  CK(h->buf[B_CP].ensure(sizeof(ColPar) * (size_t)h->ncol), "alloc");
+  CK(h->buf[B_G].ensure(4 * std::max<size_t>(1, (size_t)units) * k * (k + 1)), "alloc Gram");
+  CK(h->buf[B_T].ensure(4 * std::max<size_t>(1, (size_t)units) * k * k), "alloc transforms");
+  CK(h->buf[B_NKEPT].ensure(4 * std::max<size_t>(1, (size_t)units)), "alloc");
+  CK(h->buf[B_DMAXHZ].ensure(4 * (size_t)h->ncol), "alloc");
+  CK(h->buf[B_DOBSC].ensure(4 * (size_t)h->ncol), "alloc");
+  CK(h->buf[B_DLGC].ensure(4 * (size_t)h->ncol * G), "alloc");
+  CK(h->buf[B_DLGL].ensure(4 * (size_t)h->ncol * G), "alloc");
+  CK(h->buf[B_STATUS].ensure(16), "alloc");
+  ObsSorted os;
+  os.A = h->buf[B_SA].as<float4>();
+  os.B = h->buf[B_SB].as<float4>();
+  os.hx = h->buf[B_SHX].as<float>();
+  os.idx = h->buf[B_SIDX].as<int>();
+  os.cell_start = h->buf[B_CSTART].as<int>();
+  int launches = 0;
+  cudaStream_t st = h->st;
+  CK(cudaEventRecord(h->ev[0], st), "event");
+  // ---- observation index (kd_init counterpart) ----
+  CK(launch_obs_index(st, h->nobs, k, kp, h->buf[B_OLAT].as<float>(), h->buf[B_OLON].as<float>(),
+                      h->buf[B_OZ].as<float>(), h->buf[B_OTIME].as<float>(), h->buf[B_OVAL].as<float>(),
+                      h->buf[B_OERR].as<float>(), h->buf[B_OOBSID].as<int>(), h->buf[B_OPLATID].as<int>(),
+                      h->buf[B_HX].as<float>(), h->buf[B_HXM].as<float>(), h->buf[B_SATOBS].as<int>(),
+                      (int)h->sat_obs.size(), h->buf[B_SATPLATS].as<int>(), (int)h->sat_plats.size(),
+                      h->buf[B_GEOM].as<IndexGeom>(), h->ncell, h->buf[B_CELL].as<int>(), h->buf[B_COUNT].as<int>(),
+                      h->buf[B_FILL].as<int>(), h->buf[B_POSTMP].as<int>(), h->buf[B_ORDER].as<int>(),
+                      h->buf[B_ATMP].as<float4>(), h->buf[B_BTMP].as<float4>(), os, &launches),
+     "observation index");
+  CK(cudaEventRecord(h->ev[1], st), "event");
+  // ---- per-column parameters ----
+  CK(launch_col_prep(st, h->ncol, h->buf[B_LAT].as<float>(), h->buf[B_LON].as<float>(), h->buf[B_MASK].as<int>(),
+                     h->buf[B_MEANB].as<float>(), ns, h->loc, h->buf[B_CP].as<ColPar>(),
+                     h->buf[B_DMAXHZ].as<float>(), &launches),
+     "column prep");
+  CK(cudaMemsetAsync(h->buf[B_DOBSC].p, 0, 4 * (size_t)h->ncol, st), "memset");
+  CK(cudaMemsetAsync(h->buf[B_DLGC].p, 0, 4 * (size_t)h->ncol * G, st), "memset");
+  CK(cudaMemsetAsync(h->buf[B_DLGL].p, 0, 4 * (size_t)h->ncol * G, st), "memset");
+  CK(cudaMemsetAsync(h->buf[B_STATUS].p, 0, 16, st), "memset");
+  CK(cudaEventRecord(h->ev[2], st), "event");
+  // ---- search + localize + Gram ----
+  GramArgs ga;
+  ga.nunits = h->nunits;
+  ga.groups = G;
+  ga.k = k;
+  ga.kp = kp;
+  ga.active = h->buf[B_ACTIVE].as<int>();
+  ga.cp = h->buf[B_CP].as<ColPar>();
+  ga.loc = h->loc;
+  ga.obs = os;
+  ga.geom = h->buf[B_GEOM].as<IndexGeom>();
+  ga.G = h->buf[B_G].as<float>();
+  ga.nkept = h->buf[B_NKEPT].as<int>();
+  ga.diag_obscount = h->buf[B_DOBSC].as<float>();
+  ga.diag_lg_obscount = h->buf[B_DLGC].as<float>();
+  ga.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
+  ga.ncol = h->ncol;
+  CK(launch_gram(st, ga, &launches), "gram kernel");
+  CK(cudaEventRecord(h->ev[3], st), "event");
+  // ---- eigensolve + transform ----
+  EigArgs ea;
+  ea.nunits = h->nunits;
+  ea.k = k;
+  ea.infl = 1.0f;   // letkf_core_solve is called with infl = 1.0 (src/letkf_solver.F90:279)
+  ea.G = h->buf[B_G].as<float>();
+  ea.nkept = h->buf[B_NKEPT].as<int>();
+  ea.T = h->buf[B_T].as<float>();
+  ea.status = h->buf[B_STATUS].as<int>();
+  CK(launch_eig(st, ea, &launches), "eigen kernel");
+  CK(cudaEventRecord(h->ev[4], st), "event");
+  // ---- update + epilogue ----
+  UpdateArgs ua;
+  ua.ncol = h->ncol;
+  ua.ns = ns;
+  ua.k = k;
+  ua.groups = G;
+  ua.mask = h->buf[B_MASK].as<int>();
+  ua.col2act = h->buf[B_COL2ACT].as<int>();
+  ua.cp = h->buf[B_CP].as<ColPar>();
+  ua.loc_cls = h->loc.cls;
+  ua.vtloc_surf = h->loc.vtloc_surf;
+  ua.slab_var = h->buf[B_SLABVAR].as<int>();
+  ua.slab_lev = h->buf[B_SLABLEV].as<int>();
+  ua.var_inc_max = h->buf[B_VARINC].as<float>();
+  ua.var_lb = h->buf[B_VARLB].as<float>();
+  ua.var_ub = h->buf[B_VARUB].as<float>();
+  ua.bkg = h->buf[B_BKG].as<float>();
+  ua.mean_b = h->buf[B_MEANB].as<float>();
+  ua.sprd_b = h->buf[B_SPRDB].as<float>();
+  ua.T = h->buf[B_T].as<float>();
+  ua.nkept = h->buf[B_NKEPT].as<int>();
+  ua.ana = h->buf[B_ANA].as<float>();
+  ua.mean_a = h->buf[B_MEANA].as<float>();
+  ua.sprd_a = h->buf[B_SPRDA].as<float>();
+  ua.rtps = h->scfg.rtps;
+  ua.rtpp = h->scfg.rtpp;
+  ua.mul = h->scfg.mul;
+  ua.status = h->buf[B_STATUS].as<int>();
+  CK(launch_update(st, ua, &launches), "update kernel");
+  CK(cudaEventRecord(h->ev[5], st), "event");
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, h->buf[B_STATUS].p, 4, cudaMemcpyDeviceToHost, st), "D2H status");
+  CK(cudaStreamSynchronize(st), "solver_run");
+  float ms[5];
+  for (int i = 0; i < 5; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
+  h->tim.index_ms = ms[0];
+  h->tim.prep_ms = ms[1];
+  h->tim.gram_ms = ms[2];
+  h->tim.eig_ms = ms[3];
+  h->tim.update_ms = ms[4];
+  CK(cudaEventElapsedTime(&h->tim.total_ms, h->ev[0], h->ev[5]), "timing");
+  h->tim.launches = launches;
+  h->tim.units = h->nunits;
+  h->tim.kept_pairs = -1;
+  h->ran = true;
+  if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
+  if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");
+  if (status & 4) return fail(h, LGPU_ERR_NONFINITE, "non-finite analysis mean or spread");
+  return LGPU_OK;
+}
+
+int lgpu_get_state(lgpu_handle *h, float *state, float *mean, float *sprd) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->ran) return fail(h, LGPU_ERR_ORDER, "get_state before a successful solver_run");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t nx = (size_t)h->ncol * h->ns * h->k, nm = (size_t)h->ncol * h->ns;
+  if (state) CK(cudaMemcpyAsync(state, h->buf[B_ANA].p, nx * 4, cudaMemcpyDeviceToHost, h->st), "D2H state");
+  if (mean) CK(cudaMemcpyAsync(mean, h->buf[B_MEANA].p, nm * 4, cudaMemcpyDeviceToHost, h->st), "D2H mean");
+  if (sprd) CK(cudaMemcpyAsync(sprd, h->buf[B_SPRDA].p, nm * 4, cudaMemcpyDeviceToHost, h->st), "D2H sprd");
+  CK(cudaStreamSynchronize(h->st), "get_state");
+  return LGPU_OK;
+}
+
+int lgpu_get_diag(lgpu_handle *h, float *maxhz, float *obscount, float *lg_obscount, float *lg_obsloc) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->ran) return fail(h, LGPU_ERR_ORDER, "get_diag before a successful solver_run");
+  if (!h->scfg.save_diag) return fail(h, LGPU_ERR_CONFIG, "save_diag is off");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t n = h->ncol, ng = (size_t)h->ncol * h->loc.groups;
+  if (maxhz) CK(cudaMemcpyAsync(maxhz, h->buf[B_DMAXHZ].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  if (obscount) CK(cudaMemcpyAsync(obscount, h->buf[B_DOBSC].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  if (lg_obscount) CK(cudaMemcpyAsync(lg_obscount, h->buf[B_DLGC].p, ng * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  if (lg_obsloc) CK(cudaMemcpyAsync(lg_obsloc, h->buf[B_DLGL].p, ng * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  CK(cudaStreamSynchronize(h->st), "get_diag");
+  return LGPU_OK;
+}
+
+int lgpu_get_timings(const lgpu_handle *h, lgpu_timings *t) {
+  if (!h || !t) return LGPU_ERR_ARG;
+  *t = h->tim;
+  return LGPU_OK;
+}
+
+// letkf_solver_final (src/letkf_solver.F90:397-527) minus the NetCDF writer:
+// release the per-run work buffers.
+int lgpu_solver_final(lgpu_handle *h) {
+  if (!h) return LGPU_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->st);
+  int work[] = {B_CELL, B_COUNT, B_FILL, B_POSTMP, B_ORDER, B_ATMP, B_BTMP, B_G, B_T};
+  for (int b : work) h->buf[b].release();
+  return LGPU_OK;
+}
+
+int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap, int *n, int *ncand) {
+  if (!h || !n) return LGPU_ERR_ARG;
+  if (!h->ran) return fail(h, LGPU_ERR_ORDER, "get_obslist before a successful solver_run");
+  if (ij < 0 || ij >= h->ncol || group < 0 || group >= h->loc.groups || cap < 0)
+    return fail(h, LGPU_ERR_ARG, "get_obslist: index out of range");
+  *n = 0;
+  if (ncand) *ncand = 0;
+  if (h->h_col2act[ij] < 0) return LGPU_OK;   // masked column: no search (src/letkf_solver.F90:207)
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const int lcap = std::max(h->nobs, 1);
+  CK(h->buf[B_LIST_IDX].ensure(4 * (size_t)lcap), "alloc");
+  CK(h->buf[B_LIST_R].ensure(4 * (size_t)lcap), "alloc");
+  CK(h->buf[B_LIST_CNT].ensure(16), "alloc");
+  ObsSorted os;
+  os.A = h->buf[B_SA].as<float4>();
+  os.B = h->buf[B_SB].as<float4>();
+  os.hx = h->buf[B_SHX].as<float>();
+  os.idx = h->buf[B_SIDX].as<int>();
+  os.cell_start = h->buf[B_CSTART].as<int>();
+  CK(launch_obslist(h->st, ij, group, group, h->buf[B_CP].as<ColPar>() + ij, h->loc, os,
+                    h->buf[B_GEOM].as<IndexGeom>(), lcap, h->buf[B_LIST_IDX].as<int>(), h->buf[B_LIST_R].as<float>(),
+                    h->buf[B_LIST_CNT].as<int>()),
+     "obslist kernel");
+  int cnt[2] = {0, 0};
+  CK(cudaMemcpyAsync(cnt, h->buf[B_LIST_CNT].p, 8, cudaMemcpyDeviceToHost, h->st), "D2H");
+  CK(cudaStreamSynchronize(h->st), "obslist");
+  const int m = std::min(cnt[0], lcap);
+  std::vector<int> li(m);
+  std::vector<float> lr(m);
+  if (m > 0) {
+    CK(cudaMemcpy(li.data(), h->buf[B_LIST_IDX].p, 4 * (size_t)m, cudaMemcpyDeviceToHost), "D2H");
+    CK(cudaMemcpy(lr.data(), h->buf[B_LIST_R].p, 4 * (size_t)m, cudaMemcpyDeviceToHost), "D2H");
+  }
+  std::vector<int> ord(m);
+  for (int i = 0; i < m; i++) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](int a, int b) { return li[a] < li[b]; });
+  for (int i = 0; i < m && i < cap; i++) {
+    if (idx) idx[i] = li[ord[i]];
+    if (rloc) rloc[i] = lr[ord[i]];
+  }
+  *n = cnt[0];
+  if (ncand) *ncand = cnt[1];
+  return LGPU_OK;
+}
+
+int lgpu_host_alloc(size_t bytes, void **ptr) {
+  if (!ptr) return LGPU_ERR_ARG;
+  *ptr = nullptr;
+  cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 16);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? LGPU_ERR_NOMEM : LGPU_ERR_CUDA;
+  return LGPU_OK;
+}
+
+int lgpu_host_free(void *ptr) {
+  if (ptr && cudaFreeHost(ptr) != cudaSuccess) return LGPU_ERR_CUDA;
+  return LGPU_OK;
+}
+
+int lgpu_flush_l2(lgpu_handle *h, size_t bytes) {
+  if (!h) return LGPU_ERR_ARG;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(h->buf[B_FLUSH].ensure(bytes), "alloc flush buffer");
+  static int salt = 0;
+  CK(cudaMemsetAsync(h->buf[B_FLUSH].p, (++salt) & 0xff, bytes, h->st), "flush");
+  CK(cudaStreamSynchronize(h->st), "flush sync");
+  return LGPU_OK;
+}
+
+int lgpu_debug_metric(lgpu_handle *h, int n, const float *lat1, const float *lon1, const float *lat2,
+                      const float *lon2, float *dist) {
+  if (!h || n < 0 || (n > 0 && (!lat1 || !lon1 || !lat2 || !lon2 || !dist))) return LGPU_ERR_ARG;
+  if (n == 0) return LGPU_OK;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  float *d = nullptr;
+  CK(cudaMalloc(&d, 5 * sizeof(float) * (size_t)n), "alloc");
+  const float *srcs[4] = {lat1, lon1, lat2, lon2};
+  for (int q = 0; q < 4; q++)
+    cudaMemcpyAsync(d + (size_t)q * n, srcs[q], 4 * (size_t)n, cudaMemcpyHostToDevice, h->st);
+  cudaError_t e = launch_debug_metric(h->st, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dist, d + 4 * (size_t)n, 4 * (size_t)n, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(h, e, "debug_metric");
+  return LGPU_OK;
+}
+
+int lgpu_debug_gc(lgpu_handle *h, int n, const float *z, const float *L, float *gc) {
+  if (!h || n < 0 || (n > 0 && (!z || !L || !gc))) return LGPU_ERR_ARG;
+  if (n == 0) return LGPU_OK;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  float *d = nullptr;
+  CK(cudaMalloc(&d, 4 * sizeof(float) * (size_t)n), "alloc");
+  cudaMemcpyAsync(d, z, 4 * (size_t)n, cudaMemcpyHostToDevice, h->st);
+  cudaMemcpyAsync(d + n, L, 4 * (size_t)n, cudaMemcpyHostToDevice, h->st);
+  cudaError_t e = launch_debug_gc(h->st, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n);
+  // gc receives 2n values: the fast evaluation then the exact REAL(8) one
+  if (e == cudaSuccess) e = cudaMemcpyAsync(gc, d + 2 * (size_t)n, 8 * (size_t)n, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(h, e, "debug_gc");
+  return LGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,236 @@
+// lgpu_eig.cu -- batched symmetric eigensolve and LETKF transform, one warp
+// per (column, group) unit, FP32.
+//
+// Replaces src/letkf_core.F90:100-141: with A = G + (k-1)/infl I (G from
+// the Gram stage, upper triangle as ssyev('V','U') reads it),
+//   Pa   = V diag(1/lambda) V^T
+//   W    = V diag(sqrt((k-1)/lambda)) V^T
+//   wbar = Pa b               (b = Yb^T R^-1 rho dep, computed in the Gram stage)
+//   T    = W + wbar 1^T
+// The eigendecomposition is Householder tridiagonalisation (Golub & Van Loan,
+// Matrix Computations, 4th ed., Alg. 8.3.1) followed by the implicit-shift
+// QL iteration with Wilkinson shifts on the tridiagonal matrix (the
+// tql2 scheme of Bowdler, Martin, Reinsch & Wilkinson, Numer. Math. 11,
+// 1968), accumulating the rotations into Z, and back-transformation
+// V = Q Z.  Rows of the k x k work matrices are spread over the 32 lanes;
+// the QL scalar recurrence is evaluated redundantly by every lane (shared
+// memory broadcasts) with lane 0 as the only writer.
+#include "lgpu_internal.cuh"
+
+namespace lgpu {
+
+namespace {
+
+__device__ __forceinline__ float wsum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__host__ __device__ __forceinline__ int eig_floats_per_warp(int k) {
+  const int ld = k + 1;
+  return 2 * k * ld + 8 * k + 8;
+}
+
+__global__ void k_eig(EigArgs a, int wpb) {
+  extern __shared__ __align__(16) float sm[];
+  const int k = a.k, ld = k + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int unit = blockIdx.x * wpb + warp;
+  if (unit >= a.nunits) return;           // whole warps exit; no block-level barriers below
+  if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
+  float *A = sm + (size_t)warp * eig_floats_per_warp(k);
+  float *Z = A + k * ld;
+  float *d = Z + k * ld;
+  float *e = d + k;
+  float *tau = e + k;
+  float *bv = tau + k;
+  float *p = bv + k;
+  float *w = p + k;
+  float *fl = w + k;
+  float *gl = fl + k;
+  const float *G = a.G + (size_t)unit * k * (k + 1);
+  // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
+  const float shift = (float)(k - 1) * 1.0f / a.infl;
+  for (int t = lane; t < k * k; t += 32) {
+    const int i = t / k, j = t % k;
+    float v = (i <= j) ? G[i * (k + 1) + j] : G[j * (k + 1) + i];
+    if (i == j) v += shift;
+    A[i * ld + j] = v;
+  }
+  for (int i = lane; i < k; i += 32) bv[i] = G[i * (k + 1) + k];
+  __syncwarp();
+
+  // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j]
+  for (int j = 0; j < k - 2; j++) {
+    const int m = k - j - 1;                 // length of x = A[j+1:, j]
+    float s = 0.0f;
+    for (int r = lane; r < m; r += 32) { float x = A[(j + 1 + r) * ld + j]; s += x * x; }
+    const float sig = wsum(s);
+    const float x0 = A[(j + 1) * ld + j];
+    const float s1 = sig - x0 * x0;
+    if (!(s1 > 1e-30f * sig) || sig == 0.0f) {
+      if (lane == 0) { tau[j] = 0.0f; e[j] = x0; d[j] = A[j * ld + j]; }
+      __syncwarp();
+      continue;
+    }
+    const float alpha = -copysignf(sqrtf(sig), x0);
+    const float v0 = x0 - alpha;
+    const float t = 2.0f / (v0 * v0 + s1);
+    __syncwarp();
+    if (lane == 0) { A[(j + 1) * ld + j] = v0; tau[j] = t; e[j] = alpha; d[j] = A[j * ld + j]; }
+    __syncwarp();
+    // p = t * A22 v
+    for (int r = lane; r < m; r += 32) {
+      const float *row = A + (j + 1 + r) * ld + (j + 1);
+      float acc = 0.0f;
+      for (int c = 0; c < m; c++) acc = __fmaf_rn(row[c], A[(j + 1 + c) * ld + j], acc);
+      p[r] = t * acc;
+    }
+    __syncwarp();
+    float pv = 0.0f;
+    for (int r = lane; r < m; r += 32) pv = __fmaf_rn(p[r], A[(j + 1 + r) * ld + j], pv);
+    const float beta = 0.5f * t * wsum(pv);
+    for (int r = lane; r < m; r += 32) w[r] = p[r] - beta * A[(j + 1 + r) * ld + j];
+    __syncwarp();
+    // A22 -= v w^T + w v^T
+    for (int r = lane; r < m; r += 32) {
+      float *row = A + (j + 1 + r) * ld + (j + 1);
+      const float vr = A[(j + 1 + r) * ld + j], wr = w[r];
+      for (int c = 0; c < m; c++) {
+        const float vc = A[(j + 1 + c) * ld + j], wc = w[c];
+        row[c] = row[c] - __fmaf_rn(vr, wc, wr * vc);
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    if (k >= 2) {
+      d[k - 2] = A[(k - 2) * ld + (k - 2)];
+      e[k - 2] = A[(k - 1) * ld + (k - 2)];
+    }
+    d[k - 1] = A[(k - 1) * ld + (k - 1)];
+    e[k - 1] = 0.0f;
+  }
+  // Z = I
+  for (int t = lane; t < k * ld; t += 32) { const int i = t / ld, j = t % ld; Z[t] = (i == j) ? 1.0f : 0.0f; }
+  __syncwarp();
+
+  // ---- implicit-shift QL on (d, e)
+  int bad = 0;
+  for (int l = 0; l < k; l++) {
+    int iter = 0;
+    for (;;) {
+      int m = l;
+      for (; m < k - 1; m++) {
+        const float dd = fabsf(d[m]) + fabsf(d[m + 1]);
+        if (fabsf(e[m]) <= 1.1920929e-7f * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 60) { bad = 1; break; }
+      float g = (d[l + 1] - d[l]) / (2.0f * e[l]);
+      float r = sqrtf(g * g + 1.0f);
+      g = d[m] - d[l] + e[l] / (g + copysignf(r, g));
+      float s = 1.0f, c = 1.0f, pp = 0.0f;
+      bool deflate = false;
+      for (int i = m - 1; i >= l; i--) {
+        // every lane reads before lane 0 overwrites e[i+1], d[i+1]
+        const float ei = e[i], di = d[i], di1 = d[i + 1];
+        const float f = s * ei, b = c * ei;
+        r = sqrtf(f * f + g * g);
+        __syncwarp();
+        if (r == 0.0f) {
+          if (lane == 0) { e[i + 1] = 0.0f; d[i + 1] = di1 - pp; e[m] = 0.0f; }
+          deflate = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = di1 - pp;
+        const float rr = (di - g) * s + 2.0f * c * b;
+        pp = s * rr;
+        if (lane == 0) { e[i + 1] = r; d[i + 1] = g + pp; }
+        g = c * rr - b;
+        for (int q = lane; q < k; q += 32) {
+          const float zi = Z[q * ld + i], zf = Z[q * ld + i + 1];
+          Z[q * ld + i + 1] = s * zi + c * zf;
+          Z[q * ld + i] = c * zi - s * zf;
+        }
+      }
+      __syncwarp();
+      if (deflate) continue;
+      if (lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
+      __syncwarp();
+    }
+    if (bad) break;
+  }
+
+  // ---- back-transformation V = Q Z (reflectors applied last-to-first)
+  for (int j = k - 3; j >= 0; j--) {
+    const float t = tau[j];
+    if (t == 0.0f) continue;
+    const int m = k - j - 1;
+    for (int c = lane; c < k; c += 32) {
+      float dot = 0.0f;
+      for (int r = 0; r < m; r++) dot = __fmaf_rn(A[(j + 1 + r) * ld + j], Z[(j + 1 + r) * ld + c], dot);
+      dot *= t;
+      for (int r = 0; r < m; r++) Z[(j + 1 + r) * ld + c] -= A[(j + 1 + r) * ld + j] * dot;
+    }
+  }
+  __syncwarp();
+
+  // ---- spectral functions: f = sqrt((k-1)/lambda), g = 1/lambda
+  //      (src/letkf_core.F90:111-113, :128-131)
+  for (int l = lane; l < k; l += 32) {
+    const float lam = d[l];
+    if (!(lam > 0.0f)) bad |= 2;
+    fl[l] = sqrtf((float)(k - 1) / lam);
+    gl[l] = 1.0f / lam;
+  }
+  __syncwarp();
+  // s_l = g_l * (V^T b)_l
+  for (int l = lane; l < k; l += 32) {
+    float acc = 0.0f;
+    for (int q = 0; q < k; q++) acc = __fmaf_rn(Z[q * ld + l], bv[q], acc);
+    p[l] = gl[l] * acc;
+  }
+  __syncwarp();
+  // wbar_i = sum_l V[i][l] s_l
+  for (int i = lane; i < k; i += 32) {
+    float acc = 0.0f;
+    for (int l = 0; l < k; l++) acc = __fmaf_rn(Z[i * ld + l], p[l], acc);
+    w[i] = acc;
+  }
+  // Y = V diag(f) into A (A is no longer needed)
+  __syncwarp();
+  for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] = Z[i * ld + l] * fl[l]; }
+  __syncwarp();
+  // T_ij = sum_l Y[i][l] V[j][l] + wbar_i ; lane owns columns j
+  float *T = a.T + (size_t)unit * k * k;
+  for (int j = lane; j < k; j += 32) {
+    for (int i = 0; i < k; i++) {
+      float acc = 0.0f;
+      for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], Z[j * ld + l], acc);
+      T[i * k + j] = acc + w[i];
+    }
+  }
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  if (bad && lane == 0) atomicOr(a.status, bad);
+}
+
+}  // namespace
+
+cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches) {
+  if (a.nunits <= 0) return cudaSuccess;
+  const int per = eig_floats_per_warp(a.k);
+  int wpb = 4;
+  while (wpb > 1 && (size_t)wpb * per * sizeof(float) > 96 * 1024) wpb--;
+  const size_t smem = (size_t)wpb * per * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int grid = (a.nunits + wpb - 1) / wpb;
+  k_eig<<<grid, 32 * wpb, smem, st>>>(a, wpb);
+  (*launches)++;
+  return cudaGetLastError();
+}
+
+}  // namespace lgpu

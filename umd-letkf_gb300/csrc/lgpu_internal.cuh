@@ -1,0 +1,334 @@
+// lgpu_internal.cuh -- shared device definitions of the sm_103a LETKF path:
+// the observation metric, latitude interpolation, Gaspari-Cohn weights, the
+// spatial-index geometry and the kernel parameter blocks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "letkf_gpu.h"
+
+namespace lgpu {
+
+// ---------------------------------------------------------------- limits --
+constexpr int kMaxK = LGPU_MAX_K;          // ensemble size
+constexpr int kMaxGroups = LGPU_MAX_LEVELS;
+constexpr int kNB = 180;                   // 1-degree latitude bands of the index
+constexpr int kMaxInterp = LGPU_MAX_INTERP + 2;
+
+// Localizer classes.
+enum LocClass { LOC_NOVRT = 0, LOC_OCEAN = 1, LOC_VTGC = 2 };
+
+// linearinterp_lat table after the reference's 0/90-degree padding
+// (src/letkf_loc.F90:251-294).
+struct Interp {
+  int n;
+  float lat[kMaxInterp];
+  float dist[kMaxInterp];
+};
+
+// Localizer parameters the device needs (the plugin's "device descriptor").
+struct DevLoc {
+  int cls;
+  int groups;          // maxgroups
+  Interp hz;           // novrt/vtgc: hzloc; ocean: hzloc_prof
+  Interp hz_sat;       // ocean: hzloc_sat
+  float tloc_prof, tloc_sat;
+  int vtloc_surf;      // ocean: 1 = bkg_t mixed-layer split
+  float bkg_t_delta;
+  int bkg_t_idx, bkg_t_len;
+  float vloc;          // vtgc vertical length scale
+  const float *lev_depth;  // vtgc level depths [groups] (device)
+};
+
+// ------------------------------------------------------ exact metric -----
+// The observation metric is evaluated with explicitly rounded IEEE
+// operations (no contraction) so that host and device produce identical
+// distances: sin/cos in double by exact reduction to |x| <= pi/4 and Taylor
+// polynomials, great-circle angle from the chord in float,
+// theta = 2 asin(|a - b| / 2), distance = 6371 km * theta.
+__device__ __forceinline__ void sincos_deg_exact(double a, double &s, double &c) {
+  double q = floor(__dadd_rn(__ddiv_rn(a, 90.0), 0.5));
+  double r = __dsub_rn(a, __dmul_rn(90.0, q));
+  double x = __dmul_rn(r, 0.017453292519943295);
+  double x2 = __dmul_rn(x, x);
+  double p = 2.8114572543455206e-15;
+  p = __dadd_rn(__dmul_rn(p, x2), -7.647163731819816e-13);
+  p = __dadd_rn(__dmul_rn(p, x2), 1.6059043836821613e-10);
+  p = __dadd_rn(__dmul_rn(p, x2), -2.505210838544172e-08);
+  p = __dadd_rn(__dmul_rn(p, x2), 2.7557319223985893e-06);
+  p = __dadd_rn(__dmul_rn(p, x2), -0.0001984126984126984);
+  p = __dadd_rn(__dmul_rn(p, x2), 0.008333333333333333);
+  p = __dadd_rn(__dmul_rn(p, x2), -0.16666666666666666);
+  double sn = __dadd_rn(x, __dmul_rn(x, __dmul_rn(x2, p)));
+  double u = 4.779477332387385e-14;
+  u = __dadd_rn(__dmul_rn(u, x2), -1.1470745597729725e-11);
+  u = __dadd_rn(__dmul_rn(u, x2), 2.08767569878681e-09);
+  u = __dadd_rn(__dmul_rn(u, x2), -2.755731922398589e-07);
+  u = __dadd_rn(__dmul_rn(u, x2), 2.48015873015873e-05);
+  u = __dadd_rn(__dmul_rn(u, x2), -0.001388888888888889);
+  u = __dadd_rn(__dmul_rn(u, x2), 0.041666666666666664);
+  u = __dadd_rn(__dmul_rn(u, x2), -0.5);
+  double cs = __dadd_rn(1.0, __dmul_rn(x2, u));
+  long long qi = (((long long)q % 4) + 4) % 4;
+  if (qi == 0) { s = sn; c = cs; }
+  else if (qi == 1) { s = cs; c = -sn; }
+  else if (qi == 2) { s = -sn; c = -cs; }
+  else { s = -cs; c = sn; }
+}
+
+__device__ __forceinline__ float3 unitvec_exact(float lat, float lon) {
+  double sp, cp, sl, cl;
+  sincos_deg_exact((double)lat, sp, cp);
+  sincos_deg_exact((double)lon, sl, cl);
+  return make_float3((float)__dmul_rn(cp, cl), (float)__dmul_rn(cp, sl), (float)sp);
+}
+
+__device__ __forceinline__ float asin_poly_exact(float x) {
+  float x2 = __fmul_rn(x, x);
+  float p = 0.008390335366129875f;
+  p = __fadd_rn(__fmul_rn(p, x2), 0.009761609137058258f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.01155180111527443f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.013964843936264515f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.017352763563394547f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.022372158244252205f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.0303819440305233f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.0446428582072258f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.07500000298023224f);
+  p = __fadd_rn(__fmul_rn(p, x2), 0.1666666716337204f);
+  return __fadd_rn(x, __fmul_rn(x, __fmul_rn(x2, p)));
+}
+
+// squared chord between two unit vectors
+__device__ __forceinline__ float chord2_exact(float ax, float ay, float az, float bx, float by, float bz) {
+  float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+__device__ __forceinline__ float dist_from_chord2(float c2) {
+  float h = __fmul_rn(0.5f, __fsqrt_rn(c2));
+  if (h > 1.0f) h = 1.0f;
+  float ang;
+  if (h <= 0.5f) ang = asin_poly_exact(h);
+  else ang = __fsub_rn(1.5707963705062866f,
+                       __fmul_rn(2.0f, asin_poly_exact(__fsqrt_rn(__fmul_rn(__fsub_rn(1.0f, h), 0.5f)))));
+  return __fmul_rn(12742000.0f, ang);
+}
+
+// linearinterp_lat_get_dist (src/letkf_loc.F90:302-320), REAL arithmetic
+__device__ __forceinline__ float interp_get(const Interp &t, float lat) {
+  float al = fabsf(lat);
+  int i = 0;
+  while (i < t.n - 1 && al > t.lat[i]) i++;
+  if (i == 0) return t.dist[0];
+  float d = __fdiv_rn(__fsub_rn(al, t.lat[i - 1]), __fsub_rn(t.lat[i], t.lat[i - 1]));
+  return __fadd_rn(__fmul_rn(d, t.dist[i]), __fmul_rn(__fsub_rn(1.0f, d), t.dist[i - 1]));
+}
+
+// letkf_loc_gc (src/letkf_loc.F90:348-378) exactly: REAL(8) with the
+// reference's truncated coefficients, result rounded to REAL.
+__device__ __forceinline__ float gc_exact(float z, float L) {
+  double c = __ddiv_rn((double)L, 0.5477225575051661);
+  double abs_z = (double)fabsf(z);
+  double zc = __ddiv_rn(abs_z, c);
+  double z2 = __dmul_rn(zc, zc), z3 = __dmul_rn(z2, zc), z4 = __dmul_rn(z2, z2), z5 = __dmul_rn(z4, zc);
+  double res;
+  if (abs_z >= __dmul_rn(2.0, c)) {
+    res = 0.0;
+  } else if (abs_z > c) {
+    res = __dsub_rn(__dmul_rn(0.08333, z5), __dmul_rn(0.5, z4));
+    res = __dadd_rn(res, __dmul_rn(0.625, z3));
+    res = __dadd_rn(res, __dmul_rn(1.66667, z2));
+    res = __dsub_rn(res, __dmul_rn(5.0, zc));
+    res = __dadd_rn(res, 4.0);
+    res = __dsub_rn(res, __ddiv_rn(__dmul_rn(0.66667, c), abs_z));
+  } else {
+    res = __dadd_rn(__dmul_rn(-0.25, z5), __dmul_rn(0.5, z4));
+    res = __dadd_rn(res, __dmul_rn(0.625, z3));
+    res = __dsub_rn(res, __dmul_rn(1.66667, z2));
+    res = __dadd_rn(res, 1.0);
+  }
+  return (float)res;
+}
+
+// Fast single-precision Gaspari-Cohn with the same truncated coefficients.
+// The outer branch is evaluated as Q(t)/zc with t = 2 - zc, where
+// Q(z) = z * outer(z) re-expanded about z = 2 (coefficients exact in double,
+// rounded to float), which removes the cancellation near the support edge.
+// Absolute error against gc_exact is below 4e-7 for all inputs; callers
+// re-evaluate with gc_exact when a weight lands near the 1e-4 keep threshold.
+__device__ __forceinline__ float gc_fast(float z, float inv_c) {
+  float zc = fabsf(z) * inv_c;
+  if (zc >= 2.0f) return 0.0f;
+  if (zc > 1.0f) {
+    float t = 2.0f - zc;
+    float q = 0.08333f;
+    q = __fmaf_rn(q, t, -0.49996f);
+    q = __fmaf_rn(q, t, 0.6248f);
+    q = __fmaf_rn(q, t, 0.0005299999999996974f);
+    q = __fmaf_rn(q, t, -0.0007799999999991147f);
+    q = __fmaf_rn(q, t, 0.0005999999999986017f);
+    q = __fmaf_rn(q, t, -0.0001899999999991353f);
+    return __fdiv_rn(q, zc);
+  }
+  float p = -0.25f;
+  p = __fmaf_rn(p, zc, 0.5f);
+  p = __fmaf_rn(p, zc, 0.625f);
+  p = __fmaf_rn(p, zc, -1.66667f);
+  return __fmaf_rn(p, zc * zc, 1.0f);
+}
+
+__host__ __device__ __forceinline__ float inv_c_of(float L) {
+  return (float)(0.5477225575051661 / (double)L);
+}
+
+constexpr float kKeep = 1.0e-4f;          // src/letkf_solver.F90:251
+constexpr float kGuard1 = 1.0e-6f;        // fast-GC guard band, one factor
+constexpr float kGuard2 = 3.0e-6f;        // two-factor products
+constexpr float kStdev2Max = 3.65148377f; // SQRT(40.0/3.0) in REAL, src/letkf_solver.F90:47
+
+// Per-column parameters prepared once per run.
+struct ColPar {
+  float ux, uy, uz;     // unit vector
+  float rmax;           // maxhz * stdev2max (search radius, m)
+  float L1, L2;         // horizontal GC length scales (novrt/vtgc: L1; ocean: L1 = prof, L2 = sat)
+  float ic1, ic2;       // sqrt(0.3)/L
+  float lonn;           // longitude in [0,360)
+  float dlon;           // half-width of the longitude window (deg); >= 180 means whole bands
+  int b0, b1;           // latitude band range
+  int mld;              // ocean: surface-group level count (calc_mldlvl_bkgt)
+  int pad;
+};
+
+// Localisation weight of one (column, group, observation) with exact keep
+// decisions: fast float evaluation, exact REAL(8) re-evaluation in the guard
+// band around the keep threshold.
+__device__ __forceinline__ float localize(const DevLoc &L, const ColPar &c, int gid, float dist,
+                                          float otime, float oz, float surf) {
+  switch (L.cls) {
+  case LOC_OCEAN: {
+    // src/subclass.letkf_localizer/letkf_loc_ocean.F90:483-504
+    bool s = surf != 0.0f;
+    if (s && gid == 1) return 0.0f;
+    float Lh = s ? c.L2 : c.L1, ic = s ? c.ic2 : c.ic1, tl = s ? L.tloc_sat : L.tloc_prof;
+    float r = gc_fast(dist, ic);
+    if (tl > 0.0f) {
+      float rt = gc_fast(otime, inv_c_of(tl));
+      float p = r * rt;
+      if (fabsf(p - kKeep) <= kGuard2) p = gc_exact(dist, Lh) * gc_exact(otime, tl);
+      return p;
+    }
+    if (fabsf(r - kKeep) <= kGuard1) r = gc_exact(dist, Lh);
+    return r;
+  }
+  case LOC_VTGC: {
+    float rh = gc_fast(dist, c.ic1);
+    float dz = fabsf(oz - L.lev_depth[gid]);
+    float rv = gc_fast(dz, inv_c_of(L.vloc));
+    float p = rh * rv;
+    if (fabsf(p - kKeep) <= kGuard2) p = gc_exact(dist, c.L1) * gc_exact(dz, L.vloc);
+    return p;
+  }
+  default: {
+    // src/subclass.letkf_localizer/letkf_loc_novrt.F90:181
+    float r = gc_fast(dist, c.ic1);
+    if (fabsf(r - kKeep) <= kGuard1) r = gc_exact(dist, c.L1);
+    return r;
+  }
+  }
+}
+
+// -------------------------------------------------- index geometry -------
+// Observations are bucketed in 1-degree latitude bands; band b holds
+// nlon[b] equal longitude cells (about 1 degree wide at the band's poleward
+// edge).  Cell ids run band-major, so a longitude window of a band is a
+// contiguous run of cells and of sorted observations.
+struct IndexGeom {
+  int nlon[kNB];
+  int off[kNB + 1];
+};
+
+__host__ __device__ __forceinline__ int band_of(float lat) {
+  int b = (int)floorf(lat + 90.0f);
+  return b < 0 ? 0 : (b >= kNB ? kNB - 1 : b);
+}
+
+__host__ __device__ __forceinline__ float norm_lon(float lon) {
+  float l = fmodf(lon, 360.0f);
+  if (l < 0.0f) l += 360.0f;
+  if (l >= 360.0f) l -= 360.0f;
+  return l;
+}
+
+// ----------------------------------------------------- kernel launchers --
+struct ObsSorted {
+  float4 *A;       // (ux, uy, uz, err)
+  float4 *B;       // (dep, time, zdim, surf)
+  float *hx;       // [nobs][KP] perturbations, zero padded
+  int *idx;        // original observation index
+  int *cell_start; // [ncell + 1]
+};
+
+cudaError_t launch_obs_index(cudaStream_t st, int nobs, int k, int kp, const float *lat, const float *lon,
+                             const float *zdim, const float *time, const float *val, const float *err,
+                             const int *obsid, const int *platid, const float *hx, const float *hx_mean,
+                             const int *sat_obs, int n_sat_obs, const int *sat_plats, int n_sat_plats,
+                             const IndexGeom *geom_d, int ncell, int *d_cell, int *d_count, int *d_fill,
+                             int *d_pos_tmp, int *d_order, float4 *Atmp, float4 *Btmp, ObsSorted out,
+                             int *launches);
+
+cudaError_t launch_col_prep(cudaStream_t st, int ncol, const float *lat, const float *lon, const int *mask,
+                            const float *mean_b, int ns, const DevLoc &loc, ColPar *cp, float *diag_maxhz,
+                            int *launches);
+
+struct GramArgs {
+  int nunits, groups, k, kp;
+  const int *active;      // active (unmasked) columns
+  const ColPar *cp;
+  DevLoc loc;
+  ObsSorted obs;
+  const IndexGeom *geom;  // device copy
+  float *G;               // [unit][k][k+1]  (k x k Gram, column k = RHS)
+  int *nkept;             // [unit]
+  float *diag_obscount;   // [ncol]
+  float *diag_lg_obscount;// [group][ncol]
+  float *diag_lg_obsloc;  // [group][ncol]
+  int ncol;
+};
+cudaError_t launch_gram(cudaStream_t st, const GramArgs &a, int *launches);
+
+struct EigArgs {
+  int nunits, k;
+  float infl;
+  const float *G;
+  const int *nkept;
+  float *T;               // [unit][k][k]
+  int *status;            // [1] accumulated error bits
+};
+cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
+
+struct UpdateArgs {
+  int ncol, ns, k, groups;
+  const int *mask;        // [ncol] device
+  const int *col2act;     // [ncol] active index or -1
+  const ColPar *cp;
+  int loc_cls, vtloc_surf;
+  const int *slab_var;    // [ns] variable of each slab
+  const int *slab_lev;    // [ns] level of each slab within its variable
+  const float *var_inc_max, *var_lb, *var_ub;  // per variable
+  const float *bkg, *mean_b, *sprd_b;
+  const float *T;
+  const int *nkept;
+  float *ana, *mean_a, *sprd_a;
+  float rtps, rtpp, mul;
+  int *status;
+};
+cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches);
+
+// list emission for verification
+cudaError_t launch_obslist(cudaStream_t st, int col, int gid, int group_slot, const ColPar *cp_col, const DevLoc &loc,
+                           ObsSorted obs, const IndexGeom *geom, int cap, int *d_idx, float *d_r, int *d_counts);
+
+cudaError_t launch_debug_metric(cudaStream_t st, int n, const float *lat1, const float *lon1,
+                                const float *lat2, const float *lon2, float *dist);
+cudaError_t launch_debug_gc(cudaStream_t st, int n, const float *z, const float *L, float *fast, float *exact);
+
+}  // namespace lgpu

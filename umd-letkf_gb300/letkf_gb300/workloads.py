@@ -1,0 +1,75 @@
+"""Named analysis workloads: generator options + the localization and solver
+sections a reference YAML configuration would carry for them.
+
+  c1        90x45x10 grid, one 3-D temperature, k=20, 5,000 point obs,
+            horizontal GC 500 km x vertical GC 200 m (loc_vtgc), RTPS 0.6
+  c2        720x360x40 ocean (T, S, SSH; 81 slabs), k=40, 3,000 T/S profiles
+            + 200,000 SSH/SST swath obs, loc_novrt 800 km (equator) to
+            200 km (poles), default inflation
+  c3        720x360x40 ocean, k=32 (or 64), 500,000 clustered obs, loc_novrt
+            with a constant 60 km length scale (support ~219 km)
+  simple3d  test/simple3d-style (k=50, three 3-D variables, two synthetic
+            obs, loc_novrt 500 km -> 50 km)
+  ocean     test/ocean/vtloc-style (k=10, T/S/u/v, five synthetic obs,
+            loc_ocean with the mixed-layer split)
+  c2small / c1small  reduced grids with the same generators for fast tests
+"""
+
+C2_LOC = {"class": "loc_novrt",
+          "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 800.0e3},
+                                                          {"lat": 90.0, "radius": 200.0e3}]}}
+
+WORKLOADS = {
+    "c1": dict(gen=dict(workload="c1"),
+               localization={"class": "loc_vtgc",
+                             "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 500.0e3}]},
+                             "vtloc": 200.0},
+               solver={"inflation": {"rtps": 0.6}}),
+    "c2": dict(gen=dict(workload="c2"), localization=C2_LOC, solver={}),
+    "c2small": dict(gen=dict(workload="c2", nx=144, ny=72, nz=10, n_profiles=300, n_swaths=10, swath_len=800),
+                    localization=C2_LOC, solver={}),
+    "c3": dict(gen=dict(workload="c3"),
+               localization={"class": "loc_novrt",
+                             "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
+               solver={}),
+    "c3small": dict(gen=dict(workload="c3", nx=180, ny=90, nz=10, n_obs=40000),
+                    localization={"class": "loc_novrt",
+                                  "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
+                    solver={}),
+    "simple3d": dict(gen=dict(workload="simple3d"),
+                     localization={"class": "loc_novrt",
+                                   "hzloc": {"type": "linearinterp_lat",
+                                             "value": [{"lat": 0.0, "radius": 500.0e3},
+                                                       {"lat": 90.0, "radius": 50.0e3}]}},
+                     solver={}),
+    "ocean": dict(gen=dict(workload="ocean"),
+                  localization={"class": "loc_ocean", "save_diag": True,
+                                "hzloc_prof": {"type": "linearinterp_lat",
+                                               "value": [{"lat": 0.0, "radius": 720.0e3},
+                                                         {"lat": 90.0, "radius": 200.0e3}]},
+                                "hzloc_sat": {"type": "linearinterp_lat",
+                                              "value": [{"lat": 0.0, "radius": 500.0e3},
+                                                        {"lat": 90.0, "radius": 50.0e3}]},
+                                "sat_obs": [], "sat_plats": [1],
+                                "vtloc_surf": {"type": "bkg_t", "bkg_t_delta": 0.2, "bkg_t_var": "ocn_t"}},
+                  solver={"inflation": {"rtps": 0.0, "rtpp": 0.0, "mul": 1.0}}),
+}
+
+# test/simple3d solver/state variants (default.yaml, bounds_check.yaml,
+# inflation_{rtps,rtpp,mul}.yaml)
+SIMPLE3D_VARIANTS = {
+    "default": dict(solver={}, bounds=None),
+    "bounds_check": dict(solver={}, bounds={0: dict(ana_bounds=(-2.0, 2.0)), 1: dict(ana_inc_max=2.0),
+                                            2: dict(ana_inc_max=0.2, ana_bounds=(-2.0, 2.0))}),
+    "inflation_rtps": dict(solver={"inflation": {"rtps": 0.8}}, bounds=None),
+    "inflation_rtpp": dict(solver={"inflation": {"rtpp": 0.8}}, bounds=None),
+    "inflation_mul": dict(solver={"inflation": {"mul": 1.05}}, bounds=None),
+}
+
+
+def apply_bounds(variables, bounds):
+    """Copy of a variable list with per-variable ana_inc_max / ana_bounds."""
+    out = [dict(v) for v in variables]
+    for i, b in (bounds or {}).items():
+        out[i].update(b)
+    return out
