@@ -288,6 +288,8 @@ int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const floa
   if (!state || !mean || !sprd || !vars || nvars <= 0 || ns <= 0) return fail(h, LGPU_ERR_ARG, "set_state: bad arguments");
   if (k < 2) return fail(h, LGPU_ERR_ARG, "ensemble size must be >= 2");
   if (k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "ensemble size > 64 is not supported by this build");
+  if ((size_t)ns * ((k + 3) & ~3) * 8 > 200 * 1024)
+    return fail(h, LGPU_ERR_UNSUPPORTED, "a column's state (ns x k) exceeds the 100 KB the update kernel stages");
   // slab -> (variable, level); every slab must belong to exactly one variable
   std::vector<int> sv(ns, -1), sl(ns, -1);
   std::vector<float> inc(nvars), lb(nvars), ub(nvars);

@@ -115,7 +115,12 @@ __global__ void k_eig(EigArgs a, int wpb) {
   for (int t = lane; t < k * ld; t += 32) { const int i = t / ld, j = t % ld; Z[t] = (i == j) ? 1.0f : 0.0f; }
   __syncwarp();
 
-  // ---- implicit-shift QL on (d, e)
+  // ---- implicit-shift QL on (d, e).  Each sweep's scalar recurrence is
+  // evaluated redundantly by all lanes: d[i+1] is carried in a register and
+  // only e[i], d[i] (never written during the sweep) are read, so lane 0 can
+  // write results without intra-sweep barriers.  The sweep's rotations are
+  // recorded and applied to the rows of Z afterwards, lanes in parallel.
+  float *rc = p, *rs = w;   // rotation cosines / sines of one sweep
   int bad = 0;
   for (int l = 0; l < k; l++) {
     int iter = 0;
@@ -127,38 +132,51 @@ __global__ void k_eig(EigArgs a, int wpb) {
       }
       if (m == l) break;
       if (++iter > 60) { bad = 1; break; }
-      float g = (d[l + 1] - d[l]) / (2.0f * e[l]);
+      const float dl = d[l], el = e[l];
+      float g = (d[l + 1] - dl) / (2.0f * el);
       float r = sqrtf(g * g + 1.0f);
-      g = d[m] - d[l] + e[l] / (g + copysignf(r, g));
+      g = d[m] - dl + el / (g + copysignf(r, g));
       float s = 1.0f, c = 1.0f, pp = 0.0f;
+      float di1 = d[m];
+      int i = m - 1;
       bool deflate = false;
-      for (int i = m - 1; i >= l; i--) {
-        // every lane reads before lane 0 overwrites e[i+1], d[i+1]
-        const float ei = e[i], di = d[i], di1 = d[i + 1];
+      for (; i >= l; i--) {
+        const float ei = e[i], di = d[i];
         const float f = s * ei, b = c * ei;
         r = sqrtf(f * f + g * g);
-        __syncwarp();
+        if (lane == 0) e[i + 1] = r;
         if (r == 0.0f) {
-          if (lane == 0) { e[i + 1] = 0.0f; d[i + 1] = di1 - pp; e[m] = 0.0f; }
+          if (lane == 0) { d[i + 1] = di1 - pp; e[m] = 0.0f; }
           deflate = true;
           break;
         }
-        s = f / r;
-        c = g / r;
+        const float ir = 1.0f / r;
+        s = f * ir;
+        c = g * ir;
         g = di1 - pp;
         const float rr = (di - g) * s + 2.0f * c * b;
         pp = s * rr;
-        if (lane == 0) { e[i + 1] = r; d[i + 1] = g + pp; }
+        if (lane == 0) { d[i + 1] = g + pp; rc[i] = c; rs[i] = s; }
         g = c * rr - b;
-        for (int q = lane; q < k; q += 32) {
-          const float zi = Z[q * ld + i], zf = Z[q * ld + i + 1];
-          Z[q * ld + i + 1] = s * zi + c * zf;
-          Z[q * ld + i] = c * zi - s * zf;
-        }
+        di1 = di;
       }
       __syncwarp();
-      if (deflate) continue;
-      if (lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
+      // apply rotations m-1 .. ilo to columns (i, i+1) of every Z row
+      const int ilo = deflate ? i + 1 : l;
+      if (ilo <= m - 1) {
+        for (int q = lane; q < k; q += 32) {
+          float *zr = Z + q * ld;
+          float carry = zr[m];
+          for (int ii = m - 1; ii >= ilo; ii--) {
+            const float cc = rc[ii], ss = rs[ii];
+            const float zi = zr[ii];
+            zr[ii + 1] = ss * zi + cc * carry;
+            carry = cc * zi - ss * carry;
+          }
+          zr[ilo] = carry;
+        }
+      }
+      if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
       __syncwarp();
     }
     if (bad) break;

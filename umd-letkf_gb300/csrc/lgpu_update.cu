@@ -1,5 +1,4 @@
-// lgpu_update.cu -- ensemble update and analysis epilogue, one CTA per
-// column, one warp per slab.
+// lgpu_update.cu -- ensemble update and analysis epilogue, one CTA per column.
 //
 // Replaces src/letkf_solver.F90:282-379 for one column:
 //   x_a(1 x k) = x_b(1 x k) * T_g for every slab of every group g with local
@@ -10,22 +9,33 @@
 //   (:357-371); final spread and add the mean back (:375-379).
 // Masked columns are skipped by the reference (:207): their state stays the
 // background perturbation and their mean/spread stay the background values.
-// Member sums use a fixed butterfly order across the warp.
+//
+// The column's background perturbations (ns x k, contiguous) and its group
+// transforms are staged in shared memory with 16-byte loads; X_b T is formed
+// four members per thread from float4 rows of T; the epilogue runs one warp
+// per slab with a fixed butterfly order for the member sums.
 #include "lgpu_internal.cuh"
 
 namespace lgpu {
 
 namespace {
 
-constexpr int UT = 256;  // 8 warps per column
+constexpr int UT = 128;  // 4 warps per column
 
 __device__ __forceinline__ float bsum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-__global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups) {
-  extern __shared__ __align__(16) float Ts[];   // [tsm_groups][k][k] transforms of this column
+__device__ __forceinline__ int slab_group(const UpdateArgs &a, int lev, int mld) {
+  if (a.loc_cls == LOC_VTGC) return lev;
+  if (a.loc_cls == LOC_OCEAN && a.vtloc_surf == 1) return (lev + 1 <= mld) ? 0 : 1;
+  return 0;
+}
+
+// smem: xb [ns][kp], xa [ns][kp], T [tg][k][kp]
+__global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int kp) {
+  extern __shared__ __align__(16) float sm[];
   const int col = blockIdx.x;
   const int k = a.k, ns = a.ns;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -39,58 +49,83 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups) {
     }
     return;
   }
+  float *xb = sm;
+  float *xa = xb + (size_t)ns * kp;
+  float *Ts = xa + (size_t)ns * kp;
   const int G = a.groups;
   const size_t ubase = (size_t)act * G;
-  // stage the transforms of groups that have observations
+  const int mld = a.cp[col].mld;
+  // ---- stage X_b (rows padded to kp) and the transforms
+  if ((k & 3) == 0) {
+    const float4 *src = reinterpret_cast<const float4 *>(a.bkg + cbase);
+    const int q = k >> 2;
+    for (int t = threadIdx.x; t < ns * q; t += blockDim.x)
+      reinterpret_cast<float4 *>(xb + (t / q) * kp)[t % q] = src[t];
+  } else {
+    for (int t = threadIdx.x; t < ns * kp; t += blockDim.x) {
+      const int s = t / kp, j = t % kp;
+      xb[t] = j < k ? a.bkg[cbase + (size_t)s * k + j] : 0.0f;
+    }
+  }
   for (int g = 0; g < tsm_groups; g++) {
     if (a.nkept[ubase + g] <= 0) continue;
-    if ((k & 1) == 0) {   // k*k and every T offset are multiples of 4 floats
-      const float4 *src = reinterpret_cast<const float4 *>(a.T + (ubase + g) * k * k);
-      float4 *dst = reinterpret_cast<float4 *>(Ts + (size_t)g * k * k);
-      for (int t = threadIdx.x; t < (k * k) / 4; t += blockDim.x) dst[t] = src[t];
-    } else {
-      for (int t = threadIdx.x; t < k * k; t += blockDim.x) Ts[(size_t)g * k * k + t] = a.T[(ubase + g) * k * k + t];
+    const float *T = a.T + (ubase + g) * k * k;
+    float *dst = Ts + (size_t)g * k * kp;
+    for (int t = threadIdx.x; t < k * kp; t += blockDim.x) {
+      const int i = t / kp, j = t % kp;
+      dst[t] = j < k ? T[i * k + j] : 0.0f;
     }
   }
   __syncthreads();
-  const int mld = a.cp[col].mld;
+  // ---- X_a = X_b T_g, four members per work item
+  const int q4 = kp >> 2;
+  for (int t = threadIdx.x; t < ns * q4; t += blockDim.x) {
+    const int s = t / q4, jq = t % q4;
+    const int g = slab_group(a, a.slab_lev[s], mld);
+    const bool has = g < G && a.nkept[ubase + g] > 0;
+    float4 acc;
+    if (has) {
+      const float *T = (g < tsm_groups) ? Ts + (size_t)g * k * kp : nullptr;
+      const float *Tg = a.T + (ubase + g) * k * k;
+      const float *xr = xb + (size_t)s * kp;
+      acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int i = 0; i < k; i++) {
+        const float xi = xr[i];
+        float4 tv;
+        if (T) {
+          tv = reinterpret_cast<const float4 *>(T + (size_t)i * kp)[jq];
+        } else {
+          const int j = 4 * jq;
+          tv.x = j < k ? Tg[i * k + j] : 0.f;
+          tv.y = j + 1 < k ? Tg[i * k + j + 1] : 0.f;
+          tv.z = j + 2 < k ? Tg[i * k + j + 2] : 0.f;
+          tv.w = j + 3 < k ? Tg[i * k + j + 3] : 0.f;
+        }
+        acc.x = __fmaf_rn(xi, tv.x, acc.x);
+        acc.y = __fmaf_rn(xi, tv.y, acc.y);
+        acc.z = __fmaf_rn(xi, tv.z, acc.z);
+        acc.w = __fmaf_rn(xi, tv.w, acc.w);
+      }
+    } else {
+      acc = reinterpret_cast<const float4 *>(xb + (size_t)s * kp)[jq];
+    }
+    reinterpret_cast<float4 *>(xa + (size_t)s * kp)[jq] = acc;
+  }
+  __syncthreads();
+  // ---- epilogue, one warp per slab
   const float kf = (float)k, km1 = (float)(k - 1);
   for (int s = warp; s < ns; s += nw) {
-    const int v = a.slab_var[s], lev = a.slab_lev[s];
-    int g = 0;
-    if (a.loc_cls == LOC_VTGC) g = lev;
-    else if (a.loc_cls == LOC_OCEAN && a.vtloc_surf == 1) g = (lev + 1 <= mld) ? 0 : 1;
-    const bool has = g < G && a.nkept[ubase + g] > 0;
-    const float *xbp = a.bkg + cbase + (size_t)s * k;
+    const int v = a.slab_var[s];
     const int j0 = lane, j1 = lane + 32;
-    const float xb0 = j0 < k ? xbp[j0] : 0.0f;
-    const float xb1 = j1 < k ? xbp[j1] : 0.0f;
-    float x0 = xb0, x1 = xb1;
-    if (has) {
-      const float *T = (g < tsm_groups) ? Ts + (size_t)g * k * k : a.T + (ubase + g) * k * k;
-      float acc0 = 0.0f, acc1 = 0.0f;
-      const int i1max = k < 32 ? k : 32;
-      for (int i = 0; i < i1max; i++) {
-        const float xi = __shfl_sync(0xffffffffu, xb0, i);
-        if (j0 < k) acc0 = __fmaf_rn(xi, T[i * k + j0], acc0);
-        if (j1 < k) acc1 = __fmaf_rn(xi, T[i * k + j1], acc1);
-      }
-      for (int i = 32; i < k; i++) {
-        const float xi = __shfl_sync(0xffffffffu, xb1, i - 32);
-        if (j0 < k) acc0 = __fmaf_rn(xi, T[i * k + j0], acc0);
-        if (j1 < k) acc1 = __fmaf_rn(xi, T[i * k + j1], acc1);
-      }
-      x0 = j0 < k ? acc0 : 0.0f;
-      x1 = j1 < k ? acc1 : 0.0f;
-    }
+    const float *xr = xa + (size_t)s * kp, *br = xb + (size_t)s * kp;
+    float x0 = j0 < k ? xr[j0] : 0.0f, x1 = j1 < k ? xr[j1] : 0.0f;
+    const float xb0 = j0 < k ? br[j0] : 0.0f, xb1 = j1 < k ? br[j1] : 0.0f;
     const float mb = a.mean_b[(size_t)col * ns + s], sb = a.sprd_b[(size_t)col * ns + s];
-    // recenter
     if (j0 < k) x0 = x0 + mb;
     if (j1 < k) x1 = x1 + mb;
     float m = bsum(x0 + x1) / kf;
     if (j0 < k) x0 = x0 - m;
     if (j1 < k) x1 = x1 - m;
-    // clip the increment of the mean
     const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
     {
       float r = m - mb;
@@ -98,7 +133,6 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups) {
       r = fmaxf(r, lb - mb); r = fminf(r, ub - mb);
       m = r + mb;
     }
-    // RTPS
     if (a.rtps > 0.0f) {
       const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
       if (sa > 0.0f) {
@@ -106,14 +140,11 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups) {
         x0 = x0 * f; x1 = x1 * f;
       }
     }
-    // RTPP
     if (a.rtpp > 0.0f) {
       x0 = a.rtpp * xb0 + (1.0f - a.rtpp) * x0;
       x1 = a.rtpp * xb1 + (1.0f - a.rtpp) * x1;
     }
-    // multiplicative
     if (a.mul != 1.0f) { x0 = x0 * a.mul; x1 = x1 * a.mul; }
-    // member bounds and re-mean
     {
       if (j0 < k) { x0 = fmaxf(x0, lb - m); x0 = fminf(x0, ub - m); }
       if (j1 < k) { x1 = fmaxf(x1, lb - m); x1 = fminf(x1, ub - m); }
@@ -122,11 +153,10 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups) {
       if (j1 < k) x1 = x1 - r;
       m = m + r;
     }
-    // spread, add the mean
     const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
-    float *xa = a.ana + cbase + (size_t)s * k;
-    if (j0 < k) xa[j0] = x0 + m;
-    if (j1 < k) xa[j1] = x1 + m;
+    float *out = a.ana + cbase + (size_t)s * k;
+    if (j0 < k) out[j0] = x0 + m;
+    if (j1 < k) out[j1] = x1 + m;
     if (lane == 0) {
       a.mean_a[(size_t)col * ns + s] = m;
       a.sprd_a[(size_t)col * ns + s] = sa;
@@ -139,13 +169,17 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups) {
 
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   if (a.ncol <= 0) return cudaSuccess;
-  const size_t per = (size_t)a.k * a.k * sizeof(float);
+  const int kp = (a.k + 3) & ~3;
+  const size_t xbytes = 2 * (size_t)a.ns * kp * sizeof(float);
+  const size_t per = (size_t)a.k * kp * sizeof(float);
+  const size_t budget = 200 * 1024;
+  if (xbytes > budget) return cudaErrorInvalidValue;   // checked by the caller
   int tg = a.groups;
-  while (tg > 0 && tg * per > 64 * 1024) tg--;
-  const size_t smem = tg * per;
-  cudaError_t e = cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem > 0 ? smem : 16));
+  while (tg > 0 && xbytes + tg * per > budget) tg--;
+  const size_t smem = xbytes + tg * per;
+  cudaError_t e = cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_update<<<a.ncol, UT, smem, st>>>(a, tg);
+  k_update<<<a.ncol, UT, smem, st>>>(a, tg, kp);
   (*launches)++;
   return cudaGetLastError();
 }

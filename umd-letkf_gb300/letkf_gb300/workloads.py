@@ -8,6 +8,8 @@ sections a reference YAML configuration would carry for them.
             200 km (poles), default inflation
   c3        720x360x40 ocean, k=32 (or 64), 500,000 clustered obs, loc_novrt
             with a constant 60 km length scale (support ~219 km)
+  c2mid     c2 observations on a 360x180x10 grid (profiling-sized: the same
+            local observation counts per column, a fifth of the columns)
   simple3d  test/simple3d-style (k=50, three 3-D variables, two synthetic
             obs, loc_novrt 500 km -> 50 km)
   ocean     test/ocean/vtloc-style (k=10, T/S/u/v, five synthetic obs,
@@ -28,6 +30,7 @@ WORKLOADS = {
     "c2": dict(gen=dict(workload="c2"), localization=C2_LOC, solver={}),
     "c2small": dict(gen=dict(workload="c2", nx=144, ny=72, nz=10, n_profiles=300, n_swaths=10, swath_len=800),
                     localization=C2_LOC, solver={}),
+    "c2mid": dict(gen=dict(workload="c2", nx=360, ny=180, nz=10), localization=C2_LOC, solver={}),
     "c3": dict(gen=dict(workload="c3"),
                localization={"class": "loc_novrt",
                              "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
