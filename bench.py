@@ -215,6 +215,7 @@ def gpu_arm(args, dist):
     hbm, bf16, peak_kind = peaks()
     dev = dist.local if dist.world > 1 else 0
     s = Solver(dev)
+    s.set_variant(args.variant)
     s.solver_init(cfg["solver"])
     s.loc_init(cfg["localization"], prob.vars, prob.lev_depth)
     s.set_problem(prob)
@@ -265,6 +266,23 @@ def gpu_arm(args, dist):
         roof = {"kernel": "k_" + dom, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "traffic": traffic,
                 "peak_source": peak_kind + " bf16_tflops (burst); this kernel computes in FP32 on CUDA cores"}
+    variant = {1: "plain", 2: "batched_tc"}.get(tims[-1]["variant"], "?")
+    plain = None
+    if variant != "plain" and not args.no_plain:
+        # the plain per-column FP32 path on the same inputs (spec comparison)
+        s.set_variant("plain")
+        for _ in range(2):
+            s.run()
+        pt = []
+        for _ in range(max(1, min(args.steps, 3))):
+            s.flush_l2(256 << 20)
+            s.run()
+            pt.append(s.timings()["total_ms"])
+        pms = dist.max(statistics.mean(pt))
+        plain = {"value": dist.world * nact / (pms / 1000.0), "ms_per_step": pms,
+                 "speedup_of_headline": (dist.world * nact / (ms_max / 1000.0)) / (dist.world * nact / (pms / 1000.0))}
+        s.set_variant(args.variant)
+        s.run()
     # ---- end to end through the C ABI with page-locked host buffers
     pin = {n: PinnedArray(getattr(prob, n).shape, getattr(prob, n).dtype) for n in
            ("state", "mean", "sprd", "olat", "olon", "oz", "otime", "oval", "oerr", "oobsid", "oplatid", "hx",
@@ -305,7 +323,7 @@ def gpu_arm(args, dist):
             "config": workload_config(args, prob, cfg), "clocks": ck, "gpu_launches": launches * args.steps,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": e2e_ms},
-            "roofline": roof, "stages": stages, "analysis_finite": ok}
+            "roofline": roof, "stages": stages, "analysis_finite": ok, "variant": variant, "plain_variant": plain}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         rate, n, nth, dt = cpu_rate(prob, cfg)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
@@ -337,6 +355,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", default="auto", choices=["auto", "plain", "batched"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-variant comparison run")
     args = ap.parse_args()
     dist = Dist()
     try:

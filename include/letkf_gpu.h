@@ -138,7 +138,17 @@ typedef struct lgpu_timings {
   int launches;      /* kernels launched by the run */
   int units;         /* (column, group) solve units */
   long long kept_pairs;   /* sum over units of kept local observations (only when counted) */
+  int variant;       /* Gram variant that ran (LGPU_VARIANT_PLAIN / _BATCHED_TC) */
 } lgpu_timings;
+
+/* Gram variants.  PLAIN: one CTA per (column, group), FP32 on the CUDA
+ * cores.  BATCHED_TC: tiles of 128 neighbouring columns share their
+ * observations; the Gram of a tile is one GEMM on the tensor cores (tcgen05,
+ * TF32 with a three-term hi/lo split, FP32 accumulation).  AUTO picks
+ * BATCHED_TC.  Both give bit-identical observation lists. */
+#define LGPU_VARIANT_AUTO 0
+#define LGPU_VARIANT_PLAIN 1
+#define LGPU_VARIANT_BATCHED_TC 2
 
 int lgpu_create(int device, lgpu_handle **out);
 void lgpu_destroy(lgpu_handle *h);
@@ -147,6 +157,7 @@ const char *lgpu_last_error(const lgpu_handle *h);
 int lgpu_solver_init(lgpu_handle *h, const lgpu_solver_config *cfg);
 int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *cfg);
 int lgpu_loc_maxgroups(const lgpu_handle *h);
+int lgpu_set_variant(lgpu_handle *h, int variant);   /* no reference counterpart: selects the Gram kernel */
 
 int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, const int *mask);
 int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean,

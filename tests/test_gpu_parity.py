@@ -61,11 +61,12 @@ def test_gc_fast_and_exact(solver):
 LIST_CASES = [("simple3d", None), ("ocean", None), ("c1", None), ("c2small", 150), ("c3small", 150)]
 
 
+@pytest.mark.parametrize("variant", ["plain", "batched"])
 @pytest.mark.parametrize("name,nsample", LIST_CASES)
-def test_obslists_bitexact(name, nsample):
+def test_obslists_bitexact(name, nsample, variant):
     cfg = workload_cfg(name)
     prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
-    res = gpu_run(prob, cfg["localization"], cfg["solver"], keep_open=True)
+    res = gpu_run(prob, cfg["localization"], cfg["solver"], keep_open=True, variant=variant)
     s = res["solver"]
     o = oracle_for(prob, cfg["localization"], cfg["solver"])
     rng = np.random.default_rng(1)
@@ -104,8 +105,9 @@ def test_obslists_bitexact(name, nsample):
     o.close()
 
 
-def _check_analysis(prob, cfg_loc, cfg_solver, cols, variables=None, label=""):
-    gpu = gpu_run(prob, cfg_loc, cfg_solver, variables=variables)
+def _check_analysis(prob, cfg_loc, cfg_solver, cols, variables=None, label="", variant="auto"):
+    gpu = gpu_run(prob, cfg_loc, cfg_solver, variables=variables, variant=variant)
+    assert gpu["timings"]["variant"] == (1 if variant == "plain" else 2)
     o = oracle_for(prob, cfg_loc, cfg_solver, variables=variables)
     for prec in (32, 64):
         ref = o.run(prec, cols=cols)
@@ -129,25 +131,27 @@ def _check_analysis(prob, cfg_loc, cfg_solver, cols, variables=None, label=""):
     return gpu
 
 
+@pytest.mark.parametrize("gram", ["plain", "batched"])
 @pytest.mark.parametrize("variant", ["default", "bounds_check", "inflation_rtps", "inflation_rtpp", "inflation_mul"])
-def test_simple3d_variants(variant):
+def test_simple3d_variants(variant, gram):
     from letkf_gb300.workloads import SIMPLE3D_VARIANTS, apply_bounds
     cfg = workload_cfg("simple3d")
     prob = workload("simple3d")
     v = SIMPLE3D_VARIANTS[variant]
     variables = apply_bounds(prob.vars, v["bounds"])
     cols = np.arange(prob.ncol)[::3]
-    _check_analysis(prob, cfg["localization"], v["solver"], cols, variables=variables, label=variant)
+    _check_analysis(prob, cfg["localization"], v["solver"], cols, variables=variables, label=variant, variant=gram)
 
 
+@pytest.mark.parametrize("gram", ["plain", "batched"])
 @pytest.mark.parametrize("name", ["ocean", "c1", "c2small", "c3small"])
-def test_analysis_parity(name):
+def test_analysis_parity(name, gram):
     cfg = workload_cfg(name)
     prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
     active = np.nonzero(prob.mask == 0)[0]
     rng = np.random.default_rng(2)
     cols = np.sort(rng.choice(active, size=min(600, len(active)), replace=False))
-    _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label=name)
+    _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label=name, variant=gram)
 
 
 def test_single_observation_closed_form():
@@ -184,11 +188,12 @@ def test_edge_cases():
     masked = replace(prob, mask=np.ones_like(prob.mask))
     g = gpu_run(masked, cfg["localization"], {})
     assert np.array_equal(g["state"], prob.state)
-    for k in (2, 7, 33):
+    for k in (2, 7, 33, 64):
         p = workload("c1", k=k)
         c1 = workload_cfg("c1")
         cols = np.arange(0, p.ncol, 37)
-        _check_analysis(p, c1["localization"], c1["solver"], cols, label="k=%d" % k)
+        for gram in ("plain", "batched"):
+            _check_analysis(p, c1["localization"], c1["solver"], cols, label="k=%d %s" % (k, gram), variant=gram)
 
 
 def test_errors_and_validation():

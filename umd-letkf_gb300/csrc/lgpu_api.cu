@@ -45,7 +45,7 @@ enum {
   B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID, B_HX, B_HXM, B_SATOBS, B_SATPLATS,
   B_GEOM, B_CELL, B_COUNT, B_FILL, B_POSTMP, B_ORDER, B_ATMP, B_BTMP, B_SA, B_SB, B_SHX, B_SIDX, B_CSTART,
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
-  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH,
+  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR,
   B_COUNT_ALL
 };
 
@@ -70,6 +70,9 @@ struct lgpu_handle {
   IndexGeom geom{};
   int ncell = 0;
   int nunits = 0;
+  int variant = LGPU_VARIANT_AUTO;
+  int ntiles = 0;
+  bool used_tc = false;
   DevBuf buf[B_COUNT_ALL];
   lgpu_timings tim{};
 };
@@ -116,6 +119,36 @@ int build_interp(lgpu_handle *h, Interp &t, int n, const lgpu_interp_point *pts,
   }
   if (last_lat < 90.0f) { t.lat[t.n] = 90.0f; t.dist[t.n] = last_r; t.n++; }
   return LGPU_OK;
+}
+
+// Interleave the low 16 bits of x with zeros (Morton order helper).
+uint32_t spread16(uint32_t x) {
+  x &= 0xFFFFu;
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+// Tiles of 128 active columns that are close on the sphere: active columns
+// ordered along a Morton curve of (latitude, longitude), cut into runs.
+std::vector<int> build_tiles(const std::vector<int> &act, const float *lat, const float *lon) {
+  const size_t n = act.size();
+  std::vector<std::pair<uint32_t, int>> key(n);
+  for (size_t i = 0; i < n; i++) {
+    const int c = act[i];
+    double lo = std::fmod((double)lon[c], 360.0);
+    if (lo < 0) lo += 360.0;
+    const uint32_t qa = (uint32_t)std::min(65535.0, std::max(0.0, ((double)lat[c] + 90.0) / 180.0 * 65535.0));
+    const uint32_t qo = (uint32_t)std::min(65535.0, std::max(0.0, lo / 360.0 * 65535.0));
+    key[i] = {spread16(qo) | (spread16(qa) << 1), c};
+  }
+  std::sort(key.begin(), key.end());
+  const size_t nt = (n + 127) / 128;
+  std::vector<int> tiles(nt * 128, -1);
+  for (size_t i = 0; i < n; i++) tiles[i] = key[i].second;
+  return tiles;
 }
 
 void build_geom(IndexGeom &g, int &ncell) {
@@ -249,6 +282,14 @@ int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *c) {
 
 int lgpu_loc_maxgroups(const lgpu_handle *h) { return (h && h->loc_ok) ? h->loc.groups : -1; }
 
+int lgpu_set_variant(lgpu_handle *h, int variant) {
+  if (!h) return LGPU_ERR_ARG;
+  if (variant < LGPU_VARIANT_AUTO || variant > LGPU_VARIANT_BATCHED_TC)
+    return fail(h, LGPU_ERR_ARG, "unknown variant " + std::to_string(variant));
+  h->variant = variant;
+  return LGPU_OK;
+}
+
 int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, const int *mask) {
   if (!h) return LGPU_ERR_ARG;
   if (nij <= 0 || !lat || !lon) return fail(h, LGPU_ERR_ARG, "set_grid: bad arguments");
@@ -272,7 +313,14 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
   CK(cudaMemcpyAsync(h->buf[B_COL2ACT].p, c2a.data(), sizeof(int) * nij, cudaMemcpyHostToDevice, h->st), "H2D c2a");
   if (!act.empty())
     CK(cudaMemcpyAsync(h->buf[B_ACTIVE].p, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, h->st), "H2D act");
+  const std::vector<int> tiles = build_tiles(act, lat, lon);
+  CK(h->buf[B_TILECOLS].ensure(sizeof(int) * std::max<size_t>(1, tiles.size())), "alloc tiles");
+  CK(h->buf[B_TILEPAR].ensure(sizeof(TilePar) * std::max<size_t>(1, tiles.size() / 128)), "alloc tiles");
+  if (!tiles.empty())
+    CK(cudaMemcpyAsync(h->buf[B_TILECOLS].p, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice, h->st),
+       "H2D tiles");
   CK(cudaStreamSynchronize(h->st), "set_grid sync");
+  h->ntiles = (int)(tiles.size() / 128);
   h->ncol = nij;
   h->nact = (int)act.size();
   h->h_col2act = c2a;
@@ -415,7 +463,7 @@ int lgpu_solver_run(lgpu_handle *h) {
   CK(h->buf[B_SIDX].ensure(4 * nobs), "alloc");
   CK(h->buf[B_CSTART].ensure(4 * ((size_t)h->ncell + 1)), "alloc");
   CK(h->buf[B_CP].ensure(sizeof(ColPar) * (size_t)h->ncol), "alloc");
-  CK(h->buf[B_G].ensure(4 * std::max<size_t>(1, (size_t)units) * k * (k + 1)), "alloc Gram");
+  CK(h->buf[B_G].ensure(4 * std::max<size_t>(1, (size_t)units) * packed_size(k)), "alloc Gram");
   CK(h->buf[B_T].ensure(4 * std::max<size_t>(1, (size_t)units) * k * k), "alloc transforms");
   CK(h->buf[B_NKEPT].ensure(4 * std::max<size_t>(1, (size_t)units)), "alloc");
   CK(h->buf[B_DMAXHZ].ensure(4 * (size_t)h->ncol), "alloc");
@@ -454,6 +502,34 @@ int lgpu_solver_run(lgpu_handle *h) {
   CK(cudaMemsetAsync(h->buf[B_STATUS].p, 0, 16, st), "memset");
   CK(cudaEventRecord(h->ev[2], st), "event");
   // ---- search + localize + Gram ----
+  const bool use_tc = h->variant == LGPU_VARIANT_BATCHED_TC || (h->variant == LGPU_VARIANT_AUTO && k >= 8);
+  h->used_tc = use_tc;
+  if (use_tc) {
+    CK(launch_tile_prep(st, h->ntiles, h->buf[B_TILECOLS].as<int>(), h->buf[B_CP].as<ColPar>(),
+                        h->buf[B_TILEPAR].as<TilePar>(), &launches), "tile prep");
+    TcArgs ta;
+    ta.ntiles = h->ntiles;
+    ta.groups = G;
+    ta.k = k;
+    ta.kp = kp;
+    gram_tc_passes(k, &ta.npass, &ta.np);
+    ta.nf = packed_size(k);
+    ta.ncol = h->ncol;
+    ta.tile_cols = h->buf[B_TILECOLS].as<int>();
+    ta.col2act = h->buf[B_COL2ACT].as<int>();
+    ta.cp = h->buf[B_CP].as<ColPar>();
+    ta.tp = h->buf[B_TILEPAR].as<TilePar>();
+    ta.loc = h->loc;
+    ta.obs = os;
+    ta.geom = h->buf[B_GEOM].as<IndexGeom>();
+    ta.G = h->buf[B_G].as<float>();
+    ta.nkept = h->buf[B_NKEPT].as<int>();
+    ta.diag_obscount = h->buf[B_DOBSC].as<float>();
+    ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
+    ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
+    ta.status = h->buf[B_STATUS].as<int>();
+    CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+  }
   GramArgs ga;
   ga.nunits = h->nunits;
   ga.groups = G;
@@ -470,7 +546,7 @@ int lgpu_solver_run(lgpu_handle *h) {
   ga.diag_lg_obscount = h->buf[B_DLGC].as<float>();
   ga.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
   ga.ncol = h->ncol;
-  CK(launch_gram(st, ga, &launches), "gram kernel");
+  if (!use_tc) CK(launch_gram(st, ga, &launches), "gram kernel");
   CK(cudaEventRecord(h->ev[3], st), "event");
   // ---- eigensolve + transform ----
   EigArgs ea;
@@ -525,12 +601,14 @@ int lgpu_solver_run(lgpu_handle *h) {
   h->tim.update_ms = ms[4];
   CK(cudaEventElapsedTime(&h->tim.total_ms, h->ev[0], h->ev[5]), "timing");
   h->tim.launches = launches;
+  h->tim.variant = h->used_tc ? LGPU_VARIANT_BATCHED_TC : LGPU_VARIANT_PLAIN;
   h->tim.units = h->nunits;
   h->tim.kept_pairs = -1;
   h->ran = true;
   if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
   if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");
   if (status & 4) return fail(h, LGPU_ERR_NONFINITE, "non-finite analysis mean or spread");
+  if (status & 16) return fail(h, LGPU_ERR_CUDA, "tensor-core pipeline wait timed out");
   return LGPU_OK;
 }
 

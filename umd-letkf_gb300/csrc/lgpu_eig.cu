@@ -48,16 +48,16 @@ __global__ void k_eig(EigArgs a, int wpb) {
   float *w = p + k;
   float *fl = w + k;
   float *gl = fl + k;
-  const float *G = a.G + (size_t)unit * k * (k + 1);
+  const float *G = a.G + (size_t)unit * packed_size(k);
   // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
   const float shift = (float)(k - 1) * 1.0f / a.infl;
   for (int t = lane; t < k * k; t += 32) {
     const int i = t / k, j = t % k;
-    float v = (i <= j) ? G[i * (k + 1) + j] : G[j * (k + 1) + i];
+    float v = (i <= j) ? G[tri_idx(i, j, k)] : G[tri_idx(j, i, k)];
     if (i == j) v += shift;
     A[i * ld + j] = v;
   }
-  for (int i = lane; i < k; i += 32) bv[i] = G[i * (k + 1) + k];
+  for (int i = lane; i < k; i += 32) bv[i] = G[k * (k + 1) / 2 + i];
   __syncwarp();
 
   // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j]

@@ -5,8 +5,8 @@
 // localize, keep r > 1e-4) and the data-heavy half of letkf_core_solve
 // (src/letkf_core.F90:92-98): G = (Yb diag(rloc/err)) Yb^T and the
 // right-hand side b = (Yb diag(rloc/err)) dep, which the reference forms
-// later as Pa * hdxb_rinv * dep (:118-125).  G and b are written as one
-// k x (k+1) block per unit; the eigensolve stage consumes it.
+// later as Pa * hdxb_rinv * dep (:118-125).  The upper triangle of G and b
+// are written packed per unit; the eigensolve stage consumes them.
 //
 // Data flow per CTA: the search circle's index window is a list of
 // contiguous runs of the cell-sorted observation table; threads stream
@@ -272,9 +272,10 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
       }
       __syncthreads();
     }
-    float *G = a.G + (size_t)unit * k * (k + 1);
-    for (int t = tid; t < k * (k + 1); t += GT) {
-      const int i = t / (k + 1), jj = t % (k + 1);
+    float *G = a.G + (size_t)unit * packed_size(k);
+    for (int t = tid; t < packed_size(k); t += GT) {
+      int i, jj;
+      packed_ij(t, k, i, jj);
       const int tl = (i >> 2) * ntn + (jj >> 2);
       G[t] = red[tl * 16 + (i & 3) * 4 + (jj & 3)];
     }

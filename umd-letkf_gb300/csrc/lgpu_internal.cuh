@@ -185,6 +185,21 @@ constexpr float kGuard1 = 1.0e-6f;        // fast-GC guard band, one factor
 constexpr float kGuard2 = 3.0e-6f;        // two-factor products
 constexpr float kStdev2Max = 3.65148377f; // SQRT(40.0/3.0) in REAL, src/letkf_solver.F90:47
 
+// Packed Gram layout of one unit: the upper triangle of G (i <= j, row-major)
+// followed by the right-hand side b; k(k+3)/2 floats.
+__host__ __device__ __forceinline__ int tri_off(int i, int k) { return i * k - (i * (i - 1)) / 2; }
+__host__ __device__ __forceinline__ int tri_idx(int i, int j, int k) { return tri_off(i, k) + (j - i); }
+__host__ __device__ __forceinline__ int packed_size(int k) { return k * (k + 3) / 2; }
+// feature f -> (i, j); j == k denotes the right-hand side (y_i * dep)
+__host__ __device__ __forceinline__ void packed_ij(int f, int k, int &i, int &j) {
+  const int nt = k * (k + 1) / 2;
+  if (f >= nt) { i = f - nt; j = k; return; }
+  int r = 0;
+  while (tri_off(r + 1, k) <= f) r++;
+  i = r;
+  j = f - tri_off(r, k) + r;
+}
+
 // Per-column parameters prepared once per run.
 struct ColPar {
   float ux, uy, uz;     // unit vector
@@ -286,7 +301,7 @@ struct GramArgs {
   DevLoc loc;
   ObsSorted obs;
   const IndexGeom *geom;  // device copy
-  float *G;               // [unit][k][k+1]  (k x k Gram, column k = RHS)
+  float *G;               // [unit][packed_size(k)]  (upper triangle of G, then b)
   int *nkept;             // [unit]
   float *diag_obscount;   // [ncol]
   float *diag_lg_obscount;// [group][ncol]
@@ -294,6 +309,30 @@ struct GramArgs {
   int ncol;
 };
 cudaError_t launch_gram(cudaStream_t st, const GramArgs &a, int *launches);
+
+// Batched (tile) Gram on the tensor cores.
+struct TilePar {
+  float lonn, dlon;  // longitude window of the tile's search cap (deg)
+  int b0, b1;        // latitude band range
+};
+struct TcArgs {
+  int ntiles, groups, k, kp, npass, np, nf, ncol;
+  const int *tile_cols;   // [ntiles][128] column index or -1
+  const int *col2act;
+  const ColPar *cp;
+  const TilePar *tp;
+  DevLoc loc;
+  ObsSorted obs;
+  const IndexGeom *geom;
+  float *G;
+  int *nkept;
+  float *diag_obscount, *diag_lg_obscount, *diag_lg_obsloc;
+  int *status;
+};
+cudaError_t launch_tile_prep(cudaStream_t st, int ntiles, const int *tile_cols, const ColPar *cp, TilePar *tp,
+                             int *launches);
+cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a, int *launches);
+void gram_tc_passes(int k, int *npass, int *np);
 
 struct EigArgs {
   int nunits, k;

@@ -75,13 +75,17 @@ class _Obs(ctypes.Structure):
 class Timings(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_float), ("index_ms", ctypes.c_float), ("prep_ms", ctypes.c_float),
                 ("gram_ms", ctypes.c_float), ("eig_ms", ctypes.c_float), ("update_ms", ctypes.c_float),
-                ("launches", ctypes.c_int), ("units", ctypes.c_int), ("kept_pairs", ctypes.c_longlong)]
+                ("launches", ctypes.c_int), ("units", ctypes.c_int), ("kept_pairs", ctypes.c_longlong),
+                ("variant", ctypes.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
-EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_solver_init", "lgpu_loc_init",
+VARIANT_AUTO, VARIANT_PLAIN, VARIANT_BATCHED_TC = 0, 1, 2
+VARIANTS = {"auto": 0, "plain": 1, "batched": 2}
+
+EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_solver_init", "lgpu_loc_init",
            "lgpu_loc_maxgroups", "lgpu_set_grid", "lgpu_set_state", "lgpu_set_obs", "lgpu_solver_run",
            "lgpu_get_state", "lgpu_get_diag", "lgpu_get_timings", "lgpu_solver_final", "lgpu_get_obslist",
            "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2"]
@@ -107,6 +111,7 @@ def lib(path=None):
     L.lgpu_solver_init.argtypes = [H, ctypes.POINTER(_SolverCfg)]
     L.lgpu_loc_init.argtypes = [H, ctypes.POINTER(_LocCfg)]
     L.lgpu_loc_maxgroups.argtypes = [H]
+    L.lgpu_set_variant.argtypes = [H, ctypes.c_int]
     L.lgpu_set_grid.argtypes = [H, ctypes.c_int, FP, FP, IP]
     L.lgpu_set_state.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP, FP, ctypes.c_int, ctypes.POINTER(_Var)]
     L.lgpu_set_obs.argtypes = [H, ctypes.c_int, ctypes.POINTER(_Obs), FP, FP]
@@ -242,6 +247,12 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+    def set_variant(self, variant):
+        """Gram kernel: 'plain' (per column, FP32 CUDA cores), 'batched'
+        (128-column tiles on the tensor cores) or 'auto'."""
+        v = VARIANTS[variant] if isinstance(variant, str) else int(variant)
+        return self._ck(self.L.lgpu_set_variant(self.h, v))
 
     # -- letkf_solver_init
     def solver_init(self, cfg=None, **kw):
