@@ -2,6 +2,7 @@
 // mirrors the reference's solver/localizer initialisation, uploads, the run
 // orchestration on one CUDA stream, timings and verification helpers.
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <cstdio>
 #include <cstring>
@@ -121,33 +122,48 @@ int build_interp(lgpu_handle *h, Interp &t, int n, const lgpu_interp_point *pts,
   return LGPU_OK;
 }
 
-// Interleave the low 16 bits of x with zeros (Morton order helper).
-uint32_t spread16(uint32_t x) {
-  x &= 0xFFFFu;
-  x = (x | (x << 8)) & 0x00FF00FFu;
-  x = (x | (x << 4)) & 0x0F0F0F0Fu;
-  x = (x | (x << 2)) & 0x33333333u;
-  x = (x | (x << 1)) & 0x55555555u;
-  return x;
+// Tiles of (up to) 128 active columns that are close on the sphere: k-d
+// bisection of the columns' unit vectors, splitting the widest coordinate at
+// a multiple of 128 so that leaves hold exactly 128 columns where possible.
+void kd_split(std::vector<std::array<float, 3>> &u, std::vector<int> &id, size_t lo, size_t hi,
+              std::vector<int> &out) {
+  const size_t n = hi - lo;
+  if (n <= 128) {
+    for (size_t i = lo; i < hi; i++) out.push_back(id[i]);
+    for (size_t i = n; i < 128; i++) out.push_back(-1);
+    return;
+  }
+  float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+  for (size_t i = lo; i < hi; i++)
+    for (int d = 0; d < 3; d++) { mn[d] = std::min(mn[d], u[i][d]); mx[d] = std::max(mx[d], u[i][d]); }
+  int ax = 0;
+  for (int d = 1; d < 3; d++) if (mx[d] - mn[d] > mx[ax] - mn[ax]) ax = d;
+  size_t half = (size_t)std::max<long long>(1, std::llround((double)n / 256.0)) * 128;
+  if (half >= n) half = 128;
+  std::vector<size_t> perm(n);
+  for (size_t i = 0; i < n; i++) perm[i] = lo + i;
+  std::nth_element(perm.begin(), perm.begin() + half, perm.end(), [&](size_t a, size_t b) {
+    return u[a][ax] < u[b][ax] || (u[a][ax] == u[b][ax] && id[a] < id[b]);
+  });
+  std::vector<std::array<float, 3>> u2(n);
+  std::vector<int> id2(n);
+  for (size_t i = 0; i < n; i++) { u2[i] = u[perm[i]]; id2[i] = id[perm[i]]; }
+  for (size_t i = 0; i < n; i++) { u[lo + i] = u2[i]; id[lo + i] = id2[i]; }
+  kd_split(u, id, lo, lo + half, out);
+  kd_split(u, id, lo + half, hi, out);
 }
 
-// Tiles of 128 active columns that are close on the sphere: active columns
-// ordered along a Morton curve of (latitude, longitude), cut into runs.
 std::vector<int> build_tiles(const std::vector<int> &act, const float *lat, const float *lon) {
   const size_t n = act.size();
-  std::vector<std::pair<uint32_t, int>> key(n);
+  std::vector<std::array<float, 3>> u(n);
+  std::vector<int> id(act);
   for (size_t i = 0; i < n; i++) {
-    const int c = act[i];
-    double lo = std::fmod((double)lon[c], 360.0);
-    if (lo < 0) lo += 360.0;
-    const uint32_t qa = (uint32_t)std::min(65535.0, std::max(0.0, ((double)lat[c] + 90.0) / 180.0 * 65535.0));
-    const uint32_t qo = (uint32_t)std::min(65535.0, std::max(0.0, lo / 360.0 * 65535.0));
-    key[i] = {spread16(qo) | (spread16(qa) << 1), c};
+    const double p = lat[act[i]] * 0.017453292519943295, l = lon[act[i]] * 0.017453292519943295;
+    u[i] = {(float)(std::cos(p) * std::cos(l)), (float)(std::cos(p) * std::sin(l)), (float)std::sin(p)};
   }
-  std::sort(key.begin(), key.end());
-  const size_t nt = (n + 127) / 128;
-  std::vector<int> tiles(nt * 128, -1);
-  for (size_t i = 0; i < n; i++) tiles[i] = key[i].second;
+  std::vector<int> tiles;
+  tiles.reserve((n / 128 + 2) * 128);
+  if (n > 0) kd_split(u, id, 0, n, tiles);
   return tiles;
 }
 

@@ -150,7 +150,7 @@ __global__ void k_eig(EigArgs a, int wpb) {
           deflate = true;
           break;
         }
-        const float ir = 1.0f / r;
+        const float ir = __frcp_rn(r);
         s = f * ir;
         c = g * ir;
         g = di1 - pp;
@@ -162,18 +162,25 @@ __global__ void k_eig(EigArgs a, int wpb) {
       }
       __syncwarp();
       // apply rotations m-1 .. ilo to columns (i, i+1) of every Z row
+      // (each lane owns rows lane and lane + 32)
       const int ilo = deflate ? i + 1 : l;
       if (ilo <= m - 1) {
-        for (int q = lane; q < k; q += 32) {
-          float *zr = Z + q * ld;
-          float carry = zr[m];
+        const bool two = lane + 32 < k;
+        float *z0 = Z + lane * ld, *z1 = Z + (two ? lane + 32 : lane) * ld;
+        if (lane < k) {
+          float c0 = z0[m], c1 = z1[m];
           for (int ii = m - 1; ii >= ilo; ii--) {
             const float cc = rc[ii], ss = rs[ii];
-            const float zi = zr[ii];
-            zr[ii + 1] = ss * zi + cc * carry;
-            carry = cc * zi - ss * carry;
+            const float a0 = z0[ii], a1 = z1[ii];
+            z0[ii + 1] = ss * a0 + cc * c0;
+            c0 = cc * a0 - ss * c0;
+            if (two) {
+              z1[ii + 1] = ss * a1 + cc * c1;
+              c1 = cc * a1 - ss * c1;
+            }
           }
-          zr[ilo] = carry;
+          z0[ilo] = c0;
+          if (two) z1[ilo] = c1;
         }
       }
       if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
@@ -182,16 +189,30 @@ __global__ void k_eig(EigArgs a, int wpb) {
     if (bad) break;
   }
 
-  // ---- back-transformation V = Q Z (reflectors applied last-to-first)
-  for (int j = k - 3; j >= 0; j--) {
-    const float t = tau[j];
-    if (t == 0.0f) continue;
-    const int m = k - j - 1;
-    for (int c = lane; c < k; c += 32) {
-      float dot = 0.0f;
-      for (int r = 0; r < m; r++) dot = __fmaf_rn(A[(j + 1 + r) * ld + j], Z[(j + 1 + r) * ld + c], dot);
-      dot *= t;
-      for (int r = 0; r < m; r++) Z[(j + 1 + r) * ld + c] -= A[(j + 1 + r) * ld + j] * dot;
+  // ---- back-transformation V = Q Z (reflectors applied last-to-first);
+  // each lane owns columns lane and lane + 32
+  {
+    const bool two = lane + 32 < k;
+    const int c0 = lane, c1 = two ? lane + 32 : lane;
+    for (int j = k - 3; j >= 0; j--) {
+      const float t = tau[j];
+      if (t == 0.0f) continue;
+      const int m = k - j - 1;
+      if (lane < k) {
+        float dot0 = 0.0f, dot1 = 0.0f;
+        for (int r = 0; r < m; r++) {
+          const float v = A[(j + 1 + r) * ld + j];
+          dot0 = __fmaf_rn(v, Z[(j + 1 + r) * ld + c0], dot0);
+          dot1 = __fmaf_rn(v, Z[(j + 1 + r) * ld + c1], dot1);
+        }
+        dot0 *= t;
+        dot1 *= t;
+        for (int r = 0; r < m; r++) {
+          const float v = A[(j + 1 + r) * ld + j];
+          Z[(j + 1 + r) * ld + c0] -= v * dot0;
+          if (two) Z[(j + 1 + r) * ld + c1] -= v * dot1;
+        }
+      }
     }
   }
   __syncwarp();
@@ -222,13 +243,22 @@ __global__ void k_eig(EigArgs a, int wpb) {
   __syncwarp();
   for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] = Z[i * ld + l] * fl[l]; }
   __syncwarp();
-  // T_ij = sum_l Y[i][l] V[j][l] + wbar_i ; lane owns columns j
+  // T_ij = sum_l Y[i][l] V[j][l] + wbar_i ; lane owns columns lane, lane + 32
   float *T = a.T + (size_t)unit * k * k;
-  for (int j = lane; j < k; j += 32) {
+  if (lane < k) {
+    const bool two = lane + 32 < k;
+    const int j0 = lane, j1 = two ? lane + 32 : lane;
+    const float *v0 = Z + j0 * ld, *v1 = Z + j1 * ld;
     for (int i = 0; i < k; i++) {
-      float acc = 0.0f;
-      for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], Z[j * ld + l], acc);
-      T[i * k + j] = acc + w[i];
+      const float *yr = A + i * ld;
+      float acc0 = 0.0f, acc1 = 0.0f;
+      for (int l = 0; l < k; l++) {
+        const float y = yr[l];
+        acc0 = __fmaf_rn(y, v0[l], acc0);
+        acc1 = __fmaf_rn(y, v1[l], acc1);
+      }
+      T[i * k + j0] = acc0 + w[i];
+      if (two) T[i * k + j1] = acc1 + w[i];
     }
   }
   bad = __reduce_or_sync(0xffffffffu, bad);

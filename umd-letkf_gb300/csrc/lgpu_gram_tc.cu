@@ -31,10 +31,11 @@ namespace {
 
 constexpr int TM = 128;        // columns per tile = MMA M = TMEM lanes
 constexpr int KC = 16;         // observations per chunk (two K=8 MMA steps)
-constexpr int NT = 256;        // threads per CTA
+constexpr int NT = 512;        // threads per CTA: warps 0-7 weights, warps 8-15 features
 constexpr int NPMAX = 432;     // features per pass
 constexpr int TMEM_COLS = 512;
 constexpr int MAXSEG = 2 * kNB;
+constexpr int YT_LD = 16;      // transposed staging row: 16 observations of one member
 constexpr uint32_t CMB = 128;                 // bytes per core matrix (8 rows x 16 B)
 constexpr uint32_t SBO = (KC / 4) * CMB;      // bytes per 8-row group (all K of the chunk)
 constexpr uint32_t WB = (TM / 8) * SBO;       // bytes per W operand copy
@@ -50,14 +51,24 @@ struct TcSmem {
   int total;
   uint32_t tmem;
   unsigned long long mbar[2];
-  float4 obsA[KC];
-  float4 obsB[KC];
+  int pos[2][KC];            // sorted positions of the chunk's observations (double buffered)
+  float4 obsA[KC];           // ux, uy, uz, 1/err
+  float4 obsB[KC];           // dep, time, zdim, surf
   int obsValid[KC];
   unsigned char fi[NPMAX];
   unsigned char fj[NPMAX];
   int dcand[TM], dkept[TM];
   float drsum[TM];
 };
+
+__device__ __forceinline__ int run_lookup(const TcSmem &S, int nseg, int jj) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (S.seg_pref[mid] <= jj) lo = mid; else hi = mid - 1;
+  }
+  return S.seg_start[lo] + (jj - S.seg_pref[lo]);
+}
 
 __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
@@ -67,11 +78,10 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   const int g = (blockIdx.x / a.npass) % a.groups;
   const int tile = blockIdx.x / (a.npass * a.groups);
   const int k = a.k, kp = a.kp, NP = a.np, nf = a.nf;
-  const int kyp = kp + 4;
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
   const uint32_t stage_bytes = 2 * WB + 2 * PB;
   unsigned char *stg[2] = {dsm, dsm + stage_bytes};
-  float *oy = reinterpret_cast<float *>(dsm + 2 * stage_bytes);   // [KC][kyp]
+  float *yT = reinterpret_cast<float *>(dsm + 2 * stage_bytes);   // [kp + 4][YT_LD]
 
   // ---- setup: TMEM, barriers, feature table
   if (wid == 0) tc::tmem_alloc(&S.tmem, TMEM_COLS);
@@ -88,10 +98,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     S.fj[f] = (unsigned char)j;
   }
   const TilePar tp = a.tp[tile];
-  // W role: column tid & 127, observations [8*(tid>>7), +8) of each chunk
-  const int wc = tid & (TM - 1), wh = tid >> 7;
+  // weight role (warps 0-7): column tid & 127, observations [8*(tid>>7), +8)
+  const bool wrole = tid < 256;
+  const int wc = tid & (TM - 1), wh = (tid >> 7) & 1;
   const int col = a.tile_cols[(size_t)tile * TM + wc];
-  const bool colv = col >= 0;
+  const bool colv = wrole && col >= 0;
   ColPar cp;
   if (colv) cp = a.cp[col];
   else { cp.ux = cp.uy = cp.uz = 0.0f; cp.rmax = -1.0f; cp.L1 = cp.L2 = 1.0f; cp.ic1 = cp.ic2 = 1.0f; }
@@ -174,6 +185,8 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   }
   const int total = S.total;
   const int nchunks = (total + KC - 1) / KC;
+  if (tid < KC && tid < total) S.pos[0][tid] = run_lookup(S, nseg, tid);
+  __syncthreads();
 
   // MMA N-blocks of this pass: [0, min(NP,256)), [256, NP)
   const int nb0 = NP < 256 ? NP : 256, nb1 = NP - nb0;
@@ -183,41 +196,51 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   bool issued = false, fault = false;
   const float4 *hx4 = reinterpret_cast<const float4 *>(a.obs.hx);
   const int q4 = kp >> 2;
+  // feature role (warps 8-15): features tid-256 and tid (those < NP)
+  const int pf0 = tid - 256;
 
   for (int ch = 0; ch < nchunks; ch++) {
     const int s = ch & 1;
-    // ---- stage the chunk's observations (16 threads per observation)
+    const int pb = ch & 1;
+    // ---- stage: hx transposed to yT[member][obs] (+ dep as member k), obs records
     {
-      const int e = tid >> 4, q = tid & 15;
-      const int jj = ch * KC + e;
-      const bool v = jj < total;
-      int pos = 0;
-      if (v) {
-        int lo = 0, hi = nseg - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (S.seg_pref[mid] <= jj) lo = mid; else hi = mid - 1;
-        }
-        pos = S.seg_start[lo] + (jj - S.seg_pref[lo]);
-      }
-      const float4 B = v ? a.obs.B[pos] : make_float4(0.f, 0.f, 0.f, 0.f);
-      if (q == 0) {
-        S.obsA[e] = v ? a.obs.A[pos] : make_float4(0.f, 0.f, 0.f, 1.f);
-        S.obsB[e] = B;
-        S.obsValid[e] = v;
-      }
-      for (int qq = q; qq <= q4; qq += 16) {     // hx quads, then the quad holding dep at index k
+      const int t = tid;
+      const int nq = q4 + 1;             // hx quads + the quad holding dep at index k
+      if (t < nq * KC) {
+        const int qq = t >> 4, e = t & 15;
+        const int jj = ch * KC + e;
+        const bool v = jj < total;
+        const int pos = v ? S.pos[pb][e] : 0;
         float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
         if (v && qq < q4) y = hx4[(size_t)pos * q4 + qq];
         if (qq == (k >> 2)) {
+          const float dep = v ? a.obs.B[pos].x : 0.0f;
           const int c = k & 3;
-          if (c == 0) y.x = B.x; else if (c == 1) y.y = B.x; else if (c == 2) y.z = B.x; else y.w = B.x;
+          if (c == 0) y.x = dep; else if (c == 1) y.y = dep; else if (c == 2) y.z = dep; else y.w = dep;
         }
-        reinterpret_cast<float4 *>(oy + e * kyp)[qq] = y;
+        yT[(4 * qq + 0) * YT_LD + e] = y.x;
+        yT[(4 * qq + 1) * YT_LD + e] = y.y;
+        yT[(4 * qq + 2) * YT_LD + e] = y.z;
+        yT[(4 * qq + 3) * YT_LD + e] = y.w;
+      } else if (t >= 480 && t < 480 + KC) {
+        const int e = t - 480;
+        const int jj = ch * KC + e;
+        const bool v = jj < total;
+        const int pos = v ? S.pos[pb][e] : 0;
+        float4 A = make_float4(0.f, 0.f, 0.f, 1.f), B = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (v) { A = a.obs.A[pos]; B = a.obs.B[pos]; A.w = __frcp_rn(A.w); }
+        S.obsA[e] = A;
+        S.obsB[e] = B;
+        S.obsValid[e] = v;
+      } else if (t >= 448 && t < 448 + KC) {
+        // positions of the next chunk
+        const int e = t - 448;
+        const int jj = (ch + 1) * KC + e;
+        if (jj < total) S.pos[pb ^ 1][e] = run_lookup(S, nseg, jj);
       }
     }
-    // ---- stage s must be free: thread 0 waits for the MMAs issued two chunks
-    // ago; the barrier publishes the staged observations and the outcome
+    // ---- stage s must be free (MMAs of chunk ch-2 done): thread 0 waits, the
+    // barrier publishes the staged data and the outcome
     {
       bool bad = false;
       if (tid == 0) {
@@ -229,64 +252,66 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       if (__syncthreads_or(bad)) { fault = true; break; }
     }
     unsigned char *Whi = stg[s], *Wlo = stg[s] + WB, *Phi = stg[s] + 2 * WB, *Plo = stg[s] + 2 * WB + PB;
-    // ---- W: localisation weights of column wc for 8 observations
     bool anyk = false;
+    if (wrole) {
+      // ---- W: weights of column wc for 8 observations (exact keep decisions)
 #pragma unroll
-    for (int grp = 0; grp < 2; grp++) {
-      float w4[4];
+      for (int grp = 0; grp < 2; grp++) {
+        float h4[4], l4[4];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int e = wh * 8 + grp * 4 + u;
-        float w = 0.0f;
-        if (colv && S.obsValid[e]) {
+        for (int u = 0; u < 4; u++) {
+          const int e = wh * 8 + grp * 4 + u;
+          float w = 0.0f;
           const float4 A = S.obsA[e];
           const float c2 = chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
-          if (c2 <= c2max) {
+          if (c2 <= c2max && S.obsValid[e]) {
             const float d = dist_from_chord2(c2);
             if (d <= cp.rmax) {
               ncand++;
               const float4 B = S.obsB[e];
               const float r = localize(a.loc, cp, g, d, B.y, B.z, B.w);
               if (r > kKeep) {
-                w = __fdiv_rn(r, A.w);
+                w = r * A.w;
                 nkeep++;
                 rsum += r;
                 anyk = true;
               }
             }
           }
+          tc::split_tf32(w, h4[u], l4[u]);
         }
-        w4[u] = w;
+        const uint32_t off = kmaj(wc, wh * 8 + grp * 4);
+        *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+        *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
       }
-      float h4[4], l4[4];
+    } else {
+      // ---- P: feature products y_i * y_j for 16 observations
 #pragma unroll
-      for (int u = 0; u < 4; u++) tc::split_tf32(w4[u], h4[u], l4[u]);
-      const uint32_t off = kmaj(wc, wh * 8 + grp * 4);
-      *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
-      *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
-    }
-    // ---- P: feature products for 16 observations
-    for (int f = tid; f < NP; f += NT) {
-      const int i = S.fi[f], j = S.fj[f];
-      const bool fv = i != 255;
+      for (int rep = 0; rep < 2; rep++) {
+        const int f = pf0 + 256 * rep;
+        if (f < NP) {
+          const int i = S.fi[f], j = S.fj[f];
+          const bool fv = i != 255;
+          const float4 *yi = reinterpret_cast<const float4 *>(yT + (fv ? i : 0) * YT_LD);
+          const float4 *yj = reinterpret_cast<const float4 *>(yT + (fv ? j : 0) * YT_LD);
 #pragma unroll
-      for (int grp = 0; grp < 4; grp++) {
-        float h4[4], l4[4];
+          for (int grp = 0; grp < 4; grp++) {
+            const float4 a4 = yi[grp], b4 = yj[grp];
+            float v[4] = {a4.x * b4.x, a4.y * b4.y, a4.z * b4.z, a4.w * b4.w};
+            float h4[4], l4[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int e = grp * 4 + u;
-          const float v = fv ? oy[e * kyp + i] * oy[e * kyp + j] : 0.0f;
-          tc::split_tf32(v, h4[u], l4[u]);
+            for (int u = 0; u < 4; u++) tc::split_tf32(fv ? v[u] : 0.0f, h4[u], l4[u]);
+            const uint32_t off = kmaj(f, grp * 4);
+            *reinterpret_cast<float4 *>(Phi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+            *reinterpret_cast<float4 *>(Plo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+          }
         }
-        const uint32_t off = kmaj(f, grp * 4);
-        *reinterpret_cast<float4 *>(Phi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
-        *reinterpret_cast<float4 *>(Plo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
       }
     }
     tc::fence_proxy_async();
     const bool chunk_keep = __syncthreads_or(anyk) != 0;
     // ---- issue: D += Whi*Phi + Whi*Plo + Wlo*Phi
-    if (chunk_keep && !fault) {
+    if (chunk_keep) {
       if (tid == 0) {
         tc::fence_after();
         const uint32_t aw[3] = {tc::smem_u32(Whi), tc::smem_u32(Whi), tc::smem_u32(Wlo)};
@@ -322,7 +347,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   tc::fence_after();
 
   // ---- per-column diagnostics and kept counts (both halves of a column)
-  if (wh == 1) { S.dcand[wc] = ncand; S.dkept[wc] = nkeep; S.drsum[wc] = rsum; }
+  if (wrole && wh == 1) { S.dcand[wc] = ncand; S.dkept[wc] = nkeep; S.drsum[wc] = rsum; }
   __syncthreads();
   const int G = a.groups;
   if (tid < TM) {
@@ -417,7 +442,7 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
 size_t gram_tc_smem_bytes(int k, int np) {
   const int kp = (k + 3) & ~3;
   const size_t PB = (size_t)(np / 8) * SBO;
-  return 2 * (2 * WB + 2 * PB) + (size_t)KC * (kp + 4) * sizeof(float);
+  return 2 * (2 * WB + 2 * PB) + (size_t)(kp + 4) * YT_LD * sizeof(float);
 }
 
 void gram_tc_passes(int k, int *npass, int *np) {

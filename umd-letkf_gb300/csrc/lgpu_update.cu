@@ -56,31 +56,36 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int
   const size_t ubase = (size_t)act * G;
   const int mld = a.cp[col].mld;
   // ---- stage X_b (rows padded to kp) and the transforms
-  if ((k & 3) == 0) {
+  if (kp == k) {   // k a multiple of 4: rows are already 16-byte aligned and unpadded
     const float4 *src = reinterpret_cast<const float4 *>(a.bkg + cbase);
-    const int q = k >> 2;
-    for (int t = threadIdx.x; t < ns * q; t += blockDim.x)
-      reinterpret_cast<float4 *>(xb + (t / q) * kp)[t % q] = src[t];
+    float4 *dst = reinterpret_cast<float4 *>(xb);
+    for (int t = threadIdx.x; t < (ns * k) >> 2; t += blockDim.x) dst[t] = src[t];
   } else {
-    for (int t = threadIdx.x; t < ns * kp; t += blockDim.x) {
-      const int s = t / kp, j = t % kp;
-      xb[t] = j < k ? a.bkg[cbase + (size_t)s * k + j] : 0.0f;
-    }
+    for (int s = warp; s < ns; s += nw)
+      for (int j = lane; j < kp; j += 32) xb[s * kp + j] = j < k ? a.bkg[cbase + (size_t)s * k + j] : 0.0f;
   }
   for (int g = 0; g < tsm_groups; g++) {
     if (a.nkept[ubase + g] <= 0) continue;
     const float *T = a.T + (ubase + g) * k * k;
     float *dst = Ts + (size_t)g * k * kp;
-    for (int t = threadIdx.x; t < k * kp; t += blockDim.x) {
-      const int i = t / kp, j = t % kp;
-      dst[t] = j < k ? T[i * k + j] : 0.0f;
+    if (kp == k) {
+      const float4 *src4 = reinterpret_cast<const float4 *>(T);
+      float4 *dst4 = reinterpret_cast<float4 *>(dst);
+      for (int t = threadIdx.x; t < (k * k) >> 2; t += blockDim.x) dst4[t] = src4[t];
+    } else {
+      for (int i = warp; i < k; i += nw)
+        for (int j = lane; j < kp; j += 32) dst[i * kp + j] = j < k ? T[i * k + j] : 0.0f;
     }
   }
   __syncthreads();
-  // ---- X_a = X_b T_g, four members per work item
+  // ---- X_a = X_b T_g: a warp covers spl slabs per pass, a lane one quad of members
   const int q4 = kp >> 2;
-  for (int t = threadIdx.x; t < ns * q4; t += blockDim.x) {
-    const int s = t / q4, jq = t % q4;
+  const int spl = 32 / q4;
+  const int my_s = lane / q4, jq = lane - my_s * q4;
+  const bool lane_on = my_s < spl;
+  for (int s0 = warp * spl; s0 < ns; s0 += nw * spl) {
+    const int s = s0 + my_s;
+    if (!lane_on || s >= ns) continue;
     const int g = slab_group(a, a.slab_lev[s], mld);
     const bool has = g < G && a.nkept[ubase + g] > 0;
     float4 acc;
