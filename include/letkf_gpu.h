@@ -164,6 +164,31 @@ int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const floa
                    const float *sprd, int nvars, const lgpu_statevar *vars);
 int lgpu_set_obs(lgpu_handle *h, int nobs, const lgpu_obs *obs, const float *hx, const float *hx_mean);
 
+/* letkf_obs_read's post-processing on the device (src/letkf_obs.F90:459-488),
+ * the step before the analysis: hx_members holds the full observation-
+ * operator values of every member [nobs][k]; the library forms
+ * hx_mean = SUM(hx,1)/k and the perturbations, drops observations with
+ * qc > 0 keeping the order of the rest, and then holds what lgpu_set_obs
+ * would.  qc may be NULL (every observation kept).  *nobs_kept receives
+ * the count after compaction. */
+int lgpu_set_obs_raw(lgpu_handle *h, int nobs, const lgpu_obs *obs, const int *qc, const float *hx_members,
+                     int *nobs_kept);
+
+/* letkf_state_init's background statistics on the device
+ * (src/letkf_state.F90:326-334): members holds the full ensemble
+ * [ij][slab][member]; the library forms mean = SUM(x,1)/k, the
+ * perturbations and sprd = SQRT(DOT(x',x')/(k-1)) and then holds what
+ * lgpu_set_state would. */
+int lgpu_set_state_members(lgpu_handle *h, int k, int ns, const float *members, int nvars,
+                           const lgpu_statevar *vars);
+
+/* Verification of the two calls above: copy back the prepared background
+ * (perturbations, mean, spread) and the prepared observation arrays
+ * (kept observations only: hx perturbations [n][k], hx_mean, and the
+ * compacted lat/lon/val/err). */
+int lgpu_get_background(lgpu_handle *h, float *state, float *mean, float *sprd);
+int lgpu_get_obs_prepared(lgpu_handle *h, float *hx, float *hx_mean, float *lat, float *lon, float *val, float *err);
+
 int lgpu_solver_run(lgpu_handle *h);
 
 int lgpu_get_state(lgpu_handle *h, float *state, float *mean, float *sprd);
@@ -178,12 +203,6 @@ int lgpu_solver_final(lgpu_handle *h);
 int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
                      int *n, int *ncand);
 
-/* Verification: evaluate the library's distance metric and Gaspari-Cohn
- * weights on the device.  dist[i] = distance (m) between points
- * (lat1[i], lon1[i]) and (lat2[i], lon2[i]).  gc must hold 2n floats:
- * gc[i] = the fast single-precision weight used in the search loop and
- * gc[n + i] = letkf_loc_gc(z[i], L[i]) evaluated exactly as the reference
- * does (REAL(8), rounded to REAL). */
 /* Page-locked host memory for callers that stream state in and out every
  * analysis (host<->device copies run at full link speed from it). */
 int lgpu_host_alloc(size_t bytes, void **ptr);
@@ -193,9 +212,21 @@ int lgpu_host_free(void *ptr);
  * handle) on the library's stream so the next run starts with a cold L2. */
 int lgpu_flush_l2(lgpu_handle *h, size_t bytes);
 
+/* Verification: evaluate the library's distance metric and Gaspari-Cohn
+ * weights on the device.  dist[i] = distance (m) between points
+ * (lat1[i], lon1[i]) and (lat2[i], lon2[i]).  gc must hold 2n floats:
+ * gc[i] = the fast single-precision weight used in the search loop and
+ * gc[n + i] = letkf_loc_gc(z[i], L[i]) evaluated exactly as the reference
+ * does (REAL(8), rounded to REAL). */
 int lgpu_debug_metric(lgpu_handle *h, int n, const float *lat1, const float *lon1,
                       const float *lat2, const float *lon2, float *dist);
 int lgpu_debug_gc(lgpu_handle *h, int n, const float *z, const float *L, float *gc);
+
+/* Verification of the eigensolve stage alone (src/letkf_core.F90:100-141
+ * with infl = 1): gram holds nunits packed blocks (upper triangle of
+ * Yb^T R^-1 rho Yb row-major, then the right-hand side b; k(k+3)/2 floats);
+ * trans receives T = W + wbar 1^T, [unit][i][j] row-major. */
+int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, float *trans);
 
 #ifdef __cplusplus
 }

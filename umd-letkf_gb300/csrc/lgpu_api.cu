@@ -16,6 +16,14 @@ using namespace lgpu;
 
 namespace lgpu {
 size_t gram_smem_bytes(int k);
+cudaError_t launch_hx_stats(cudaStream_t st, int nobs, int k, float *hx, float *hx_mean, const int *qc, int *flag,
+                            int *pos, int *total);
+cudaError_t launch_compact(cudaStream_t st, int nobs, int k, const int *flag, const int *pos, const float *const *src_f,
+                           float *const *dst_f, int nf, const int *const *src_i, int *const *dst_i, int ni,
+                           const float *hx, float *hx_out, const float *hxm, float *hxm_out);
+cudaError_t launch_state_stats(cudaStream_t st, long long ncs, int k, float *x, float *mean, float *sprd);
+cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
+                             int *status);
 }
 
 namespace {
@@ -46,7 +54,9 @@ enum {
   B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID, B_HX, B_HXM, B_SATOBS, B_SATPLATS,
   B_GEOM, B_CELL, B_COUNT, B_FILL, B_POSTMP, B_ORDER, B_ATMP, B_BTMP, B_SA, B_SB, B_SHX, B_SIDX, B_CSTART,
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
-  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR,
+  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC,
+  B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7, B_RAWQC, B_RAWHX, B_RAWHXM, B_FLAG, B_POS,
+  B_PTRS, B_TOTAL,
   B_COUNT_ALL
 };
 
@@ -332,6 +342,8 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
   const std::vector<int> tiles = build_tiles(act, lat, lon);
   CK(h->buf[B_TILECOLS].ensure(sizeof(int) * std::max<size_t>(1, tiles.size())), "alloc tiles");
   CK(h->buf[B_TILEPAR].ensure(sizeof(TilePar) * std::max<size_t>(1, tiles.size() / 128)), "alloc tiles");
+  CK(h->buf[B_TILEN].ensure(sizeof(int) * std::max<size_t>(1, tiles.size() / 128)), "alloc tiles");
+  CK(h->buf[B_TILEOFF].ensure(sizeof(int) * (tiles.size() / 128 + 1)), "alloc tiles");
   if (!tiles.empty())
     CK(cudaMemcpyAsync(h->buf[B_TILECOLS].p, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice, h->st),
        "H2D tiles");
@@ -433,6 +445,116 @@ int lgpu_set_obs(lgpu_handle *h, int nobs, const lgpu_obs *o, const float *hx, c
   return LGPU_OK;
 }
 
+// src/letkf_obs.F90:459-488 on the device
+int lgpu_set_obs_raw(lgpu_handle *h, int nobs, const lgpu_obs *o, const int *qc, const float *hx_members,
+                     int *nobs_kept) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->state_ok) return fail(h, LGPU_ERR_ORDER, "set_obs_raw before set_state (the ensemble size is needed)");
+  if (nobs < 0 || (nobs > 0 && (!o || !hx_members || !o->lat || !o->lon || !o->zdim || !o->time || !o->val ||
+                                 !o->err || !o->obsid || !o->platid)))
+    return fail(h, LGPU_ERR_ARG, "set_obs_raw: bad arguments");
+  for (int i = 0; i < nobs; i++)
+    if ((!qc || qc[i] <= 0) && !(o->err[i] > 0.0f))
+      return fail(h, LGPU_ERR_ARG, "set_obs_raw: observation error must be > 0 at obs " + std::to_string(i));
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t n = std::max(nobs, 1), k = h->k;
+  const int raw[8] = {B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7};
+  const int dst[8] = {B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID};
+  const void *src[8] = {o ? o->lat : nullptr, o ? o->lon : nullptr, o ? o->zdim : nullptr, o ? o->time : nullptr,
+                        o ? o->val : nullptr, o ? o->err : nullptr, o ? o->obsid : nullptr, o ? o->platid : nullptr};
+  for (int q = 0; q < 8; q++) {
+    CK(h->buf[raw[q]].ensure(n * 4), "alloc raw obs");
+    CK(h->buf[dst[q]].ensure(n * 4), "alloc obs");
+    if (nobs > 0) CK(cudaMemcpyAsync(h->buf[raw[q]].p, src[q], (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D");
+  }
+  CK(h->buf[B_RAWHX].ensure(n * k * 4), "alloc raw hx");
+  CK(h->buf[B_RAWHXM].ensure(n * 4), "alloc");
+  CK(h->buf[B_HX].ensure(n * k * 4), "alloc hx");
+  CK(h->buf[B_HXM].ensure(n * 4), "alloc hx_mean");
+  CK(h->buf[B_RAWQC].ensure(n * 4), "alloc");
+  CK(h->buf[B_FLAG].ensure(n * 4), "alloc");
+  CK(h->buf[B_POS].ensure(n * 4), "alloc");
+  CK(h->buf[B_TOTAL].ensure(16), "alloc");
+  CK(h->buf[B_PTRS].ensure(32 * sizeof(void *)), "alloc");
+  if (nobs > 0) {
+    CK(cudaMemcpyAsync(h->buf[B_RAWHX].p, hx_members, (size_t)nobs * k * 4, cudaMemcpyHostToDevice, h->st), "H2D hx");
+    if (qc) CK(cudaMemcpyAsync(h->buf[B_RAWQC].p, qc, (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D qc");
+  }
+  CK(launch_hx_stats(h->st, nobs, (int)k, h->buf[B_RAWHX].as<float>(), h->buf[B_RAWHXM].as<float>(),
+                     qc ? h->buf[B_RAWQC].as<int>() : nullptr, h->buf[B_FLAG].as<int>(), h->buf[B_POS].as<int>(),
+                     h->buf[B_TOTAL].as<int>()),
+     "hx statistics");
+  void *ptrs[32];
+  for (int q = 0; q < 6; q++) { ptrs[q] = h->buf[raw[q]].p; ptrs[8 + q] = h->buf[dst[q]].p; }
+  for (int q = 0; q < 2; q++) { ptrs[16 + q] = h->buf[raw[6 + q]].p; ptrs[24 + q] = h->buf[dst[6 + q]].p; }
+  CK(cudaMemcpyAsync(h->buf[B_PTRS].p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, h->st), "H2D ptrs");
+  void **dp = h->buf[B_PTRS].as<void *>();
+  CK(launch_compact(h->st, nobs, (int)k, h->buf[B_FLAG].as<int>(), h->buf[B_POS].as<int>(),
+                    reinterpret_cast<const float *const *>(dp), reinterpret_cast<float *const *>(dp + 8), 6,
+                    reinterpret_cast<const int *const *>(dp + 16), reinterpret_cast<int *const *>(dp + 24), 2,
+                    h->buf[B_RAWHX].as<float>(), h->buf[B_HX].as<float>(), h->buf[B_RAWHXM].as<float>(),
+                    h->buf[B_HXM].as<float>()),
+     "observation compaction");
+  int kept = 0;
+  CK(cudaMemcpyAsync(&kept, h->buf[B_TOTAL].p, 4, cudaMemcpyDeviceToHost, h->st), "D2H total");
+  CK(cudaStreamSynchronize(h->st), "set_obs_raw");
+  h->nobs = kept;
+  if (nobs_kept) *nobs_kept = kept;
+  h->obs_ok = true;
+  h->ran = false;
+  return LGPU_OK;
+}
+
+// src/letkf_state.F90:326-334 on the device
+int lgpu_set_state_members(lgpu_handle *h, int k, int ns, const float *members, int nvars, const lgpu_statevar *vars) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!members) return fail(h, LGPU_ERR_ARG, "set_state_members: bad arguments");
+  // validate and upload exactly as lgpu_set_state, with the members in place of the perturbations
+  const size_t nm = (size_t)h->ncol * (ns > 0 ? ns : 1);
+  int rc = LGPU_OK;
+  {
+    // lgpu_set_state copies mean/sprd from the host; give it placeholders and
+    // overwrite them with the device statistics below
+    std::vector<float> tmp(nm, 0.0f);
+    rc = lgpu_set_state(h, k, ns, members, tmp.data(), tmp.data(), nvars, vars);
+  }
+  if (rc != LGPU_OK) return rc;
+  CK(launch_state_stats(h->st, (long long)h->ncol * ns, k, h->buf[B_BKG].as<float>(), h->buf[B_MEANB].as<float>(),
+                        h->buf[B_SPRDB].as<float>()),
+     "background statistics");
+  CK(cudaStreamSynchronize(h->st), "set_state_members");
+  return LGPU_OK;
+}
+
+int lgpu_get_background(lgpu_handle *h, float *state, float *mean, float *sprd) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->state_ok) return fail(h, LGPU_ERR_ORDER, "get_background before set_state");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t nx = (size_t)h->ncol * h->ns * h->k, nm = (size_t)h->ncol * h->ns;
+  if (state) CK(cudaMemcpyAsync(state, h->buf[B_BKG].p, nx * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  if (mean) CK(cudaMemcpyAsync(mean, h->buf[B_MEANB].p, nm * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  if (sprd) CK(cudaMemcpyAsync(sprd, h->buf[B_SPRDB].p, nm * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  CK(cudaStreamSynchronize(h->st), "get_background");
+  return LGPU_OK;
+}
+
+int lgpu_get_obs_prepared(lgpu_handle *h, float *hx, float *hx_mean, float *lat, float *lon, float *val, float *err) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->obs_ok) return fail(h, LGPU_ERR_ORDER, "get_obs_prepared before set_obs");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t n = h->nobs, k = h->k;
+  if (n > 0) {
+    if (hx) CK(cudaMemcpyAsync(hx, h->buf[B_HX].p, n * k * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+    if (hx_mean) CK(cudaMemcpyAsync(hx_mean, h->buf[B_HXM].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+    if (lat) CK(cudaMemcpyAsync(lat, h->buf[B_OLAT].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+    if (lon) CK(cudaMemcpyAsync(lon, h->buf[B_OLON].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+    if (val) CK(cudaMemcpyAsync(val, h->buf[B_OVAL].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+    if (err) CK(cudaMemcpyAsync(err, h->buf[B_OERR].p, n * 4, cudaMemcpyDeviceToHost, h->st), "D2H");
+  }
+  CK(cudaStreamSynchronize(h->st), "get_obs_prepared");
+  return LGPU_OK;
+}
+
 // letkf_solver_run (src/letkf_solver.F90:150-389)
 int lgpu_solver_run(lgpu_handle *h) {
   if (!h) return LGPU_ERR_ARG;
@@ -523,6 +645,19 @@ int lgpu_solver_run(lgpu_handle *h) {
   if (use_tc) {
     CK(launch_tile_prep(st, h->ntiles, h->buf[B_TILECOLS].as<int>(), h->buf[B_CP].as<ColPar>(),
                         h->buf[B_TILEPAR].as<TilePar>(), &launches), "tile prep");
+    // tile candidate streams: count, size the record buffer, fill
+    CK(launch_tile_count(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os,
+                         h->buf[B_TILEN].as<int>(), h->buf[B_TILEOFF].as<int>(), &launches),
+       "tile count");
+    int nchunk_total = 0;
+    CK(cudaMemcpyAsync(&nchunk_total, h->buf[B_TILEOFF].as<int>() + h->ntiles, sizeof(int), cudaMemcpyDeviceToHost, st),
+       "D2H stream size");
+    CK(cudaStreamSynchronize(st), "stream size sync");
+    CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
+    CK(launch_tile_fill(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
+                        h->buf[B_TILEOFF].as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
+                        h->buf[B_STATUS].as<int>(), &launches),
+       "tile fill");
     TcArgs ta;
     ta.ntiles = h->ntiles;
     ta.groups = G;
@@ -534,10 +669,10 @@ int lgpu_solver_run(lgpu_handle *h) {
     ta.tile_cols = h->buf[B_TILECOLS].as<int>();
     ta.col2act = h->buf[B_COL2ACT].as<int>();
     ta.cp = h->buf[B_CP].as<ColPar>();
-    ta.tp = h->buf[B_TILEPAR].as<TilePar>();
     ta.loc = h->loc;
-    ta.obs = os;
-    ta.geom = h->buf[B_GEOM].as<IndexGeom>();
+    ta.rec = h->buf[B_TILEREC].as<unsigned char>();
+    ta.tile_off = h->buf[B_TILEOFF].as<int>();
+    ta.tile_n = h->buf[B_TILEN].as<int>();
     ta.G = h->buf[B_G].as<float>();
     ta.nkept = h->buf[B_NKEPT].as<int>();
     ta.diag_obscount = h->buf[B_DOBSC].as<float>();
@@ -713,6 +848,35 @@ int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, i
   }
   *n = cnt[0];
   if (ncand) *ncand = cnt[1];
+  return LGPU_OK;
+}
+
+int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, float *trans) {
+  if (!h || nunits < 0 || (nunits > 0 && (!gram || !trans))) return LGPU_ERR_ARG;
+  if (k < 2 || k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "debug_transform: k outside [2, 64]");
+  if (nunits == 0) return LGPU_OK;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const size_t nf = packed_size(k), nt = (size_t)k * k;
+  float *dG = nullptr, *dT = nullptr;
+  int *dn = nullptr;
+  CK(cudaMalloc(&dG, 4 * nf * nunits), "alloc");
+  cudaError_t e = cudaMalloc(&dT, 4 * nt * nunits);
+  if (e == cudaSuccess) e = cudaMalloc(&dn, 4 * ((size_t)nunits + 1));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dG, gram, 4 * nf * nunits, cudaMemcpyHostToDevice, h->st);
+  std::vector<int> ones(nunits + 1, 1);
+  ones[nunits] = 0;   // status word
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dn, ones.data(), 4 * ((size_t)nunits + 1), cudaMemcpyHostToDevice, h->st);
+  if (e == cudaSuccess) e = launch_eig_debug(h->st, nunits, k, dG, dn, dT, dn + nunits);
+  int status = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(trans, dT, 4 * nt * nunits, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status, dn + nunits, 4, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cudaFree(dG);
+  cudaFree(dT);
+  cudaFree(dn);
+  if (e != cudaSuccess) return cuda_fail(h, e, "debug_transform");
+  if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
+  if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");
   return LGPU_OK;
 }
 

@@ -125,10 +125,15 @@ __global__ void k_eig(EigArgs a, int wpb) {
   for (int l = 0; l < k; l++) {
     int iter = 0;
     for (;;) {
-      int m = l;
-      for (; m < k - 1; m++) {
-        const float dd = fabsf(d[m]) + fabsf(d[m + 1]);
-        if (fabsf(e[m]) <= 1.1920929e-7f * dd) break;
+      // first m >= l with a negligible e[m] (m = k-1 if none): lanes test
+      // 32 consecutive candidates at a time
+      int m = k - 1;
+      for (int base = l; base < k - 1; base += 32) {
+        const int mm = base + lane;
+        bool small = false;
+        if (mm < k - 1) small = fabsf(e[mm]) <= 1.1920929e-7f * (fabsf(d[mm]) + fabsf(d[mm + 1]));
+        const unsigned bal = __ballot_sync(0xffffffffu, small);
+        if (bal) { m = base + __ffs(bal) - 1; break; }
       }
       if (m == l) break;
       if (++iter > 60) { bad = 1; break; }
@@ -266,6 +271,22 @@ __global__ void k_eig(EigArgs a, int wpb) {
 }
 
 }  // namespace
+
+cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
+
+cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
+                             int *status) {
+  EigArgs a;
+  a.nunits = nunits;
+  a.k = k;
+  a.infl = 1.0f;
+  a.G = G;
+  a.nkept = nkept;
+  a.T = T;
+  a.status = status;
+  int l = 0;
+  return launch_eig(st, a, &l);
+}
 
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches) {
   if (a.nunits <= 0) return cudaSuccess;

@@ -45,6 +45,7 @@ struct __align__(16) GramSmem {
   int ncand_chunk;
 };
 
+template <bool TWO>
 __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
   extern __shared__ __align__(16) float dyn[];
   __shared__ GramSmem S;
@@ -61,6 +62,9 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
   const int tile = gram_thread ? tid % ntiles : 0;
   const int slice = gram_thread ? tid / ntiles : 0;
   const int mi = tile / ntn, ni = tile % ntn;
+  // more tiles than threads (k > 60): threads also own tile tid + GT
+  const bool tile2 = TWO && ntiles > GT && tid + GT < ntiles;
+  const int mi2 = tile2 ? (tid + GT) / ntn : 0, ni2 = tile2 ? (tid + GT) % ntn : 0;
 
   for (int unit = blockIdx.x; unit < a.nunits; unit += gridDim.x) {
     const int act = unit / a.groups, g = unit % a.groups;
@@ -143,11 +147,15 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
     const int total = S.total;
 
     // ---- 2. stream candidates, localize, compact, accumulate
-    float acc[4][4];
+    float acc[4][4], acc2[TWO ? 4 : 1][4];
 #pragma unroll
     for (int r = 0; r < 4; r++)
 #pragma unroll
       for (int c = 0; c < 4; c++) acc[r][c] = 0.0f;
+#pragma unroll
+    for (int r = 0; r < (TWO ? 4 : 1); r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc2[r][c] = 0.0f;
     int head = 0, tail = 0;          // ring indices (monotone)
     int ncand = 0, nkept = 0;        // block totals
     float rsum = 0.0f;               // per-thread partial sum of kept weights
@@ -252,6 +260,20 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
 #pragma unroll
               for (int c = 0; c < 4; c++) acc[r2][c] = __fmaf_rn(ar[r2], br[c], acc[r2][c]);
           }
+          if constexpr (TWO) if (tile2) {
+            const float *ap2 = As + 4 * mi2;
+            const float *bp2 = Bs + 4 * ni2;
+            for (int e = 0; e < cnt; e++) {
+              const float4 av = *reinterpret_cast<const float4 *>(ap2 + e * kp);
+              const float4 bv = *reinterpret_cast<const float4 *>(bp2 + e * kb);
+              const float ar[4] = {av.x, av.y, av.z, av.w};
+              const float br[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+              for (int r2 = 0; r2 < 4; r2++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc2[TWO ? r2 : 0][c] = __fmaf_rn(ar[r2], br[c], acc2[TWO ? r2 : 0][c]);
+            }
+          }
         }
         head += cnt;
         __syncthreads();
@@ -272,6 +294,13 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
       }
       __syncthreads();
     }
+    if constexpr (TWO) if (tile2) {
+#pragma unroll
+      for (int r2 = 0; r2 < 4; r2++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) red[(tid + GT) * 16 + r2 * 4 + c] = acc2[TWO ? r2 : 0][c];
+    }
+    __syncthreads();
     float *G = a.G + (size_t)unit * packed_size(k);
     for (int t = tid; t < packed_size(k); t += GT) {
       int i, jj;
@@ -365,10 +394,14 @@ size_t gram_smem_bytes(int k) {
 cudaError_t launch_gram(cudaStream_t st, const GramArgs &a, int *launches) {
   if (a.nunits <= 0) return cudaSuccess;
   const size_t smem = gram_smem_bytes(a.k);
-  cudaError_t e = cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int kp = (a.k + 3) & ~3;
+  const bool two = (kp / 4) * ((a.k + 1 + 3) / 4) > GT;
+  cudaError_t e = two ? cudaFuncSetAttribute(k_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                      : cudaFuncSetAttribute(k_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int grid = a.nunits;
-  k_gram<<<grid, GT, smem, st>>>(a);
+  if (two) k_gram<true><<<grid, GT, smem, st>>>(a);
+  else k_gram<false><<<grid, GT, smem, st>>>(a);
   (*launches)++;
   return cudaGetLastError();
 }

@@ -12,16 +12,38 @@
 //
 // M = 128 columns, N = the k(k+3)/2 packed features (split into passes of at
 // most 432 so the accumulator fits TMEM), K = candidate observations in
-// chunks of 16.  Per chunk, CUDA-core threads evaluate the exact distance and
-// the localizer for every (column, observation) pair (bit-identical keep
-// decisions to the per-column path), form the feature products, split both
-// operands into tf32 hi + lo parts and store them in the no-swizzle K-major
-// core-matrix layout; one thread issues tcgen05.mma kind::tf32 for the
-// three products hi*hi + hi*lo + lo*hi with FP32 accumulation in TMEM
-// (relative error ~2^-21 per product, FP32-class).  Two shared-memory stages
-// let the tensor cores run while the next chunk is produced; chunks in which
-// no column keeps any observation issue no MMA.  The epilogue reads TMEM
-// lane c = column c and writes the packed Gram block of each unit.
+// chunks of 16.
+//
+// Candidate streams.  Before the GEMM, three small kernels turn each tile's
+// search window (latitude bands x longitude range of its cap) into a record
+// stream: every observation inside the tile's cap, in window order, packed
+// per chunk of 16 as [16 x (ux,uy,uz,err)] [16 x (dep,time,zdim,surf)]
+// [member-major y: (k+1 rounded to 4) rows x 16] -- one contiguous block per
+// chunk, read once per (group, pass) CTA with one bulk async copy.
+//
+// GEMM CTA roles (17 warps):
+//   warps 0-15  producers; thread t owns column t % 128 for observations
+//               [4 (t / 128), +4) of each chunk and feature t:
+//               weights: the distance (fast float path without branches;
+//               the exact metric and the per-column localizer where the
+//               fast value lies near the search radius or the keep
+//               threshold: bit-identical keep decisions to the per-column
+//               path), W = rloc / err;
+//               features: y_i * y_j, y_i * dep over the chunk;
+//               both operands are split into tf32 hi + lo parts and stored
+//               in the no-swizzle K-major core-matrix layout of an operand
+//               stage;
+//   warp 16     one thread keeps the record ring filled (cp.async.bulk, one
+//               per chunk, mbarrier transaction counts; a slot is refilled
+//               once every producer has finished the chunk in it), issues
+//               tcgen05.mma kind::tf32 for hi*hi + hi*lo + lo*hi (FP32
+//               accumulation in TMEM, relative error ~2^-21 per product) and
+//               frees the stage with tcgen05.commit; chunks in which no
+//               column keeps an observation issue no MMA.
+// The epilogue reads TMEM lane c = column c and writes the packed Gram block
+// of each unit.  Every wait is bounded; a wait that runs out sets status bit
+// 16, the MMA thread waits (bounded) for its copies in flight and TMEM is
+// freed.
 #include "lgpu_internal.cuh"
 #include "lgpu_tc.cuh"
 
@@ -31,45 +53,319 @@ namespace {
 
 constexpr int TM = 128;        // columns per tile = MMA M = TMEM lanes
 constexpr int KC = 16;         // observations per chunk (two K=8 MMA steps)
-constexpr int NT = 512;        // threads per CTA: warps 0-7 weights, warps 8-15 features
+constexpr int NPW = 16;        // producer warps: 0-7 weights, 8-15 features
+constexpr int MMA_WARP = NPW;
+constexpr int NT = 32 * (NPW + 1);
 constexpr int NPMAX = 432;     // features per pass
-constexpr int TMEM_COLS = 512;
-constexpr int MAXSEG = 2 * kNB;
-constexpr int YT_LD = 16;      // transposed staging row: 16 observations of one member
+constexpr int NSMAX = 3, NRMAX = 8;
 constexpr uint32_t CMB = 128;                 // bytes per core matrix (8 rows x 16 B)
 constexpr uint32_t SBO = (KC / 4) * CMB;      // bytes per 8-row group (all K of the chunk)
 constexpr uint32_t WB = (TM / 8) * SBO;       // bytes per W operand copy
+constexpr float kGuardFast = 3.0e-6f;         // keep-threshold band where the exact distance is re-evaluated
+constexpr size_t kSmemBudget = 227 * 1024 - 4096;   // dynamic shared memory (static part below 4 KB)
+constexpr int WT = 256;        // threads of the stream kernels
+constexpr int YS = 20;         // floats per member row of a chunk record (16 observations + 4: conflict-free rows)
 
 __device__ __forceinline__ uint32_t kmaj(int row, int kk) {
   return (uint32_t)(row >> 3) * SBO + (uint32_t)(kk >> 2) * CMB + (uint32_t)(row & 7) * 16u + (uint32_t)(kk & 3) * 4u;
 }
 
-struct TcSmem {
-  int seg_start[MAXSEG];
-  int seg_pref[MAXSEG + 1];
-  int wsc[NT / 32];
-  int total;
-  uint32_t tmem;
-  unsigned long long mbar[2];
-  int pos[2][KC];            // sorted positions of the chunk's observations (double buffered)
-  float4 obsA[KC];           // ux, uy, uz, 1/err
-  float4 obsB[KC];           // dep, time, zdim, surf
-  int obsValid[KC];
-  unsigned char fi[NPMAX];
-  unsigned char fj[NPMAX];
-  int dcand[TM], dkept[TM];
-  float drsum[TM];
-};
-
-__device__ __forceinline__ int run_lookup(const TcSmem &S, int nseg, int jj) {
-  int lo = 0, hi = nseg - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (S.seg_pref[mid] <= jj) lo = mid; else hi = mid - 1;
-  }
-  return S.seg_start[lo] + (jj - S.seg_pref[lo]);
+__device__ __forceinline__ bool in_cap(const TilePar &t, float4 A) {
+  const float dx = __fsub_rn(t.cx, A.x), dy = __fsub_rn(t.cy, A.y), dz = __fsub_rn(t.cz, A.z);
+  return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz)) <= t.c2cap;
 }
 
+// ---------------------------------------------------------------------------
+// Search window of a tile as runs of the cell-sorted observation table
+// (per latitude band at most two runs, the second for a window across 0/360),
+// concatenated: candidate j of the window lives at seg_start[s] + j -
+// seg_pref[s] for the last s with seg_pref[s] <= j.  Block of WT threads.
+struct Window {
+  int seg_start[2 * kNB];
+  int seg_pref[2 * kNB + 1];
+  int wsc[WT / 32];
+  int nseg, total;
+};
+
+__device__ void build_window(Window &W, const TilePar &tp, const IndexGeom *geom, const int *cell_start) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nb = tp.b1 - tp.b0 + 1;
+  int l0 = 0, l1 = 0;
+  if (tid < nb) {
+    const int b = tp.b0 + tid;
+    const int nl = geom->nlon[b], off = geom->off[b];
+    int s0 = 0, s1 = 0;
+    bool whole = tp.dlon >= 180.0f;
+    int clo = 0, chi = nl - 1;
+    if (!whole) {
+      clo = (int)floorf((tp.lonn - tp.dlon) * (float)nl / 360.0f);
+      chi = (int)floorf((tp.lonn + tp.dlon) * (float)nl / 360.0f);
+      if (chi - clo + 1 >= nl) whole = true;
+    }
+    if (whole) {
+      s0 = cell_start[off];
+      l0 = cell_start[off + nl] - s0;
+    } else if (clo < 0) {
+      s0 = cell_start[off + clo + nl];
+      l0 = cell_start[off + nl] - s0;
+      s1 = cell_start[off];
+      l1 = cell_start[off + chi + 1] - s1;
+    } else if (chi >= nl) {
+      s0 = cell_start[off + clo];
+      l0 = cell_start[off + nl] - s0;
+      s1 = cell_start[off];
+      l1 = cell_start[off + (chi - nl) + 1] - s1;
+    } else {
+      s0 = cell_start[off + clo];
+      l0 = cell_start[off + chi + 1] - s0;
+    }
+    W.seg_start[2 * tid] = s0;
+    W.seg_start[2 * tid + 1] = s1;
+  }
+  const int x = l0 + l1;
+  int incl = x;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) W.wsc[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int sv = lane < WT / 32 ? W.wsc[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, sv, o);
+      if (lane >= o) sv += y;
+    }
+    if (lane < WT / 32) W.wsc[lane] = sv;
+  }
+  __syncthreads();
+  const int base = (wid > 0 ? W.wsc[wid - 1] : 0) + incl - x;
+  if (tid < nb) {
+    W.seg_pref[2 * tid] = base;
+    W.seg_pref[2 * tid + 1] = base + l0;
+  }
+  if (tid == 0) {
+    W.nseg = 2 * nb;
+    W.total = W.wsc[WT / 32 - 1];
+    W.seg_pref[2 * nb] = W.total;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int window_pos(const Window &W, int j) {
+  int lo = 0, hi = W.nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (W.seg_pref[mid] <= j) lo = mid; else hi = mid - 1;
+  }
+  return W.seg_start[lo] + (j - W.seg_pref[lo]);
+}
+
+// candidates per tile: observations of the window inside the tile's cap
+__global__ void __launch_bounds__(WT) k_tile_count(int ntiles, const TilePar *tps, const IndexGeom *geom,
+                                                   const float4 *obsA, const int *cell_start, int *tile_n) {
+  __shared__ Window W;
+  __shared__ int red[WT / 32];
+  const int tile = blockIdx.x;
+  const TilePar tp = tps[tile];
+  build_window(W, tp, geom, cell_start);
+  int cnt = 0;
+  for (int j = threadIdx.x; j < W.total; j += WT) cnt += in_cap(tp, obsA[window_pos(W, j)]);
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < WT / 32; w++) t += red[w];
+    tile_n[tile] = t;
+  }
+}
+
+// chunk offsets of the tile streams: tile_off[t] = sum over earlier tiles of
+// ceil(n / 16); tile_off[ntiles] = total chunks.  One block.
+__global__ void k_tile_scan(int ntiles, const int *tile_n, int *tile_off) {
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int base = 0; base < ntiles; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < ntiles ? (tile_n[i] + KC - 1) / KC : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int s = lane < nw ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      if (lane < nw) wsum[lane] = s;
+    }
+    __syncthreads();
+    const int excl = carry + (w > 0 ? wsum[w - 1] : 0) + x - v;
+    if (i < ntiles) tile_off[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) tile_off[ntiles] = carry;
+}
+
+// one record entry: slot e of chunk c of the tile stream
+__device__ __forceinline__ void put_record(unsigned char *rec0, int cb, int k, int kp, int kr, int q, const float4 &A,
+                                           const float4 &B, const float *hx) {
+  unsigned char *r = rec0 + (size_t)(q >> 4) * cb;
+  const int e = q & 15;
+  reinterpret_cast<float4 *>(r)[e] = A;
+  reinterpret_cast<float4 *>(r + 256)[e] = B;
+  float *yT = reinterpret_cast<float *>(r + 512);
+  if (hx) {
+    const float4 *h4 = reinterpret_cast<const float4 *>(hx);
+    for (int qq = 0; qq < (kp >> 2); qq++) {
+      const float4 v = h4[qq];
+      const int i = 4 * qq;
+      if (i + 0 < k) yT[(i + 0) * YS + e] = v.x;
+      if (i + 1 < k) yT[(i + 1) * YS + e] = v.y;
+      if (i + 2 < k) yT[(i + 2) * YS + e] = v.z;
+      if (i + 3 < k) yT[(i + 3) * YS + e] = v.w;
+    }
+    yT[k * YS + e] = B.x;
+  } else {
+    for (int i = 0; i <= k; i++) yT[i * YS + e] = 0.0f;
+  }
+  for (int i = k + 1; i < kr; i++) yT[i * YS + e] = 0.0f;
+  if (e < YS - 16)
+    for (int i = 0; i < kr; i++) yT[i * YS + 16 + e] = 0.0f;
+}
+
+// tile streams: the window scanned again in order, cap members compacted
+// (order preserving) into the tile's chunk records; the last chunk padded
+// with zero entries
+__global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps, const IndexGeom *geom, ObsSorted obs,
+                                                  int k, int kp, int kr, int cb, const int *tile_off,
+                                                  unsigned char *rec, int *status) {
+  __shared__ Window W;
+  __shared__ int wsc[WT / 32];
+  const int tile = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const TilePar tp = tps[tile];
+  build_window(W, tp, geom, obs.cell_start);
+  const int c0 = tile_off[tile];
+  const int cap = (tile_off[tile + 1] - c0) * KC;
+  unsigned char *rec0 = rec + (size_t)c0 * cb;
+  int base = 0;
+  for (int jb = 0; jb < W.total; jb += WT) {
+    const int j = jb + tid;
+    int p = 0;
+    float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool ok = false;
+    if (j < W.total) {
+      p = window_pos(W, j);
+      A = obs.A[p];
+      ok = in_cap(tp, A);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) wsc[wid] = __popc(m);
+    __syncthreads();
+    int before = 0, cnt = 0;
+    for (int w = 0; w < WT / 32; w++) {
+      before += w < wid ? wsc[w] : 0;
+      cnt += wsc[w];
+    }
+    const int q = base + before + __popc(m & ((1u << lane) - 1u));
+    if (ok) {
+      if (q < cap) put_record(rec0, cb, k, kp, kr, q, A, obs.B[p], obs.hx + (size_t)p * kp);
+      else atomicOr(status, 16);
+    }
+    base += cnt;
+    __syncthreads();
+  }
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int q = base + tid; q < cap; q += WT) put_record(rec0, cb, k, kp, kr, q, z, z, nullptr);
+  if (tid == 0 && (base > cap || cap - base >= KC)) atomicOr(status, 16);   // count and fill disagree
+}
+
+struct TcSmem {
+  unsigned long long full[NSMAX], empty[NSMAX], rfull[NRMAX], done;
+  int anyk[NSMAX];           // chunk index + 1 of the last chunk of the stage with a kept pair
+  uint32_t tmem;
+  int issued;
+  int fault;
+  unsigned char fi[NPMAX];
+  unsigned char fj[NPMAX];
+};
+
+// asin(x), 0 <= x <= 0.5: Taylor series of asin to x^21 in Horner form with
+// fused multiply-adds (a few ulp)
+__device__ __forceinline__ float asin_fast(float x) {
+  const float x2 = x * x;
+  float p = 0.008390335366129875f;
+  p = __fmaf_rn(p, x2, 0.009761609137058258f);
+  p = __fmaf_rn(p, x2, 0.01155180111527443f);
+  p = __fmaf_rn(p, x2, 0.013964843936264515f);
+  p = __fmaf_rn(p, x2, 0.017352763563394547f);
+  p = __fmaf_rn(p, x2, 0.022372158244252205f);
+  p = __fmaf_rn(p, x2, 0.0303819440305233f);
+  p = __fmaf_rn(p, x2, 0.0446428582072258f);
+  p = __fmaf_rn(p, x2, 0.07500000298023224f);
+  p = __fmaf_rn(p, x2, 0.1666666716337204f);
+  return __fmaf_rn(x * x2, p, x);
+}
+
+// Gaspari-Cohn of zc = |z| / c without branches: the same two polynomials as
+// gc_fast (outer one in the shifted variable t = 2 - zc, divided by zc with
+// the approximate divide); within 1e-6 of gc_exact.
+__device__ __forceinline__ float gc_branchless(float zc) {
+  const float t = 2.0f - zc;
+  float q = 0.08333f;
+  q = __fmaf_rn(q, t, -0.49996f);
+  q = __fmaf_rn(q, t, 0.6248f);
+  q = __fmaf_rn(q, t, 0.0005299999999996974f);
+  q = __fmaf_rn(q, t, -0.0007799999999991147f);
+  q = __fmaf_rn(q, t, 0.0005999999999986017f);
+  q = __fmaf_rn(q, t, -0.0001899999999991353f);
+  const float qo = __fdividef(q, zc);
+  float p = -0.25f;
+  p = __fmaf_rn(p, zc, 0.5f);
+  p = __fmaf_rn(p, zc, 0.625f);
+  p = __fmaf_rn(p, zc, -1.66667f);
+  const float pi = __fmaf_rn(p, zc * zc, 1.0f);
+  return zc >= 2.0f ? 0.0f : (zc > 1.0f ? qo : pi);
+}
+
+// per-CTA constants of the localizer's fast path
+struct LocK {
+  float icv, levg;            // vtgc: vertical 1/c, depth of the group's level
+  float tprof, tsat;          // ocean: time scales (0 = off)
+  float ictp, icts;           // ocean: their 1/c
+};
+
+// fast localisation weight (no branches); LOC selects the localizer class
+template <int LOC>
+__device__ __forceinline__ float loc_fast(const LocK &lk, const ColPar &cp, int g, float d, const float4 &B) {
+  if (LOC == LOC_VTGC) {
+    return gc_branchless(d * cp.ic1) * gc_branchless(fabsf(B.z - lk.levg) * lk.icv);
+  } else if (LOC == LOC_OCEAN) {
+    const bool sat = B.w != 0.0f;
+    const float rh = gc_branchless(d * (sat ? cp.ic2 : cp.ic1));
+    const float tl = sat ? lk.tsat : lk.tprof;
+    const float rt = tl > 0.0f ? gc_branchless(fabsf(B.y) * (sat ? lk.icts : lk.ictp)) : 1.0f;
+    return (sat && g == 1) ? 0.0f : rh * rt;
+  } else {
+    return gc_branchless(d * cp.ic1);
+  }
+}
+
+__device__ __forceinline__ void bar_arrive(unsigned long long *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(b)) : "memory");
+}
+
+template <int LOC, int NS, int NR>
 __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(16) TcSmem S;
@@ -77,17 +373,28 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   const int pass = blockIdx.x % a.npass;
   const int g = (blockIdx.x / a.npass) % a.groups;
   const int tile = blockIdx.x / (a.npass * a.groups);
-  const int k = a.k, kp = a.kp, NP = a.np, nf = a.nf;
+  const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
   const uint32_t stage_bytes = 2 * WB + 2 * PB;
-  unsigned char *stg[2] = {dsm, dsm + stage_bytes};
-  float *yT = reinterpret_cast<float *>(dsm + 2 * stage_bytes);   // [kp + 4][YT_LD]
+  auto stage_ptr = [&](int s) { return dsm + (size_t)s * stage_bytes; };
+  unsigned char *ring = dsm + (size_t)NS * stage_bytes;
+  const int c0 = a.tile_off[tile];
+  const int nchunks = a.tile_off[tile + 1] - c0;
+  const int ntile = a.tile_n[tile];
+  const uint32_t tmem_cols = a.tmem_cols;
 
   // ---- setup: TMEM, barriers, feature table
-  if (wid == 0) tc::tmem_alloc(&S.tmem, TMEM_COLS);
+  if (wid == 0) tc::tmem_alloc(&S.tmem, tmem_cols);
   if (tid == 0) {
-    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.mbar[0]), 1);
-    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.mbar[1]), 1);
+    for (int s = 0; s < NS; s++) {
+      tc::mbar_init(reinterpret_cast<uint64_t *>(&S.full[s]), NPW);
+      tc::mbar_init(reinterpret_cast<uint64_t *>(&S.empty[s]), 1);
+      S.anyk[s] = 0;
+    }
+    for (int r = 0; r < NR; r++) tc::mbar_init(reinterpret_cast<uint64_t *>(&S.rfull[r]), 1);
+    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.done), 1);
+    S.issued = 0;
+    S.fault = 0;
     tc::mbar_fence_init();
   }
   for (int f = tid; f < NP; f += NT) {
@@ -97,263 +404,208 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     S.fi[f] = (unsigned char)i;
     S.fj[f] = (unsigned char)j;
   }
-  const TilePar tp = a.tp[tile];
-  // weight role (warps 0-7): column tid & 127, observations [8*(tid>>7), +8)
-  const bool wrole = tid < 256;
-  const int wc = tid & (TM - 1), wh = (tid >> 7) & 1;
-  const int col = a.tile_cols[(size_t)tile * TM + wc];
-  const bool colv = wrole && col >= 0;
-  ColPar cp;
-  if (colv) cp = a.cp[col];
-  else { cp.ux = cp.uy = cp.uz = 0.0f; cp.rmax = -1.0f; cp.L1 = cp.L2 = 1.0f; cp.ic1 = cp.ic2 = 1.0f; }
-  float c2max = -1.0f;
-  if (colv) {
-    const float hq = fminf(cp.rmax / 12742000.0f, 1.5707963f);
-    const float sh = sinf(hq);
-    c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
-  }
-  int ncand = 0, nkeep = 0;
-  float rsum = 0.0f;
-
-  // ---- index window of the tile -> runs of the sorted observation table
-  const int nb = tp.b1 - tp.b0 + 1;
-  if (tid < nb) {
-    const int b = tp.b0 + tid;
-    const int nl = a.geom->nlon[b], off = a.geom->off[b];
-    int s0 = 0, l0 = 0, s1 = 0, l1 = 0;
-    bool whole = tp.dlon >= 180.0f;
-    int clo = 0, chi = nl - 1;
-    if (!whole) {
-      clo = (int)floorf((tp.lonn - tp.dlon) * (float)nl / 360.0f);
-      chi = (int)floorf((tp.lonn + tp.dlon) * (float)nl / 360.0f);
-      if (chi - clo + 1 >= nl) whole = true;
-    }
-    if (whole) {
-      s0 = a.obs.cell_start[off];
-      l0 = a.obs.cell_start[off + nl] - s0;
-    } else if (clo < 0) {
-      s0 = a.obs.cell_start[off + clo + nl];
-      l0 = a.obs.cell_start[off + nl] - s0;
-      s1 = a.obs.cell_start[off];
-      l1 = a.obs.cell_start[off + chi + 1] - s1;
-    } else if (chi >= nl) {
-      s0 = a.obs.cell_start[off + clo];
-      l0 = a.obs.cell_start[off + nl] - s0;
-      s1 = a.obs.cell_start[off];
-      l1 = a.obs.cell_start[off + (chi - nl) + 1] - s1;
-    } else {
-      s0 = a.obs.cell_start[off + clo];
-      l0 = a.obs.cell_start[off + chi + 1] - s0;
-    }
-    S.seg_start[2 * tid] = s0;
-    S.seg_start[2 * tid + 1] = s1;
-    S.seg_pref[2 * tid] = l0;
-    S.seg_pref[2 * tid + 1] = l1;
-  }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = S.tmem;
-  const int nseg = 2 * nb;
-  {
-    const int i0 = 2 * tid, i1 = 2 * tid + 1;
-    const int v0 = i0 < nseg ? S.seg_pref[i0] : 0;
-    const int v1 = i1 < nseg ? S.seg_pref[i1] : 0;
-    const int x = v0 + v1;
-    int incl = x;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    if (lane == 31) S.wsc[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-      int s = lane < NT / 32 ? S.wsc[lane] : 0;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s += y;
-      }
-      if (lane < NT / 32) S.wsc[lane] = s;
-    }
-    __syncthreads();
-    const int basev = (wid > 0 ? S.wsc[wid - 1] : 0) + incl - x;
-    __syncthreads();
-    if (i0 < nseg) S.seg_pref[i0] = basev;
-    if (i1 < nseg) S.seg_pref[i1] = basev + v0;
-    if (tid == 0) { S.total = S.wsc[NT / 32 - 1]; S.seg_pref[nseg] = S.total; }
-    __syncthreads();
-  }
-  const int total = S.total;
-  const int nchunks = (total + KC - 1) / KC;
-  if (tid < KC && tid < total) S.pos[0][tid] = run_lookup(S, nseg, tid);
-  __syncthreads();
 
-  // MMA N-blocks of this pass: [0, min(NP,256)), [256, NP)
-  const int nb0 = NP < 256 ? NP : 256, nb1 = NP - nb0;
-  const uint32_t id0 = tc::idesc_tf32(TM, nb0), id1 = nb1 > 0 ? tc::idesc_tf32(TM, nb1) : 0u;
-  bool pending0 = false, pending1 = false;
-  uint32_t phase0 = 0, phase1 = 0;
-  bool issued = false, fault = false;
-  const float4 *hx4 = reinterpret_cast<const float4 *>(a.obs.hx);
-  const int q4 = kp >> 2;
-  // feature role (warps 8-15): features tid-256 and tid (those < NP)
-  const int pf0 = tid - 256;
+  // producer thread: column wc, observations [4 wq, 4 wq + 4) of each chunk,
+  // and feature f = tid
+  const int wc = tid & (TM - 1), wq = (tid >> 7) & 3;
+  int ncand = 0, nkeep = 0;
+  float rsum = 0.0f;
 
-  for (int ch = 0; ch < nchunks; ch++) {
-    const int s = ch & 1;
-    const int pb = ch & 1;
-    // ---- stage: hx transposed to yT[member][obs] (+ dep as member k), obs records
-    {
-      const int t = tid;
-      const int nq = q4 + 1;             // hx quads + the quad holding dep at index k
-      if (t < nq * KC) {
-        const int qq = t >> 4, e = t & 15;
-        const int jj = ch * KC + e;
-        const bool v = jj < total;
-        const int pos = v ? S.pos[pb][e] : 0;
-        float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (v && qq < q4) y = hx4[(size_t)pos * q4 + qq];
-        if (qq == (k >> 2)) {
-          const float dep = v ? a.obs.B[pos].x : 0.0f;
-          const int c = k & 3;
-          if (c == 0) y.x = dep; else if (c == 1) y.y = dep; else if (c == 2) y.z = dep; else y.w = dep;
-        }
-        yT[(4 * qq + 0) * YT_LD + e] = y.x;
-        yT[(4 * qq + 1) * YT_LD + e] = y.y;
-        yT[(4 * qq + 2) * YT_LD + e] = y.z;
-        yT[(4 * qq + 3) * YT_LD + e] = y.w;
-      } else if (t >= 480 && t < 480 + KC) {
-        const int e = t - 480;
-        const int jj = ch * KC + e;
-        const bool v = jj < total;
-        const int pos = v ? S.pos[pb][e] : 0;
-        float4 A = make_float4(0.f, 0.f, 0.f, 1.f), B = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (v) { A = a.obs.A[pos]; B = a.obs.B[pos]; A.w = __frcp_rn(A.w); }
-        S.obsA[e] = A;
-        S.obsB[e] = B;
-        S.obsValid[e] = v;
-      } else if (t >= 448 && t < 448 + KC) {
-        // positions of the next chunk
-        const int e = t - 448;
-        const int jj = (ch + 1) * KC + e;
-        if (jj < total) S.pos[pb ^ 1][e] = run_lookup(S, nseg, jj);
-      }
+  if (wid < NPW) {
+    const int col = a.tile_cols[(size_t)tile * TM + wc];
+    const bool colv = col >= 0;
+    ColPar cp;
+    if (colv) cp = a.cp[col];
+    else { cp.ux = cp.uy = cp.uz = 0.0f; cp.rmax = -1.0f; cp.L1 = cp.L2 = 1.0f; cp.ic1 = cp.ic2 = 1.0f; }
+    float c2max = -1.0f;
+    if (colv) {
+      const float hq = fminf(cp.rmax / 12742000.0f, 1.5707963f);
+      const float sh = sinf(hq);
+      c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
     }
-    // ---- stage s must be free (MMAs of chunk ch-2 done): thread 0 waits, the
-    // barrier publishes the staged data and the outcome
-    {
-      bool bad = false;
-      if (tid == 0) {
-        if (s == 0 && pending0) bad = !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.mbar[0]), phase0);
-        if (s == 1 && pending1) bad = !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.mbar[1]), phase1);
+    const float rlo = cp.rmax * (1.0f - 2e-5f), rhi = cp.rmax * (1.0f + 2e-5f);
+    LocK lk;
+    lk.icv = LOC == LOC_VTGC ? inv_c_of(a.loc.vloc) : 1.0f;
+    lk.levg = LOC == LOC_VTGC ? a.loc.lev_depth[g] : 0.0f;
+    lk.tprof = a.loc.tloc_prof;
+    lk.tsat = a.loc.tloc_sat;
+    lk.ictp = (LOC == LOC_OCEAN && lk.tprof > 0.0f) ? inv_c_of(lk.tprof) : 1.0f;
+    lk.icts = (LOC == LOC_OCEAN && lk.tsat > 0.0f) ? inv_c_of(lk.tsat) : 1.0f;
+    const int f = tid;
+    const bool fin = f < NP;
+    const int fi = fin ? S.fi[f] : 255, fj = fin ? S.fj[f] : 255;
+    const bool fv = fi != 255;
+    const int rowi = (fv ? fi : 0) * YS, rowj = (fv ? fj : 0) * YS;
+
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int s = ch % NS, r = ch % NR;
+      if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[r]), (ch / NR) & 1)) { S.fault = 1; break; }
+      if (ch >= NS && !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.empty[s]), ((ch / NS) - 1) & 1)) {
+        S.fault = 1;
+        break;
       }
-      if (s == 0 && pending0) { phase0 ^= 1; pending0 = false; }
-      if (s == 1 && pending1) { phase1 ^= 1; pending1 = false; }
-      if (__syncthreads_or(bad)) { fault = true; break; }
-    }
-    unsigned char *Whi = stg[s], *Wlo = stg[s] + WB, *Phi = stg[s] + 2 * WB, *Plo = stg[s] + 2 * WB + PB;
-    bool anyk = false;
-    if (wrole) {
-      // ---- W: weights of column wc for 8 observations (exact keep decisions)
+      const unsigned char *rec = ring + (size_t)r * cb;
+      const float4 *RA = reinterpret_cast<const float4 *>(rec);
+      unsigned char *Whi = stage_ptr(s), *Wlo = Whi + WB, *Phi = Whi + 2 * WB, *Plo = Phi + PB;
+
+      // ---- weights: four observations, fast path without branches
+      float w[4];
+      unsigned unsure = 0, inr = 0;
 #pragma unroll
-      for (int grp = 0; grp < 2; grp++) {
+      for (int u = 0; u < 4; u++) {
+        const int e = wq * 4 + u;
+        const float4 A = RA[e];
+        const float4 B = RA[16 + e];
+        const float dx = __fsub_rn(cp.ux, A.x), dy = __fsub_rn(cp.uy, A.y), dz = __fsub_rn(cp.uz, A.z);
+        const float c2f = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
+        const bool cand = (ch * KC + e < ntile) && (c2f <= c2max);
+        const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
+        const float d = 12742000.0f * asin_fast(fminf(hf, 0.5f));
+        const float rl = loc_fast<LOC>(lk, cp, g, d, B);
+        const bool in = cand && d <= cp.rmax;
+        const bool uns = cand && (hf > 0.5f || (d >= rlo && d <= rhi) || (in && fabsf(rl - kKeep) <= kGuardFast));
+        const bool kept = in && rl > kKeep;
+        w[u] = kept ? rl : 0.0f;
+        unsure |= (uns ? 1u : 0u) << u;
+        inr |= (in ? 1u : 0u) << u;
+      }
+      // ---- rare: exact metric and the per-column localizer
+      if (__any_sync(0xffffffffu, unsure != 0)) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (!((unsure >> u) & 1u)) continue;
+          const int e = wq * 4 + u;
+          const float4 A = RA[e];
+          const float4 B = RA[16 + e];
+          const float de = dist_from_chord2(chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z));
+          const bool in = de <= cp.rmax;
+          float rl = in ? localize(a.loc, cp, g, de, B.y, B.z, B.w) : 0.0f;
+          w[u] = (in && rl > kKeep) ? rl : 0.0f;
+          inr = (inr & ~(1u << u)) | ((in ? 1u : 0u) << u);
+        }
+      }
+      bool anyk = false;
+      {
         float h4[4], l4[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-          const int e = wh * 8 + grp * 4 + u;
-          float w = 0.0f;
-          const float4 A = S.obsA[e];
-          const float c2 = chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
-          if (c2 <= c2max && S.obsValid[e]) {
-            const float d = dist_from_chord2(c2);
-            if (d <= cp.rmax) {
-              ncand++;
-              const float4 B = S.obsB[e];
-              const float r = localize(a.loc, cp, g, d, B.y, B.z, B.w);
-              if (r > kKeep) {
-                w = r * A.w;
-                nkeep++;
-                rsum += r;
-                anyk = true;
-              }
-            }
+          const float rl = w[u];
+          ncand += (inr >> u) & 1u;
+          float wv = 0.0f;
+          if (rl > 0.0f) {
+            nkeep++;
+            rsum += rl;
+            anyk = true;
+            wv = rl * __frcp_rn(RA[wq * 4 + u].w);
           }
-          tc::split_tf32(w, h4[u], l4[u]);
+          tc::split_tf32(wv, h4[u], l4[u]);
         }
-        const uint32_t off = kmaj(wc, wh * 8 + grp * 4);
+        const uint32_t off = kmaj(wc, wq * 4);
         *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
         *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
       }
-    } else {
-      // ---- P: feature products y_i * y_j for 16 observations
+      // ---- feature products: feature f over the 16 observations
+      if (fin) {
+        const float *yT = reinterpret_cast<const float *>(rec + 512);
+        const float4 *yi = reinterpret_cast<const float4 *>(yT + rowi);
+        const float4 *yj = reinterpret_cast<const float4 *>(yT + rowj);
 #pragma unroll
-      for (int rep = 0; rep < 2; rep++) {
-        const int f = pf0 + 256 * rep;
-        if (f < NP) {
-          const int i = S.fi[f], j = S.fj[f];
-          const bool fv = i != 255;
-          const float4 *yi = reinterpret_cast<const float4 *>(yT + (fv ? i : 0) * YT_LD);
-          const float4 *yj = reinterpret_cast<const float4 *>(yT + (fv ? j : 0) * YT_LD);
+        for (int grp = 0; grp < 4; grp++) {
+          const float4 a4 = yi[grp], b4 = yj[grp];
+          const float v[4] = {a4.x * b4.x, a4.y * b4.y, a4.z * b4.z, a4.w * b4.w};
+          float h4[4], l4[4];
 #pragma unroll
-          for (int grp = 0; grp < 4; grp++) {
-            const float4 a4 = yi[grp], b4 = yj[grp];
-            float v[4] = {a4.x * b4.x, a4.y * b4.y, a4.z * b4.z, a4.w * b4.w};
-            float h4[4], l4[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) tc::split_tf32(fv ? v[u] : 0.0f, h4[u], l4[u]);
-            const uint32_t off = kmaj(f, grp * 4);
-            *reinterpret_cast<float4 *>(Phi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
-            *reinterpret_cast<float4 *>(Plo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
-          }
+          for (int u = 0; u < 4; u++) tc::split_tf32(fv ? v[u] : 0.0f, h4[u], l4[u]);
+          const uint32_t off = kmaj(f, grp * 4);
+          *reinterpret_cast<float4 *>(Phi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+          *reinterpret_cast<float4 *>(Plo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
         }
       }
+      if (__any_sync(0xffffffffu, anyk) && lane == 0) S.anyk[s] = ch + 1;
+      tc::fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) bar_arrive(&S.full[s]);
     }
-    tc::fence_proxy_async();
-    const bool chunk_keep = __syncthreads_or(anyk) != 0;
-    // ---- issue: D += Whi*Phi + Whi*Plo + Wlo*Phi
-    if (chunk_keep) {
-      if (tid == 0) {
-        tc::fence_after();
-        const uint32_t aw[3] = {tc::smem_u32(Whi), tc::smem_u32(Whi), tc::smem_u32(Wlo)};
-        const uint32_t bp[3] = {tc::smem_u32(Phi), tc::smem_u32(Plo), tc::smem_u32(Phi)};
+  } else if (wid == MMA_WARP) {
+    // ================================================= MMA issue + record loads (one thread)
+    if (lane == 0) {
+      const unsigned char *src = a.rec + (size_t)c0 * cb;
+      auto load = [&](int ch) {
+        tc::bulk_load(ring + (size_t)(ch % NR) * cb, src + (size_t)ch * cb, (uint32_t)cb,
+                      reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]));
+      };
+      int n_loaded = nchunks < NR ? nchunks : NR;
+      for (int ch = 0; ch < n_loaded; ch++) load(ch);
+      const int nb0 = NP < 256 ? NP : 256, nb1 = NP - nb0;
+      const uint32_t id0 = tc::idesc_tf32(TM, nb0), id1 = nb1 > 0 ? tc::idesc_tf32(TM, nb1) : 0u;
+      bool issued = false;
+      for (int ch = 0; ch < nchunks; ch++) {
+        const int s = ch % NS;
+        if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.full[s]), (ch / NS) & 1)) { S.fault = 1; break; }
+        // every producer is done with the records of chunk ch: refill the slot
+        if (n_loaded < nchunks) load(n_loaded++);
+        if (S.anyk[s] == ch + 1) {
+          tc::fence_after();
+          const uint32_t whi = tc::smem_u32(stage_ptr(s)), wlo = whi + WB, phi = whi + 2 * WB, plo = phi + PB;
 #pragma unroll
-        for (int t = 0; t < 3; t++)
+          for (int t = 0; t < 3; t++)
 #pragma unroll
-          for (int ks = 0; ks < KC / 8; ks++) {
-            const uint32_t acc = (issued || t > 0 || ks > 0) ? 1u : 0u;
-            const uint64_t ad = tc::smem_desc(aw[t] + ks * 2 * CMB, CMB, SBO);
-            const uint64_t bd0 = tc::smem_desc(bp[t] + ks * 2 * CMB, CMB, SBO);
-            tc::mma_tf32(tmem, ad, bd0, id0, acc);
-            if (nb1 > 0) {
-              const uint64_t bd1 = tc::smem_desc(bp[t] + (uint32_t)(nb0 / 8) * SBO + ks * 2 * CMB, CMB, SBO);
-              tc::mma_tf32(tmem + (uint32_t)nb0, ad, bd1, id1, acc);
+            for (int ks = 0; ks < KC / 8; ks++) {
+              const uint32_t acc = (issued || t > 0 || ks > 0) ? 1u : 0u;
+              const uint32_t aw = t == 2 ? wlo : whi, bp = t == 1 ? plo : phi;
+              const uint64_t ad = tc::smem_desc(aw + ks * 2 * CMB, CMB, SBO);
+              const uint64_t bd0 = tc::smem_desc(bp + ks * 2 * CMB, CMB, SBO);
+              tc::mma_tf32(tmem, ad, bd0, id0, acc);
+              if (nb1 > 0) {
+                const uint64_t bd1 = tc::smem_desc(bp + (uint32_t)(nb0 / 8) * SBO + ks * 2 * CMB, CMB, SBO);
+                tc::mma_tf32(tmem + (uint32_t)nb0, ad, bd1, id1, acc);
+              }
             }
-          }
-        tc::commit(reinterpret_cast<uint64_t *>(&S.mbar[s]));
+          tc::commit(reinterpret_cast<uint64_t *>(&S.empty[s]));
+          issued = true;
+        } else {
+          bar_arrive(&S.empty[s]);
+        }
       }
-      issued = true;
-      if (s == 0) pending0 = true; else pending1 = true;
+      // every MMA issued by this thread has completed once `done` flips
+      tc::commit(reinterpret_cast<uint64_t *>(&S.done));
+      if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.done), 0)) S.fault = 1;
+      S.issued = issued ? 1 : 0;
+      // no record copy may still be in flight when the CTA exits
+      for (int ch = n_loaded > NR ? n_loaded - NR : 0; ch < n_loaded; ch++)
+        if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]), (ch / NR) & 1)) S.fault = 1;
     }
   }
-  // ---- drain (thread 0 waits, the barrier publishes the outcome)
-  {
-    bool bad = false;
-    if (tid == 0) {
-      if (pending0 && !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.mbar[0]), phase0)) bad = true;
-      if (pending1 && !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.mbar[1]), phase1)) bad = true;
-    }
-    if (__syncthreads_or(bad)) fault = true;
-  }
-  tc::fence_after();
-
-  // ---- per-column diagnostics and kept counts (both halves of a column)
-  if (wrole && wh == 1) { S.dcand[wc] = ncand; S.dkept[wc] = nkeep; S.drsum[wc] = rsum; }
+  tc::fence_before();
   __syncthreads();
+  tc::fence_after();
+  const bool fault = S.fault != 0;
+  const bool issued = S.issued != 0;
+  // per-column partial counts of observation quarters 1-3, in the (now idle)
+  // operand stage memory
+  int *dcand = reinterpret_cast<int *>(dsm), *dkept = dcand + 3 * TM;
+  float *drsum = reinterpret_cast<float *>(dkept + 3 * TM);
+  if (wid < NPW && wq > 0) {
+    dcand[(wq - 1) * TM + wc] = ncand;
+    dkept[(wq - 1) * TM + wc] = nkeep;
+    drsum[(wq - 1) * TM + wc] = rsum;
+  }
+  __syncthreads();
+
+  // ---- per-column diagnostics, kept counts, epilogue (warps 0-3 = TMEM lanes)
   const int G = a.groups;
   if (tid < TM) {
-    ncand += S.dcand[wc];
-    nkeep += S.dkept[wc];
-    rsum += S.drsum[wc];
+    for (int q = 0; q < 3; q++) {
+      ncand += dcand[q * TM + wc];
+      nkeep += dkept[q * TM + wc];
+      rsum += drsum[q * TM + wc];
+    }
+    const int col = a.tile_cols[(size_t)tile * TM + wc];
+    const bool colv = col >= 0;
     size_t unit = 0;
     if (colv) unit = (size_t)a.col2act[col] * G + g;
     if (colv && pass == 0) {
@@ -362,7 +614,6 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       if (a.diag_lg_obsloc) a.diag_lg_obsloc[(size_t)g * a.ncol + col] = rsum;
       if (g == 0 && a.diag_obscount) a.diag_obscount[col] = (float)ncand;
     }
-    // ---- epilogue: TMEM lane tid = column tid, 16 features per load
     float *Gp = a.G + unit * (size_t)nf + (size_t)pass * NP;
     const int nvalid = nf - pass * NP < NP ? nf - pass * NP : NP;
     for (int f0 = 0; f0 < NP; f0 += 16) {
@@ -383,7 +634,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   if (fault && tid == 0) atomicOr(a.status, 16);
   tc::fence_before();
   __syncthreads();
-  if (wid == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+  if (wid == 0) tc::tmem_dealloc(tmem, tmem_cols);
 }
 
 // Tile caps: centre = normalised mean of the tile's unit vectors, angular
@@ -431,19 +682,31 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
     }
     t.lonn = (float)lon;
     t.dlon = (float)dl;
+    t.cx = (float)cx;
+    t.cy = (float)cy;
+    t.cz = (float)cz;
+    const double ch = 2.0 * sin(0.5 * fmin(alpha, 3.14159265358979));
+    t.c2cap = (float)(ch * ch * 1.00001 + 1e-9);
     t.b0 = band_of((float)(lat - adeg));
     t.b1 = band_of((float)(lat + adeg));
     tp[tile] = t;
   }
 }
 
+// Stage / ring depths: three operand stages when they fit beside three record
+// slots, else two stages and eight slots.
+void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem) {
+  const size_t PB = (size_t)(np / 8) * SBO;
+  const size_t stage = 2 * WB + 2 * PB;
+  const size_t cb = record_bytes(k);
+  if (3 * stage + 3 * cb <= kSmemBudget) { *ns = 3; *nr = 3; }
+  else { *ns = 2; *nr = 8; }
+  *smem = (size_t)*ns * stage + (size_t)*nr * cb;
+}
+
 }  // namespace
 
-size_t gram_tc_smem_bytes(int k, int np) {
-  const int kp = (k + 3) & ~3;
-  const size_t PB = (size_t)(np / 8) * SBO;
-  return 2 * (2 * WB + 2 * PB) + (size_t)(kp + 4) * YT_LD * sizeof(float);
-}
+size_t record_bytes(int k) { return 512 + (size_t)(((k + 4) & ~3) * YS) * sizeof(float); }
 
 void gram_tc_passes(int k, int *npass, int *np) {
   const int nf = packed_size(k);
@@ -463,16 +726,59 @@ cudaError_t launch_tile_prep(cudaStream_t st, int ntiles, const int *tile_cols, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a, int *launches) {
-  if (a.ntiles <= 0) return cudaSuccess;
-  const size_t smem = gram_tc_smem_bytes(a.k, a.np);
-  cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const long long grid = (long long)a.ntiles * a.groups * a.npass;
-  if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
-  k_gram_tc<<<(int)grid, NT, smem, st>>>(a);
+cudaError_t launch_tile_count(cudaStream_t st, int ntiles, const TilePar *tp, const IndexGeom *geom,
+                              const ObsSorted &obs, int *tile_n, int *tile_off, int *launches) {
+  if (ntiles <= 0) return cudaMemsetAsync(tile_off, 0, sizeof(int), st);
+  k_tile_count<<<ntiles, WT, 0, st>>>(ntiles, tp, geom, obs.A, obs.cell_start, tile_n);
+  k_tile_scan<<<1, 1024, 0, st>>>(ntiles, tile_n, tile_off);
+  (*launches) += 2;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_fill(cudaStream_t st, int ntiles, const TilePar *tp, const IndexGeom *geom,
+                             const ObsSorted &obs, int k, int kp, const int *tile_off, unsigned char *rec,
+                             int *status, int *launches) {
+  if (ntiles <= 0) return cudaSuccess;
+  const int kr = (k + 4) & ~3;
+  k_tile_fill<<<ntiles, WT, 0, st>>>(ntiles, tp, geom, obs, k, kp, kr, (int)record_bytes(k), tile_off, rec, status);
   (*launches)++;
   return cudaGetLastError();
+}
+
+template <int LOC, int NS, int NR>
+static cudaError_t launch_gram_tc_t(cudaStream_t st, const TcArgs &a, size_t smem, long long grid) {
+  cudaError_t e =
+      cudaFuncSetAttribute(k_gram_tc<LOC, NS, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_gram_tc<LOC, NS, NR><<<(int)grid, NT, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int LOC>
+static cudaError_t launch_gram_tc_loc(cudaStream_t st, const TcArgs &a, int ns, size_t smem, long long grid) {
+  return ns == 3 ? launch_gram_tc_t<LOC, 3, 3>(st, a, smem, grid) : launch_gram_tc_t<LOC, 2, 8>(st, a, smem, grid);
+}
+
+cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
+  if (a_in.ntiles <= 0) return cudaSuccess;
+  TcArgs a = a_in;
+  a.cb = (int)record_bytes(a.k);
+  uint32_t tc = 32;
+  while ((int)tc < a.np) tc <<= 1;
+  a.tmem_cols = tc;
+  int ns, nr;
+  size_t smem;
+  gram_tc_config(a.k, a.np, &ns, &nr, &smem);
+  const long long grid = (long long)a.ntiles * a.groups * a.npass;
+  if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+  cudaError_t e;
+  switch (a.loc.cls) {
+  case LOC_OCEAN: e = launch_gram_tc_loc<LOC_OCEAN>(st, a, ns, smem, grid); break;
+  case LOC_VTGC: e = launch_gram_tc_loc<LOC_VTGC>(st, a, ns, smem, grid); break;
+  default: e = launch_gram_tc_loc<LOC_NOVRT>(st, a, ns, smem, grid); break;
+  }
+  (*launches)++;
+  return e;
 }
 
 }  // namespace lgpu

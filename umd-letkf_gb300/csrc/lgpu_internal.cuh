@@ -314,16 +314,20 @@ cudaError_t launch_gram(cudaStream_t st, const GramArgs &a, int *launches);
 struct TilePar {
   float lonn, dlon;  // longitude window of the tile's search cap (deg)
   int b0, b1;        // latitude band range
+  float cx, cy, cz;  // cap centre (unit vector)
+  float c2cap;       // squared chord of the cap radius, with margin
 };
 struct TcArgs {
   int ntiles, groups, k, kp, npass, np, nf, ncol;
   const int *tile_cols;   // [ntiles][128] column index or -1
   const int *col2act;
   const ColPar *cp;
-  const TilePar *tp;
   DevLoc loc;
-  ObsSorted obs;
-  const IndexGeom *geom;
+  const unsigned char *rec;  // tile candidate streams (chunk records)
+  const int *tile_off;       // [ntiles + 1] first chunk of each tile's stream
+  const int *tile_n;         // [ntiles] candidates of each tile
+  int cb;                    // bytes per chunk record (set by the launcher)
+  uint32_t tmem_cols;        // TMEM columns per CTA (set by the launcher)
   float *G;
   int *nkept;
   float *diag_obscount, *diag_lg_obscount, *diag_lg_obsloc;
@@ -331,6 +335,14 @@ struct TcArgs {
 };
 cudaError_t launch_tile_prep(cudaStream_t st, int ntiles, const int *tile_cols, const ColPar *cp, TilePar *tp,
                              int *launches);
+// tile candidate streams: counts + chunk offsets (tile_off[ntiles] = total
+// chunks), then the records (record_bytes(k) per chunk of 16)
+size_t record_bytes(int k);
+cudaError_t launch_tile_count(cudaStream_t st, int ntiles, const TilePar *tp, const IndexGeom *geom,
+                              const ObsSorted &obs, int *tile_n, int *tile_off, int *launches);
+cudaError_t launch_tile_fill(cudaStream_t st, int ntiles, const TilePar *tp, const IndexGeom *geom,
+                             const ObsSorted &obs, int k, int kp, const int *tile_off, unsigned char *rec,
+                             int *status, int *launches);
 cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a, int *launches);
 void gram_tc_passes(int k, int *npass, int *np);
 

@@ -78,6 +78,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long 
   return false;
 }
 
+// Bulk async copy global -> shared (16-byte aligned addresses, size a
+// multiple of 16), completion counted in bytes on `mbar`; the calling thread
+// also arrives on `mbar` with the expected byte count.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+               : "memory");
+}
+
 // 32 lanes x 16 consecutive 32-bit TMEM columns -> 16 registers per thread.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   uint32_t r[16];

@@ -88,7 +88,9 @@ VARIANTS = {"auto": 0, "plain": 1, "batched": 2}
 EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_solver_init", "lgpu_loc_init",
            "lgpu_loc_maxgroups", "lgpu_set_grid", "lgpu_set_state", "lgpu_set_obs", "lgpu_solver_run",
            "lgpu_get_state", "lgpu_get_diag", "lgpu_get_timings", "lgpu_solver_final", "lgpu_get_obslist",
-           "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2"]
+           "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2",
+           "lgpu_set_obs_raw", "lgpu_set_state_members", "lgpu_get_background",
+           "lgpu_get_obs_prepared", "lgpu_debug_transform"]
 
 _lib = None
 
@@ -126,6 +128,11 @@ def lib(path=None):
     L.lgpu_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
     L.lgpu_host_free.argtypes = [ctypes.c_void_p]
     L.lgpu_flush_l2.argtypes = [H, ctypes.c_size_t]
+    L.lgpu_set_obs_raw.argtypes = [H, ctypes.c_int, ctypes.POINTER(_Obs), IP, FP, IP]
+    L.lgpu_set_state_members.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, ctypes.c_int, ctypes.POINTER(_Var)]
+    L.lgpu_get_background.argtypes = [H, FP, FP, FP]
+    L.lgpu_debug_transform.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP]
+    L.lgpu_get_obs_prepared.argtypes = [H, FP, FP, FP, FP, FP, FP]
     if path is None:
         _lib = L
     return L
@@ -327,6 +334,56 @@ class Solver:
         self.nobs = len(arrs[0])
         return self._ck(self.L.lgpu_set_obs(self.h, self.nobs, ctypes.byref(o), _fp(hx), _fp(hx_mean)))
 
+    @staticmethod
+    def _vars(variables):
+        vs = (_Var * len(variables))()
+        for i, v in enumerate(variables):
+            vs[i].grid_s_idx, vs[i].levels = v["grid_s_idx"], v["levels"]
+            vs[i].ana_inc_max = v.get("ana_inc_max", 9.99e36)
+            b = v.get("ana_bounds", (-9.99e36, 9.99e36))
+            vs[i].ana_bounds[0], vs[i].ana_bounds[1] = b[0], b[1]
+        return vs
+
+    def set_state_members(self, members, variables):
+        """Full ensemble members [ij, slab, member]; the background mean,
+        perturbations and spread are formed on the device
+        (src/letkf_state.F90:326-334)."""
+        members = _f32(members)
+        ncol, ns, k = members.shape
+        self.k, self.ns = k, ns
+        return self._ck(self.L.lgpu_set_state_members(self.h, k, ns, _fp(members), len(variables),
+                                                      self._vars(variables)))
+
+    def set_obs_raw(self, lat, lon, zdim, time, val, err, obsid, platid, hx_members, qc=None):
+        """Observations with full member H(x) values [obs, member] and QC
+        flags; the mean/perturbation split and the QC compaction run on the
+        device (src/letkf_obs.F90:459-488).  Returns the kept count."""
+        arrs = [_f32(a) for a in (lat, lon, zdim, time, val, err)] + [_i32(obsid), _i32(platid)]
+        hx = _f32(hx_members)
+        o = _Obs(*[_fp(a) for a in arrs[:6]], _ip(arrs[6]), _ip(arrs[7]))
+        q = _i32(qc) if qc is not None else None
+        kept = ctypes.c_int(0)
+        self._ck(self.L.lgpu_set_obs_raw(self.h, len(arrs[0]), ctypes.byref(o), _ip(q) if q is not None else None,
+                                         _fp(hx), ctypes.byref(kept)))
+        self.nobs = kept.value
+        return kept.value
+
+    def get_background(self):
+        x = np.empty((self.ncol, self.ns, self.k), np.float32)
+        m = np.empty((self.ncol, self.ns), np.float32)
+        sp = np.empty((self.ncol, self.ns), np.float32)
+        self._ck(self.L.lgpu_get_background(self.h, _fp(x), _fp(m), _fp(sp)))
+        return x, m, sp
+
+    def get_obs_prepared(self):
+        n = self.nobs
+        out = dict(hx=np.empty((n, self.k), np.float32), hx_mean=np.empty(n, np.float32),
+                   lat=np.empty(n, np.float32), lon=np.empty(n, np.float32), val=np.empty(n, np.float32),
+                   err=np.empty(n, np.float32))
+        self._ck(self.L.lgpu_get_obs_prepared(self.h, *[_fp(out[k]) for k in ("hx", "hx_mean", "lat", "lon", "val",
+                                                                              "err")]))
+        return out
+
     def set_problem(self, prob, variables=None):
         """Upload a letkf_gb300.synth.Problem (grid, state, observations)."""
         self.set_grid(prob.lat, prob.lon, prob.mask)
@@ -381,6 +438,15 @@ class Solver:
         n = len(a[0])
         out = np.zeros(n, np.float32)
         self._ck(self.L.lgpu_debug_metric(self.h, n, *[_fp(x) for x in a], _fp(out)))
+        return out
+
+    def debug_transform(self, gram_packed):
+        """Eigensolve stage on packed Gram blocks [nunits, k(k+3)/2] -> T [nunits, k, k]."""
+        g = _f32(gram_packed)
+        nunits, nf = g.shape
+        k = int(round((-3 + (9 + 8 * nf) ** 0.5) / 2))
+        out = np.zeros((nunits, k, k), np.float32)
+        self._ck(self.L.lgpu_debug_transform(self.h, nunits, k, _fp(g), _fp(out)))
         return out
 
     def debug_gc(self, z, L):
