@@ -203,6 +203,27 @@ int lgpu_solver_final(lgpu_handle *h);
 int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
                      int *n, int *ncand);
 
+/* lgpu_get_obslist for callers that cannot allocate device memory.
+ * No counterpart in the reference (the reference builds its lists in Fortran
+ * automatic arrays on the host stack).  It is meant for hosts that drive the
+ * analysis from inside their own memory manager -- a model's pre-allocated
+ * device pool, a cycling driver that forbids allocation after start-up, code
+ * running while a stream is being captured -- where the lazily grown list
+ * buffer of lgpu_get_obslist is not allowed.  Same arguments, results and
+ * canonical order as lgpu_get_obslist.  It calls no cudaMalloc/cudaFree: its
+ * scratch is one fixed __device__ array of 4 * LGPU_NOALLOC_MAX_LIST + 64
+ * ints (about 4 MB) that every device loading the library holds until the
+ * process exits.  Handles whose observation table is larger than
+ * LGPU_NOALLOC_MAX_LIST are rejected with LGPU_ERR_CAPACITY.  All calls
+ * share that array (the counters are cleared on each call): calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture. */
+#define LGPU_NOALLOC_MAX_LIST 262144
+int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
+                             int *n, int *ncand);
+
+
 /* Page-locked host memory for callers that stream state in and out every
  * analysis (host<->device copies run at full link speed from it). */
 int lgpu_host_alloc(size_t bytes, void **ptr);

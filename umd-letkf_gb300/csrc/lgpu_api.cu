@@ -16,6 +16,10 @@ using namespace lgpu;
 
 namespace lgpu {
 size_t gram_smem_bytes(int k);
+cudaError_t noalloc_scratch(int device, int **out);
+int noalloc_max_list();
+cudaError_t launch_obslist_noalloc(cudaStream_t st, int gid, const ColPar *cp_col, const DevLoc &loc, ObsSorted obs,
+                                   const IndexGeom *geom, int nmax, int *scratch);
 cudaError_t launch_hx_stats(cudaStream_t st, int nobs, int k, float *hx, float *hx_mean, const int *qc, int *flag,
                             int *pos, int *total);
 cudaError_t launch_compact(cudaStream_t st, int nobs, int k, const int *flag, const int *pos, const float *const *src_f,
@@ -845,6 +849,47 @@ int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, i
   for (int i = 0; i < m && i < cap; i++) {
     if (idx) idx[i] = li[ord[i]];
     if (rloc) rloc[i] = lr[ord[i]];
+  }
+  *n = cnt[0];
+  if (ncand) *ncand = cnt[1];
+  return LGPU_OK;
+}
+
+// lgpu_get_obslist without any allocation (see include/letkf_gpu.h).
+int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap, int *n, int *ncand) {
+  if (!h || !n) return LGPU_ERR_ARG;
+  if (!h->ran) return fail(h, LGPU_ERR_ORDER, "get_obslist_noalloc before a successful solver_run");
+  if (ij < 0 || ij >= h->ncol || group < 0 || group >= h->loc.groups || cap < 0)
+    return fail(h, LGPU_ERR_ARG, "get_obslist_noalloc: index out of range");
+  const int nmax = noalloc_max_list();
+  if (h->nobs > nmax)
+    return fail(h, LGPU_ERR_CAPACITY, "get_obslist_noalloc: " + std::to_string(h->nobs) +
+                                          " observations exceed the fixed list scratch of " + std::to_string(nmax));
+  *n = 0;
+  if (ncand) *ncand = 0;
+  if (h->h_col2act[ij] < 0) return LGPU_OK;   // masked column: no search (src/letkf_solver.F90:207)
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  int *scr = nullptr;
+  CK(noalloc_scratch(h->device, &scr), "cudaGetSymbolAddress(list scratch)");
+  ObsSorted os;
+  os.A = h->buf[B_SA].as<float4>();
+  os.B = h->buf[B_SB].as<float4>();
+  os.hx = h->buf[B_SHX].as<float>();
+  os.idx = h->buf[B_SIDX].as<int>();
+  os.cell_start = h->buf[B_CSTART].as<int>();
+  CK(launch_obslist_noalloc(h->st, group, h->buf[B_CP].as<ColPar>() + ij, h->loc, os, h->buf[B_GEOM].as<IndexGeom>(),
+                            nmax, scr),
+     "obslist kernel (no alloc)");
+  int cnt[2] = {0, 0};
+  CK(cudaMemcpyAsync(cnt, scr, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st), "D2H counts");
+  CK(cudaStreamSynchronize(h->st), "obslist (no alloc)");
+  const int m = std::min(std::min(cnt[0], nmax), cap);
+  if (m > 0) {
+    if (idx) CK(cudaMemcpyAsync(idx, scr + 64 + 2 * (size_t)nmax, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost, h->st),
+                "D2H idx");
+    if (rloc) CK(cudaMemcpyAsync(rloc, scr + 64 + 3 * (size_t)nmax, sizeof(float) * (size_t)m, cudaMemcpyDeviceToHost,
+                                 h->st), "D2H rloc");
+    CK(cudaStreamSynchronize(h->st), "obslist (no alloc)");
   }
   *n = cnt[0];
   if (ncand) *ncand = cnt[1];

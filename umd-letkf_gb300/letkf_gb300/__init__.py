@@ -89,7 +89,7 @@ EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error",
            "lgpu_loc_maxgroups", "lgpu_set_grid", "lgpu_set_state", "lgpu_set_obs", "lgpu_solver_run",
            "lgpu_get_state", "lgpu_get_diag", "lgpu_get_timings", "lgpu_solver_final", "lgpu_get_obslist",
            "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2",
-           "lgpu_set_obs_raw", "lgpu_set_state_members", "lgpu_get_background",
+           "lgpu_get_obslist_noalloc", "lgpu_set_obs_raw", "lgpu_set_state_members", "lgpu_get_background",
            "lgpu_get_obs_prepared", "lgpu_debug_transform"]
 
 _lib = None
@@ -128,6 +128,7 @@ def lib(path=None):
     L.lgpu_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
     L.lgpu_host_free.argtypes = [ctypes.c_void_p]
     L.lgpu_flush_l2.argtypes = [H, ctypes.c_size_t]
+    L.lgpu_get_obslist_noalloc.argtypes = [H, ctypes.c_int, ctypes.c_int, IP, FP, ctypes.c_int, IP, IP]
     L.lgpu_set_obs_raw.argtypes = [H, ctypes.c_int, ctypes.POINTER(_Obs), IP, FP, IP]
     L.lgpu_set_state_members.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, ctypes.c_int, ctypes.POINTER(_Var)]
     L.lgpu_get_background.argtypes = [H, FP, FP, FP]
@@ -424,6 +425,19 @@ class Solver:
         self._ck(self.L.lgpu_get_obslist(self.h, int(ij), int(group), _ip(idx), _fp(r), cap, ctypes.byref(n),
                                          ctypes.byref(nc)))
         m = min(n.value, cap)
+        return idx[:m].copy(), r[:m].copy(), nc.value
+
+    def obslist_noalloc(self, ij, group=0, out=None):
+        """lgpu_get_obslist_noalloc: same list as obslist() without any device
+        allocation; `out` = (idx int32, rloc float32) caller buffers."""
+        if out is None:
+            cap = max(self.nobs, 1)
+            out = (np.zeros(cap, np.int32), np.zeros(cap, np.float32))
+        idx, r = out
+        n, nc = ctypes.c_int(0), ctypes.c_int(0)
+        self._ck(self.L.lgpu_get_obslist_noalloc(self.h, int(ij), int(group), _ip(idx), _fp(r), len(idx),
+                                                 ctypes.byref(n), ctypes.byref(nc)))
+        m = min(n.value, len(idx))
         return idx[:m].copy(), r[:m].copy(), nc.value
 
     def final(self):
