@@ -39,6 +39,10 @@ METRIC = "gridpoints/s on 1 GB300: batched+learned vs plain LETKF at fixed analy
 UNIT = "gridpoints/s"
 
 
+# nominal FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 flop x 2.07 GHz
+SIMT_FP32_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -235,37 +239,49 @@ def gpu_arm(args, dist):
     ms = statistics.mean(t["total_ms"] for t in tims)
     ms_max = dist.max(ms)
     value = dist.world * nact / (ms_max / 1000.0)
-    stage = {k: statistics.mean(t[k] for t in tims) for k in ("index_ms", "prep_ms", "gram_ms", "eig_ms", "update_ms")}
+    stage = {k: statistics.mean(t[k] for t in tims)
+             for k in ("index_ms", "prep_ms", "gram_ms", "tiles_ms", "eig_ms", "update_ms")}
     launches = tims[-1]["launches"]
     diag = s.get_diag()
     kept = float(np.sum(diag["lg_obscount"], dtype=np.float64))
     cand = float(np.sum(diag["obscount"], dtype=np.float64))
     k, ns, ncol = prob.k, prob.ns, prob.ncol
     units = tims[-1]["units"]
-    # algorithmic work: Gram + RHS 2k(k+1) flop per kept obs;
-    # eigensolve ~9k^3 + transform 4k^3 per unit; update 2k^2 per slab and the
-    # state read + analysis write.
-    gram_flop = 2.0 * k * (k + 1) * kept
+    # algorithmic work per launch: the Gram kernel does one
+    # multiply-add per packed feature (k(k+3)/2 of them: upper triangle of G
+    # and the right-hand side) per kept (column, observation) pair; the
+    # eigensolve ~9k^3 + transform 4k^3 per unit; the update reads the
+    # background members and writes the analysis members, mean and spread.
+    gram_flop = float(k * (k + 3)) * kept
     eig_flop = 13.0 * k ** 3 * units
     upd_bytes = 2.0 * ncol * ns * k * 4 + 4.0 * ncol * ns * 4
+    gram_kernel_ms = stage["gram_ms"] - stage["tiles_ms"]
     stages = {
-        "gram": {"ms": stage["gram_ms"], "tflops": gram_flop / (stage["gram_ms"] * 1e-3) / 1e12},
+        "tile_streams": {"ms": stage["tiles_ms"]},
+        "gram": {"ms": gram_kernel_ms, "tflops": gram_flop / (gram_kernel_ms * 1e-3) / 1e12},
         "eig": {"ms": stage["eig_ms"], "tflops": eig_flop / (stage["eig_ms"] * 1e-3) / 1e12},
         "update": {"ms": stage["update_ms"], "gbs": upd_bytes / (stage["update_ms"] * 1e-3) / 1e9},
         "index": {"ms": stage["index_ms"]}, "prep": {"ms": stage["prep_ms"]},
         "kept_pairs": kept, "candidate_pairs": cand}
-    dom = max(("gram", "eig", "update"), key=lambda n: stage[n + "_ms"])
-    traffic = read_traffic(dom)
+    times = {"gram": gram_kernel_ms, "eig": stage["eig_ms"], "update": stage["update_ms"]}
+    dom = max(times, key=times.get)
+    kname = {"gram": "k_gram_tc" if tims[-1]["variant"] == 2 else "k_gram", "eig": "k_eig", "update": "k_update"}[dom]
+    traffic = read_traffic(kname)
     if dom == "update":
         ach = upd_bytes / (stage["update_ms"] * 1e-3) / 1e9
-        roof = {"kernel": "k_update", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+        roof = {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                 "frac": ach / hbm, "traffic": traffic, "peak_source": peak_kind + " hbm_gbs (burst)"}
     else:
         fl = gram_flop if dom == "gram" else eig_flop
-        ach = fl / (stage[dom + "_ms"] * 1e-3) / 1e12
-        roof = {"kernel": "k_" + dom, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+        ach = fl / (times[dom] * 1e-3) / 1e12
+        simt = SIMT_FP32_TFLOPS
+        roof = {"kernel": kname, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "traffic": traffic,
-                "peak_source": peak_kind + " bf16_tflops (burst); this kernel computes in FP32 on CUDA cores"}
+                "peak_source": peak_kind + " bf16_tflops (burst)",
+                "note": ("TF32 three-term split on tcgen05; dense TF32 is half the bf16 rate and the split triples "
+                         "the MMAs, so bf16/6 bounds this kernel's algorithmic rate" if dom == "gram" else
+                         "FP32 on the CUDA cores (no tensor work); nominal FP32 SIMT peak %.1f TFLOP/s, "
+                         "frac of it %.4f" % (simt, ach / simt))}
     variant = {1: "plain", 2: "batched_tc"}.get(tims[-1]["variant"], "?")
     plain = None
     if variant != "plain" and not args.no_plain:
@@ -283,29 +299,37 @@ def gpu_arm(args, dist):
                  "speedup_of_headline": (dist.world * nact / (ms_max / 1000.0)) / (dist.world * nact / (pms / 1000.0))}
         s.set_variant(args.variant)
         s.run()
-    # ---- end to end through the C ABI with page-locked host buffers
+    # ---- end to end through the C ABI with page-locked host buffers: the
+    # state is bound in place (lgpu_bind_state, the reference's in-place
+    # letkf_solver_run); every step uploads the observations and the
+    # background and downloads the analysis into the bound arrays
     pin = {n: PinnedArray(getattr(prob, n).shape, getattr(prob, n).dtype) for n in
-           ("state", "mean", "sprd", "olat", "olon", "oz", "otime", "oval", "oerr", "oobsid", "oplatid", "hx",
-            "hx_mean")}
+           ("olat", "olon", "oz", "otime", "oval", "oerr", "oobsid", "oplatid", "hx", "hx_mean")}
     for n, p in pin.items():
         p.array[...] = getattr(prob, n)
     outp = [PinnedArray(prob.state.shape), PinnedArray(prob.mean.shape), PinnedArray(prob.sprd.shape)]
-    h2d = sum(p.array.nbytes for p in pin.values())
+    h2d = sum(p.array.nbytes for p in pin.values()) + sum(p.array.nbytes for p in outp)
     d2h = sum(p.array.nbytes for p in outp)
 
+    def refill():   # the same background every step (outside the timed region)
+        for p, src in zip(outp, (prob.state, prob.mean, prob.sprd)):
+            np.copyto(p.array, src)
+
+    s.bind_state(outp[0].array, outp[1].array, outp[2].array, prob.vars)
+
     def e2e_step():
-        s.set_state(pin["state"].array, pin["mean"].array, pin["sprd"].array, prob.vars)
         s.set_obs(pin["olat"].array, pin["olon"].array, pin["oz"].array, pin["otime"].array, pin["oval"].array,
                   pin["oerr"].array, pin["oobsid"].array, pin["oplatid"].array, pin["hx"].array,
                   pin["hx_mean"].array)
         s.run()
-        s.get_state(tuple(p.array for p in outp))
 
     for _ in range(max(1, min(args.warmup, 2))):
+        refill()
         e2e_step()
     dist.barrier()
     et = []
     for _ in range(args.steps):
+        refill()
         s.flush_l2(256 << 20)
         t0 = time.perf_counter()
         e2e_step()
@@ -334,10 +358,28 @@ def gpu_arm(args, dist):
     return 0
 
 
+def single_run(args):
+    """One lgpu_solver_run of the workload, for kernel profiles; prints the
+    library's stage timings."""
+    from letkf_gb300 import Solver
+    prob, cfg = make_problem(args.workload)
+    s = Solver(0)
+    try:
+        s.set_variant(args.variant)
+        s.solver_init(cfg["solver"])
+        s.loc_init(cfg["localization"], prob.vars, prob.lev_depth)
+        s.set_problem(prob)
+        s.run()
+        print(json.dumps({"workload": args.workload, "timings": s.timings()}), flush=True)
+    finally:
+        s.close()
+    return 0
+
+
 def read_traffic(kernel):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (profiles/<kernel>_c2.md, line 'traffic_bytes_per_launch: N')."""
-    p = os.path.join(ROOT, "profiles", "k_%s_c2.md" % kernel)
+    p = os.path.join(ROOT, "profiles", "%s_c2.md" % kernel)
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -357,7 +399,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default="auto", choices=["auto", "plain", "batched"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-variant comparison run")
+    ap.add_argument("--single-run", action="store_true",
+                    help="one analysis of --workload (no timing loop): the case profiled under ncu")
     args = ap.parse_args()
+    if args.single_run:
+        return single_run(args)
     dist = Dist()
     try:
         if args.impl == "reference":

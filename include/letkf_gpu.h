@@ -139,6 +139,7 @@ typedef struct lgpu_timings {
   int units;         /* (column, group) solve units */
   long long kept_pairs;   /* sum over units of kept local observations (only when counted) */
   int variant;       /* Gram variant that ran (LGPU_VARIANT_PLAIN / _BATCHED_TC) */
+  float tiles_ms;    /* BATCHED_TC: part of gram_ms spent building the tile candidate streams */
 } lgpu_timings;
 
 /* Gram variants.  PLAIN: one CTA per (column, group), FP32 on the CUDA
@@ -192,6 +193,20 @@ int lgpu_get_obs_prepared(lgpu_handle *h, float *hx, float *hx_mean, float *lat,
 int lgpu_solver_run(lgpu_handle *h);
 
 int lgpu_get_state(lgpu_handle *h, float *state, float *mean, float *sprd);
+
+/* letkf_solver_run's in-place state (src/letkf_solver.F90:283-330 overwrites
+ * state_ij, state_mean_ij, state_sprd_ij with the analysis): binds the
+ * caller's arrays (layout and arguments as lgpu_set_state).  Each following
+ * lgpu_solver_run reads the background from them and writes the analysis
+ * back into them before it returns.  The upload of the members runs on a
+ * copy stream concurrently with the search, Gram and eigensolve stages; the
+ * update runs in column chunks whose analysis is downloaded while the next
+ * chunks are computed.  Page-locked arrays (lgpu_host_alloc) give full link
+ * speed.  The arrays must stay allocated and untouched by the caller while
+ * lgpu_solver_run executes; lgpu_set_state or another lgpu_bind_state
+ * releases them. */
+int lgpu_bind_state(lgpu_handle *h, int k, int ns, float *state, float *mean, float *sprd, int nvars,
+                    const lgpu_statevar *vars);
 int lgpu_get_diag(lgpu_handle *h, float *maxhz, float *obscount, float *lg_obscount, float *lg_obsloc);
 int lgpu_get_timings(const lgpu_handle *h, lgpu_timings *t);
 int lgpu_solver_final(lgpu_handle *h);

@@ -66,10 +66,16 @@ enum {
 
 }  // namespace
 
+constexpr int kOutChunks = 16;   // column chunks of the update / analysis download of a bound state
+
 struct lgpu_handle {
   int device = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t cst = nullptr;      // host<->device copies of a bound state
   cudaEvent_t ev[8] = {};
+  cudaEvent_t ev_in[2] = {};       // bound state: mean/spread, members uploaded
+  cudaEvent_t ev_out[kOutChunks] = {};
+  float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
   std::string err;
   bool solver_ok = false, loc_ok = false, grid_ok = false, state_ok = false, obs_ok = false, ran = false;
   lgpu_solver_config scfg{0.0f, 0.0f, 1.0f, 1};
@@ -212,8 +218,13 @@ int lgpu_create(int device, lgpu_handle **out) {
   lgpu_handle *h = new lgpu_handle();
   h->device = device;
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev)
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_in)
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_out)
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   build_geom(h->geom, h->ncell);
   if (h->buf[B_GEOM].ensure(sizeof(IndexGeom)) != cudaSuccess ||
       cudaMemcpy(h->buf[B_GEOM].p, &h->geom, sizeof(IndexGeom), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -228,9 +239,13 @@ void lgpu_destroy(lgpu_handle *h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->cst) cudaStreamSynchronize(h->cst);
   for (auto &b : h->buf) b.release();
   for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : h->ev_in) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : h->ev_out) if (ev) cudaEventDestroy(ev);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->cst) cudaStreamDestroy(h->cst);
   delete h;
 }
 
@@ -361,9 +376,12 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
   return LGPU_OK;
 }
 
-int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean, const float *sprd, int nvars,
-                   const lgpu_statevar *vars) {
-  if (!h) return LGPU_ERR_ARG;
+namespace {
+
+// Validation, device buffers and slab metadata shared by lgpu_set_state and
+// lgpu_bind_state; the member data is not copied here.
+int prepare_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean, const float *sprd, int nvars,
+                  const lgpu_statevar *vars) {
   if (!h->grid_ok) return fail(h, LGPU_ERR_ORDER, "set_state before set_grid");
   if (!state || !mean || !sprd || !vars || nvars <= 0 || ns <= 0) return fail(h, LGPU_ERR_ARG, "set_state: bad arguments");
   if (k < 2) return fail(h, LGPU_ERR_ARG, "ensemble size must be >= 2");
@@ -401,9 +419,8 @@ int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const floa
   CK(h->buf[B_VARINC].ensure(nvars * 4), "alloc varinc");
   CK(h->buf[B_VARLB].ensure(nvars * 4), "alloc varlb");
   CK(h->buf[B_VARUB].ensure(nvars * 4), "alloc varub");
-  CK(cudaMemcpyAsync(h->buf[B_BKG].p, state, nx * 4, cudaMemcpyHostToDevice, h->st), "H2D state");
-  CK(cudaMemcpyAsync(h->buf[B_MEANB].p, mean, nm * 4, cudaMemcpyHostToDevice, h->st), "H2D mean");
-  CK(cudaMemcpyAsync(h->buf[B_SPRDB].p, sprd, nm * 4, cudaMemcpyHostToDevice, h->st), "H2D sprd");
+  (void)nx;
+  (void)nm;
   CK(cudaMemcpyAsync(h->buf[B_SLABVAR].p, sv.data(), ns * 4, cudaMemcpyHostToDevice, h->st), "H2D sv");
   CK(cudaMemcpyAsync(h->buf[B_SLABLEV].p, sl.data(), ns * 4, cudaMemcpyHostToDevice, h->st), "H2D sl");
   CK(cudaMemcpyAsync(h->buf[B_VARINC].p, inc.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D inc");
@@ -414,8 +431,47 @@ int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const floa
   h->ns = ns;
   h->kp = (k + 3) & ~3;
   h->vars.assign(vars, vars + nvars);
-  h->state_ok = true;
+  return LGPU_OK;
+}
+
+}  // namespace
+
+int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean, const float *sprd, int nvars,
+                   const lgpu_statevar *vars) {
+  if (!h) return LGPU_ERR_ARG;
+  h->state_ok = false;
   h->ran = false;
+  h->bound_state = h->bound_mean = h->bound_sprd = nullptr;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(cudaStreamSynchronize(h->cst), "copy stream");
+  const int rc = prepare_state(h, k, ns, state, mean, sprd, nvars, vars);
+  if (rc != LGPU_OK) return rc;
+  const size_t nx = (size_t)h->ncol * ns * k, nm = (size_t)h->ncol * ns;
+  CK(cudaMemcpyAsync(h->buf[B_BKG].p, state, nx * 4, cudaMemcpyHostToDevice, h->st), "H2D state");
+  CK(cudaMemcpyAsync(h->buf[B_MEANB].p, mean, nm * 4, cudaMemcpyHostToDevice, h->st), "H2D mean");
+  CK(cudaMemcpyAsync(h->buf[B_SPRDB].p, sprd, nm * 4, cudaMemcpyHostToDevice, h->st), "H2D sprd");
+  CK(cudaStreamSynchronize(h->st), "set_state sync");
+  h->state_ok = true;
+  return LGPU_OK;
+}
+
+// In-place state, the reference's semantics: letkf_solver_run reads the
+// background from state_ij / state_mean_ij / state_sprd_ij and overwrites
+// them with the analysis (src/letkf_solver.F90:283-330).
+int lgpu_bind_state(lgpu_handle *h, int k, int ns, float *state, float *mean, float *sprd, int nvars,
+                    const lgpu_statevar *vars) {
+  if (!h) return LGPU_ERR_ARG;
+  h->state_ok = false;
+  h->ran = false;
+  h->bound_state = h->bound_mean = h->bound_sprd = nullptr;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(cudaStreamSynchronize(h->cst), "copy stream");
+  const int rc = prepare_state(h, k, ns, state, mean, sprd, nvars, vars);
+  if (rc != LGPU_OK) return rc;
+  h->bound_state = state;
+  h->bound_mean = mean;
+  h->bound_sprd = sprd;
+  h->state_ok = true;
   return LGPU_OK;
 }
 
@@ -621,7 +677,19 @@ int lgpu_solver_run(lgpu_handle *h) {
   os.cell_start = h->buf[B_CSTART].as<int>();
   int launches = 0;
   cudaStream_t st = h->st;
+  const bool bound = h->bound_state != nullptr;
   CK(cudaEventRecord(h->ev[0], st), "event");
+  if (bound) {
+    // background upload on the copy stream, concurrent with the index,
+    // search, Gram and eigensolve stages (the update waits for it)
+    const size_t nx = (size_t)h->ncol * ns * k, nm = (size_t)h->ncol * ns;
+    CK(cudaStreamWaitEvent(h->cst, h->ev[0], 0), "stream wait");
+    CK(cudaMemcpyAsync(h->buf[B_MEANB].p, h->bound_mean, nm * 4, cudaMemcpyHostToDevice, h->cst), "H2D mean");
+    CK(cudaMemcpyAsync(h->buf[B_SPRDB].p, h->bound_sprd, nm * 4, cudaMemcpyHostToDevice, h->cst), "H2D sprd");
+    CK(cudaEventRecord(h->ev_in[0], h->cst), "event");
+    CK(cudaMemcpyAsync(h->buf[B_BKG].p, h->bound_state, nx * 4, cudaMemcpyHostToDevice, h->cst), "H2D state");
+    CK(cudaEventRecord(h->ev_in[1], h->cst), "event");
+  }
   // ---- observation index (kd_init counterpart) ----
   CK(launch_obs_index(st, h->nobs, k, kp, h->buf[B_OLAT].as<float>(), h->buf[B_OLON].as<float>(),
                       h->buf[B_OZ].as<float>(), h->buf[B_OTIME].as<float>(), h->buf[B_OVAL].as<float>(),
@@ -633,7 +701,8 @@ int lgpu_solver_run(lgpu_handle *h) {
                       h->buf[B_ATMP].as<float4>(), h->buf[B_BTMP].as<float4>(), os, &launches),
      "observation index");
   CK(cudaEventRecord(h->ev[1], st), "event");
-  // ---- per-column parameters ----
+  // ---- per-column parameters (the ocean localizer reads the background mean) ----
+  if (bound) CK(cudaStreamWaitEvent(st, h->ev_in[0], 0), "stream wait");
   CK(launch_col_prep(st, h->ncol, h->buf[B_LAT].as<float>(), h->buf[B_LON].as<float>(), h->buf[B_MASK].as<int>(),
                      h->buf[B_MEANB].as<float>(), ns, h->loc, h->buf[B_CP].as<ColPar>(),
                      h->buf[B_DMAXHZ].as<float>(), &launches),
@@ -662,6 +731,7 @@ int lgpu_solver_run(lgpu_handle *h) {
                         h->buf[B_TILEOFF].as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
                         h->buf[B_STATUS].as<int>(), &launches),
        "tile fill");
+    CK(cudaEventRecord(h->ev[6], st), "event");
     TcArgs ta;
     ta.ntiles = h->ntiles;
     ta.groups = G;
@@ -742,16 +812,44 @@ int lgpu_solver_run(lgpu_handle *h) {
   ua.rtpp = h->scfg.rtpp;
   ua.mul = h->scfg.mul;
   ua.status = h->buf[B_STATUS].as<int>();
-  CK(launch_update(st, ua, &launches), "update kernel");
+  if (!bound) {
+    ua.col0 = 0;
+    ua.ncols = h->ncol;
+    CK(launch_update(st, ua, &launches), "update kernel");
+  } else {
+    // column chunks; each chunk's analysis is copied into the caller's
+    // arrays while the next chunks are updated
+    CK(cudaStreamWaitEvent(st, h->ev_in[1], 0), "stream wait");
+    const int per = (h->ncol + kOutChunks - 1) / kOutChunks;
+    for (int c = 0; c < kOutChunks; c++) {
+      ua.col0 = c * per;
+      ua.ncols = std::min(h->ncol, (c + 1) * per) - ua.col0;
+      if (ua.ncols <= 0) break;
+      CK(launch_update(st, ua, &launches), "update kernel");
+      CK(cudaEventRecord(h->ev_out[c], st), "event");
+      CK(cudaStreamWaitEvent(h->cst, h->ev_out[c], 0), "stream wait");
+      const size_t xo = (size_t)ua.col0 * ns * k, xn = (size_t)ua.ncols * ns * k;
+      const size_t mo = (size_t)ua.col0 * ns, mn = (size_t)ua.ncols * ns;
+      CK(cudaMemcpyAsync(h->bound_state + xo, h->buf[B_ANA].as<float>() + xo, xn * 4, cudaMemcpyDeviceToHost, h->cst),
+         "D2H state");
+      CK(cudaMemcpyAsync(h->bound_mean + mo, h->buf[B_MEANA].as<float>() + mo, mn * 4, cudaMemcpyDeviceToHost, h->cst),
+         "D2H mean");
+      CK(cudaMemcpyAsync(h->bound_sprd + mo, h->buf[B_SPRDA].as<float>() + mo, mn * 4, cudaMemcpyDeviceToHost, h->cst),
+         "D2H sprd");
+    }
+  }
   CK(cudaEventRecord(h->ev[5], st), "event");
   int status = 0;
   CK(cudaMemcpyAsync(&status, h->buf[B_STATUS].p, 4, cudaMemcpyDeviceToHost, st), "D2H status");
   CK(cudaStreamSynchronize(st), "solver_run");
+  if (bound) CK(cudaStreamSynchronize(h->cst), "solver_run copies");
   float ms[5];
   for (int i = 0; i < 5; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
   h->tim.index_ms = ms[0];
   h->tim.prep_ms = ms[1];
   h->tim.gram_ms = ms[2];
+  h->tim.tiles_ms = 0.0f;
+  if (h->used_tc) CK(cudaEventElapsedTime(&h->tim.tiles_ms, h->ev[2], h->ev[6]), "timing");
   h->tim.eig_ms = ms[3];
   h->tim.update_ms = ms[4];
   CK(cudaEventElapsedTime(&h->tim.total_ms, h->ev[0], h->ev[5]), "timing");

@@ -358,6 +358,7 @@ cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
 
 struct UpdateArgs {
   int ncol, ns, k, groups;
+  int col0, ncols;        // columns [col0, col0 + ncols) of this launch
   const int *mask;        // [ncol] device
   const int *col2act;     // [ncol] active index or -1
   const ColPar *cp;

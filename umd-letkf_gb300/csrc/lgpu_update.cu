@@ -36,7 +36,7 @@ __device__ __forceinline__ int slab_group(const UpdateArgs &a, int lev, int mld)
 // smem: xb [ns][kp], xa [ns][kp], T [tg][k][kp]
 __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int kp) {
   extern __shared__ __align__(16) float sm[];
-  const int col = blockIdx.x;
+  const int col = a.col0 + blockIdx.x;
   const int k = a.k, ns = a.ns;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const size_t cbase = (size_t)col * ns * k;
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int
 }  // namespace
 
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
-  if (a.ncol <= 0) return cudaSuccess;
+  if (a.ncol <= 0 || a.ncols <= 0) return cudaSuccess;
   const int kp = (a.k + 3) & ~3;
   const size_t xbytes = 2 * (size_t)a.ns * kp * sizeof(float);
   const size_t per = (size_t)a.k * kp * sizeof(float);
@@ -184,7 +184,7 @@ cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   const size_t smem = xbytes + tg * per;
   cudaError_t e = cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_update<<<a.ncol, UT, smem, st>>>(a, tg, kp);
+  k_update<<<a.ncols, UT, smem, st>>>(a, tg, kp);
   (*launches)++;
   return cudaGetLastError();
 }

@@ -76,7 +76,7 @@ class Timings(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_float), ("index_ms", ctypes.c_float), ("prep_ms", ctypes.c_float),
                 ("gram_ms", ctypes.c_float), ("eig_ms", ctypes.c_float), ("update_ms", ctypes.c_float),
                 ("launches", ctypes.c_int), ("units", ctypes.c_int), ("kept_pairs", ctypes.c_longlong),
-                ("variant", ctypes.c_int)]
+                ("variant", ctypes.c_int), ("tiles_ms", ctypes.c_float)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -90,7 +90,7 @@ EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error",
            "lgpu_get_state", "lgpu_get_diag", "lgpu_get_timings", "lgpu_solver_final", "lgpu_get_obslist",
            "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2",
            "lgpu_get_obslist_noalloc", "lgpu_set_obs_raw", "lgpu_set_state_members", "lgpu_get_background",
-           "lgpu_get_obs_prepared", "lgpu_debug_transform"]
+           "lgpu_get_obs_prepared", "lgpu_debug_transform", "lgpu_bind_state"]
 
 _lib = None
 
@@ -134,6 +134,7 @@ def lib(path=None):
     L.lgpu_get_background.argtypes = [H, FP, FP, FP]
     L.lgpu_debug_transform.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP]
     L.lgpu_get_obs_prepared.argtypes = [H, FP, FP, FP, FP, FP, FP]
+    L.lgpu_bind_state.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP, FP, ctypes.c_int, ctypes.POINTER(_Var)]
     if path is None:
         _lib = L
     return L
@@ -326,7 +327,23 @@ class Solver:
             b = v.get("ana_bounds", (-9.99e36, 9.99e36))
             vs[i].ana_bounds[0], vs[i].ana_bounds[1] = b[0], b[1]
         self.k, self.ns = k, ns
+        self._bound = None
         return self._ck(self.L.lgpu_set_state(self.h, k, ns, _fp(state), _fp(mean), _fp(sprd), len(variables), vs))
+
+    def bind_state(self, state, mean, sprd, variables):
+        """lgpu_bind_state: every following run() reads the background from
+        these arrays and overwrites them with the analysis (in place, like the
+        reference's state_ij).  They must be writable float32 C-contiguous
+        arrays (page-locked ones, PinnedArray.array, give full link speed) and
+        stay alive while bound."""
+        for a in (state, mean, sprd):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous and a.flags.writeable):
+                raise ValueError("bind_state needs writable float32 C-contiguous arrays")
+        ncol, ns, k = state.shape
+        self.k, self.ns = k, ns
+        self._bound = (state, mean, sprd)
+        return self._ck(self.L.lgpu_bind_state(self.h, k, ns, _fp(state), _fp(mean), _fp(sprd), len(variables),
+                                               self._vars(variables)))
 
     def set_obs(self, lat, lon, zdim, time, val, err, obsid, platid, hx, hx_mean):
         arrs = [_f32(a) for a in (lat, lon, zdim, time, val, err)] + [_i32(obsid), _i32(platid)]
