@@ -28,7 +28,7 @@ __device__ __forceinline__ float wsum(float v) {
 
 __host__ __device__ __forceinline__ int eig_floats_per_warp(int k) {
   const int ld = k + 1;
-  return 2 * k * ld + 8 * k + 8;
+  return k * ld + 8 * k + 8;
 }
 
 __global__ void k_eig(EigArgs a, int wpb) {
@@ -38,9 +38,8 @@ __global__ void k_eig(EigArgs a, int wpb) {
   const int unit = blockIdx.x * wpb + warp;
   if (unit >= a.nunits) return;           // whole warps exit; no block-level barriers below
   if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
-  float *A = sm + (size_t)warp * eig_floats_per_warp(k);
-  float *Z = A + k * ld;
-  float *d = Z + k * ld;
+  float *A = sm + (size_t)warp * eig_floats_per_warp(k);   // A, then Q, then V (one k x k matrix)
+  float *d = A + k * ld;
   float *e = d + k;
   float *tau = e + k;
   float *bv = tau + k;
@@ -60,7 +59,8 @@ __global__ void k_eig(EigArgs a, int wpb) {
   for (int i = lane; i < k; i += 32) bv[i] = G[k * (k + 1) / 2 + i];
   __syncwarp();
 
-  // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j]
+  // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j];
+  // its vector v_j = A[j+1:, j] stays in column j
   for (int j = 0; j < k - 2; j++) {
     const int m = k - j - 1;                 // length of x = A[j+1:, j]
     float s = 0.0f;
@@ -111,156 +111,163 @@ __global__ void k_eig(EigArgs a, int wpb) {
     d[k - 1] = A[(k - 1) * ld + (k - 1)];
     e[k - 1] = 0.0f;
   }
-  // Z = I
-  for (int t = lane; t < k * ld; t += 32) { const int i = t / ld, j = t % ld; Z[t] = (i == j) ? 1.0f : 0.0f; }
   __syncwarp();
 
-  // ---- implicit-shift QL on (d, e).  Each sweep's scalar recurrence is
-  // evaluated redundantly by all lanes: d[i+1] is carried in a register and
-  // only e[i], d[i] (never written during the sweep) are read, so lane 0 can
-  // write results without intra-sweep barriers.  The sweep's rotations are
-  // recorded and applied to the rows of Z afterwards, lanes in parallel.
-  float *rc = p, *rs = w;   // rotation cosines / sines of one sweep
-  int bad = 0;
-  for (int l = 0; l < k; l++) {
-    int iter = 0;
-    for (;;) {
-      // first m >= l with a negligible e[m] (m = k-1 if none): lanes test
-      // 32 consecutive candidates at a time
-      int m = k - 1;
-      for (int base = l; base < k - 1; base += 32) {
-        const int mm = base + lane;
-        bool small = false;
-        if (mm < k - 1) small = fabsf(e[mm]) <= 1.1920929e-7f * (fabsf(d[mm]) + fabsf(d[mm + 1]));
-        const unsigned bal = __ballot_sync(0xffffffffu, small);
-        if (bal) { m = base + __ffs(bal) - 1; break; }
-      }
-      if (m == l) break;
-      if (++iter > 60) { bad = 1; break; }
-      const float dl = d[l], el = e[l];
-      float g = (d[l + 1] - dl) / (2.0f * el);
-      float r = sqrtf(g * g + 1.0f);
-      g = d[m] - dl + el / (g + copysignf(r, g));
-      float s = 1.0f, c = 1.0f, pp = 0.0f;
-      float di1 = d[m];
-      int i = m - 1;
-      bool deflate = false;
-      for (; i >= l; i--) {
-        const float ei = e[i], di = d[i];
-        const float f = s * ei, b = c * ei;
-        r = sqrtf(f * f + g * g);
-        if (lane == 0) e[i + 1] = r;
-        if (r == 0.0f) {
-          if (lane == 0) { d[i + 1] = di1 - pp; e[m] = 0.0f; }
-          deflate = true;
-          break;
-        }
-        const float ir = __frcp_rn(r);
-        s = f * ir;
-        c = g * ir;
-        g = di1 - pp;
-        const float rr = (di - g) * s + 2.0f * c * b;
-        pp = s * rr;
-        if (lane == 0) { d[i + 1] = g + pp; rc[i] = c; rs[i] = s; }
-        g = c * rr - b;
-        di1 = di;
-      }
-      __syncwarp();
-      // apply rotations m-1 .. ilo to columns (i, i+1) of every Z row
-      // (each lane owns rows lane and lane + 32)
-      const int ilo = deflate ? i + 1 : l;
-      if (ilo <= m - 1) {
-        const bool two = lane + 32 < k;
-        float *z0 = Z + lane * ld, *z1 = Z + (two ? lane + 32 : lane) * ld;
-        if (lane < k) {
-          float c0 = z0[m], c1 = z1[m];
-          for (int ii = m - 1; ii >= ilo; ii--) {
-            const float cc = rc[ii], ss = rs[ii];
-            const float a0 = z0[ii], a1 = z1[ii];
-            z0[ii + 1] = ss * a0 + cc * c0;
-            c0 = cc * a0 - ss * c0;
-            if (two) {
-              z1[ii + 1] = ss * a1 + cc * c1;
-              c1 = cc * a1 - ss * c1;
-            }
-          }
-          z0[ilo] = c0;
-          if (two) z1[ilo] = c1;
-        }
-      }
-      if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
-      __syncwarp();
-    }
-    if (bad) break;
-  }
-
-  // ---- back-transformation V = Q Z (reflectors applied last-to-first);
-  // each lane owns columns lane and lane + 32
+  // ---- Q = H_0 H_1 ... H_{k-3} formed in place, last reflector first: the
+  // trailing block [j+1:, j+1:] holds H_{j+1}..H_{k-3} (identity on row and
+  // column j+1); v_j is still in column j, outside the block.  Each lane owns
+  // columns lane and lane + 32.
   {
     const bool two = lane + 32 < k;
     const int c0 = lane, c1 = two ? lane + 32 : lane;
-    for (int j = k - 3; j >= 0; j--) {
+    for (int j = k - 2; j >= 0; j--) {
+      // identity on row and column j + 1 of the block
+      if (c0 > j + 1 && c0 < k) { A[(j + 1) * ld + c0] = 0.0f; A[c0 * ld + (j + 1)] = 0.0f; }
+      if (two && c1 > j + 1) { A[(j + 1) * ld + c1] = 0.0f; A[c1 * ld + (j + 1)] = 0.0f; }
+      if (lane == 0) A[(j + 1) * ld + (j + 1)] = 1.0f;
+      __syncwarp();
+      if (j > k - 3) continue;                 // the last block (2 x 2) has no reflector
       const float t = tau[j];
       if (t == 0.0f) continue;
       const int m = k - j - 1;
-      if (lane < k) {
-        float dot0 = 0.0f, dot1 = 0.0f;
-        for (int r = 0; r < m; r++) {
-          const float v = A[(j + 1 + r) * ld + j];
-          dot0 = __fmaf_rn(v, Z[(j + 1 + r) * ld + c0], dot0);
-          dot1 = __fmaf_rn(v, Z[(j + 1 + r) * ld + c1], dot1);
-        }
-        dot0 *= t;
-        dot1 *= t;
-        for (int r = 0; r < m; r++) {
-          const float v = A[(j + 1 + r) * ld + j];
-          Z[(j + 1 + r) * ld + c0] -= v * dot0;
-          if (two) Z[(j + 1 + r) * ld + c1] -= v * dot1;
-        }
+      // w_c = t * sum_r v_r Q[r][c]; Q[r][c] -= v_r w_c  (rows, columns j+1..k-1)
+      float w0 = 0.0f, w1 = 0.0f;
+      const bool in0 = c0 > j && c0 < k, in1 = two && c1 > j;
+      for (int r = 0; r < m; r++) {
+        const float v = A[(j + 1 + r) * ld + j];
+        if (in0) w0 = __fmaf_rn(v, A[(j + 1 + r) * ld + c0], w0);
+        if (in1) w1 = __fmaf_rn(v, A[(j + 1 + r) * ld + c1], w1);
       }
+      w0 *= t;
+      w1 *= t;
+      __syncwarp();
+      for (int r = 0; r < m; r++) {
+        const float v = A[(j + 1 + r) * ld + j];
+        if (in0) A[(j + 1 + r) * ld + c0] -= v * w0;
+        if (in1) A[(j + 1 + r) * ld + c1] -= v * w1;
+      }
+      __syncwarp();
+    }
+    // row and column 0: Q e_0 = e_0
+    if (c0 > 0 && c0 < k) { A[c0] = 0.0f; A[c0 * ld] = 0.0f; }
+    if (two) { A[c1] = 0.0f; A[c1 * ld] = 0.0f; }
+    if (lane == 0) A[0] = 1.0f;
+    __syncwarp();
+  }
+
+  // ---- implicit-shift QL on (d, e), rotations applied at once to the
+  // columns (i, i+1) of Q (V = Q Z).  The scalar recurrence is evaluated
+  // redundantly by every lane: d[i+1] is carried in a register and only e[i],
+  // d[i] (not yet written in this sweep) are read, so lane 0 alone writes
+  // results, without barriers inside the sweep.  Each lane owns rows lane and
+  // lane + 32 of Q and carries the pending column i+1 of its rows.
+  int bad = 0;
+  {
+    const bool two = lane + 32 < k;
+    const bool own = lane < k;
+    float *q0 = A + (own ? lane : 0) * ld, *q1 = A + (two ? lane + 32 : 0) * ld;
+    for (int l = 0; l < k; l++) {
+      int iter = 0;
+      for (;;) {
+        // first m >= l with a negligible e[m] (m = k-1 if none): lanes test
+        // 32 consecutive candidates at a time
+        int m = k - 1;
+        for (int base = l; base < k - 1; base += 32) {
+          const int mm = base + lane;
+          bool small = false;
+          if (mm < k - 1) small = fabsf(e[mm]) <= 1.1920929e-7f * (fabsf(d[mm]) + fabsf(d[mm + 1]));
+          const unsigned bal = __ballot_sync(0xffffffffu, small);
+          if (bal) { m = base + __ffs(bal) - 1; break; }
+        }
+        if (m == l) break;
+        if (++iter > 60) { bad = 1; break; }
+        const float dl = d[l], el = e[l];
+        float g = (d[l + 1] - dl) / (2.0f * el);
+        float r = sqrtf(g * g + 1.0f);
+        g = d[m] - dl + el / (g + copysignf(r, g));
+        float s = 1.0f, c = 1.0f, pp = 0.0f;
+        float di1 = d[m];
+        float z0 = own ? q0[m] : 0.0f, z1 = two ? q1[m] : 0.0f;   // pending column i+1
+        float ei = e[m - 1], di = d[m - 1];
+        int i = m - 1;
+        bool deflate = false;
+        for (; i >= l; i--) {
+          const int in = i > 0 ? i - 1 : 0;
+          const float ei_n = e[in], di_n = d[in];           // next step's operands
+          const float a0 = own ? q0[i] : 0.0f, a1 = two ? q1[i] : 0.0f;
+          const float f = s * ei, b = c * ei;
+          r = sqrtf(f * f + g * g);
+          if (lane == 0) e[i + 1] = r;
+          if (r == 0.0f) {
+            if (lane == 0) { d[i + 1] = di1 - pp; e[m] = 0.0f; }
+            deflate = true;
+            break;
+          }
+          const float ir = __frcp_rn(r);
+          s = f * ir;
+          c = g * ir;
+          g = di1 - pp;
+          const float rr = (di - g) * s + 2.0f * c * b;
+          pp = s * rr;
+          if (lane == 0) d[i + 1] = g + pp;
+          g = c * rr - b;
+          di1 = di;
+          // rotation (c, s) on columns (i, i+1) of the lane's rows
+          if (own) { q0[i + 1] = s * a0 + c * z0; z0 = c * a0 - s * z0; }
+          if (two) { q1[i + 1] = s * a1 + c * z1; z1 = c * a1 - s * z1; }
+          ei = ei_n;
+          di = di_n;
+        }
+        const int ilo = deflate ? i + 1 : l;
+        if (own) q0[ilo] = z0;
+        if (two) q1[ilo] = z1;
+        if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
+        __syncwarp();
+      }
+      if (bad) break;
     }
   }
   __syncwarp();
 
   // ---- spectral functions: f = sqrt((k-1)/lambda), g = 1/lambda
-  //      (src/letkf_core.F90:111-113, :128-131)
+  //      (src/letkf_core.F90:111-113, :128-131); fl holds sqrt(f)
   for (int l = lane; l < k; l += 32) {
     const float lam = d[l];
     if (!(lam > 0.0f)) bad |= 2;
-    fl[l] = sqrtf((float)(k - 1) / lam);
+    fl[l] = sqrtf(sqrtf((float)(k - 1) / lam));
     gl[l] = 1.0f / lam;
   }
   __syncwarp();
   // s_l = g_l * (V^T b)_l
   for (int l = lane; l < k; l += 32) {
     float acc = 0.0f;
-    for (int q = 0; q < k; q++) acc = __fmaf_rn(Z[q * ld + l], bv[q], acc);
+    for (int q = 0; q < k; q++) acc = __fmaf_rn(A[q * ld + l], bv[q], acc);
     p[l] = gl[l] * acc;
   }
   __syncwarp();
   // wbar_i = sum_l V[i][l] s_l
   for (int i = lane; i < k; i += 32) {
     float acc = 0.0f;
-    for (int l = 0; l < k; l++) acc = __fmaf_rn(Z[i * ld + l], p[l], acc);
+    for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], p[l], acc);
     w[i] = acc;
   }
-  // Y = V diag(f) into A (A is no longer needed)
   __syncwarp();
-  for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] = Z[i * ld + l] * fl[l]; }
+  // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
+  for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] *= fl[l]; }
   __syncwarp();
-  // T_ij = sum_l Y[i][l] V[j][l] + wbar_i ; lane owns columns lane, lane + 32
+  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; lane owns columns lane, lane + 32
   float *T = a.T + (size_t)unit * k * k;
   if (lane < k) {
     const bool two = lane + 32 < k;
     const int j0 = lane, j1 = two ? lane + 32 : lane;
-    const float *v0 = Z + j0 * ld, *v1 = Z + j1 * ld;
+    const float *u0 = A + j0 * ld, *u1 = A + j1 * ld;
     for (int i = 0; i < k; i++) {
-      const float *yr = A + i * ld;
+      const float *ur = A + i * ld;
       float acc0 = 0.0f, acc1 = 0.0f;
       for (int l = 0; l < k; l++) {
-        const float y = yr[l];
-        acc0 = __fmaf_rn(y, v0[l], acc0);
-        acc1 = __fmaf_rn(y, v1[l], acc1);
+        const float y = ur[l];
+        acc0 = __fmaf_rn(y, u0[l], acc0);
+        acc1 = __fmaf_rn(y, u1[l], acc1);
       }
       T[i * k + j0] = acc0 + w[i];
       if (two) T[i * k + j1] = acc1 + w[i];
@@ -290,10 +297,19 @@ cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G,
 
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches) {
   if (a.nunits <= 0) return cudaSuccess;
-  const int per = eig_floats_per_warp(a.k);
-  int wpb = 4;
-  while (wpb > 1 && (size_t)wpb * per * sizeof(float) > 96 * 1024) wpb--;
-  const size_t smem = (size_t)wpb * per * sizeof(float);
+  // warps per block: the most resident warps per SM for this unit size
+  const size_t per = (size_t)eig_floats_per_warp(a.k) * sizeof(float);
+  const size_t sm_bytes = 227 * 1024;
+  int wpb = 1, best = 0;
+  for (int c = 1; c <= 8; c++) {
+    if ((size_t)c * per > sm_bytes) break;
+    int blocks = (int)(sm_bytes / ((size_t)c * per + 1024));   // 1 KB reserved per block
+    if (blocks > 32) blocks = 32;
+    int warps = blocks * c;
+    if (warps > 64) warps = 64;
+    if (warps > best) { best = warps; wpb = c; }
+  }
+  const size_t smem = (size_t)wpb * per;
   cudaError_t e = cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int grid = (a.nunits + wpb - 1) / wpb;
