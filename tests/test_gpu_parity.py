@@ -62,6 +62,31 @@ def test_gc_fast_and_exact(solver):
     assert np.array_equal(exact[:20000].view(np.uint32), ref.view(np.uint32))
 
 
+def test_fast_weight_path_bounds(solver):
+    """The batched Gram's fast distance and weight against the exact ones,
+    near the search radius and the 1e-4 keep threshold (the bands that send a
+    pair to the exact path hold a 5x margin over these bounds)."""
+    rng = np.random.default_rng(21)
+    n = 400000
+    L = rng.choice(np.array([60e3, 200e3, 500e3, 800e3], np.float32), n)
+    lat1 = rng.uniform(-89.0, 89.0, n)
+    lon1 = rng.uniform(0.0, 360.0, n)
+    # separations spread over the whole support, denser near the keep threshold (z/c ~ 1.78-1.83)
+    zc = np.where(rng.random(n) < 0.5, rng.uniform(0.0, 2.0, n), rng.uniform(1.70, 1.90, n))
+    dist = zc * L / np.sqrt(0.3)
+    brg = rng.uniform(0.0, 2 * np.pi, n)
+    dlat = np.degrees(dist / 6371e3) * np.cos(brg)
+    lat2 = np.clip(lat1 + dlat, -89.9, 89.9)
+    lon2 = (lon1 + np.degrees(dist / 6371e3) * np.sin(brg) / np.cos(np.radians(lat1))) % 360.0
+    de, df, re, rf = solver.debug_weight(lat1, lon1, lat2, lon2, L)
+    ok = de > 1.0
+    assert np.max(np.abs(df[ok].astype(np.float64) / de[ok] - 1.0)) <= 1e-6
+    near = (re > 2e-5) & (re < 5e-4)
+    assert near.sum() > 10000
+    assert np.max(np.abs(rf[near].astype(np.float64) - re[near])) <= 2e-8
+    assert np.max(np.abs(rf.astype(np.float64) - re)) <= 1e-6
+
+
 LIST_CASES = [("simple3d", None), ("ocean", None), ("c1", None), ("c2small", 150), ("c3small", 150)]
 
 
@@ -157,6 +182,18 @@ def test_analysis_parity(name, gram):
     rng = np.random.default_rng(2)
     cols = np.sort(rng.choice(active, size=min(600, len(active)), replace=False))
     _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label=name, variant=gram)
+
+
+@pytest.mark.parametrize("k", [12, 20])
+def test_ocean_groups_with_k_multiple_of_4(k):
+    """loc_ocean (two localisation groups) with k a multiple of 4: the update
+    stages both groups' transforms with bulk async copies."""
+    cfg = workload_cfg("ocean")
+    prob = workload("ocean", k=k)
+    active = np.nonzero(prob.mask == 0)[0]
+    cols = active[:: max(1, len(active) // 400)]
+    for gram in ("plain", "batched"):
+        _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label="ocean k=%d" % k, variant=gram)
 
 
 def test_single_observation_closed_form():

@@ -1064,6 +1064,26 @@ int lgpu_debug_metric(lgpu_handle *h, int n, const float *lat1, const float *lon
   return LGPU_OK;
 }
 
+int lgpu_debug_weight(lgpu_handle *h, int n, const float *lat1, const float *lon1, const float *lat2,
+                      const float *lon2, const float *L, float *out) {
+  if (!h || n < 0 || (n > 0 && (!lat1 || !lon1 || !lat2 || !lon2 || !L || !out))) return LGPU_ERR_ARG;
+  if (n == 0) return LGPU_OK;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  float *d = nullptr;
+  CK(cudaMalloc(&d, 9 * sizeof(float) * (size_t)n), "alloc");
+  const float *src[5] = {lat1, lon1, lat2, lon2, L};
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < 5 && e == cudaSuccess; q++)
+    e = cudaMemcpyAsync(d + q * (size_t)n, src[q], 4 * (size_t)n, cudaMemcpyHostToDevice, h->st);
+  if (e == cudaSuccess) e = launch_debug_weight(h->st, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n,
+                                                d + 4 * (size_t)n, d + 5 * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + 5 * (size_t)n, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(h, e, "debug_weight");
+  return LGPU_OK;
+}
+
 int lgpu_debug_gc(lgpu_handle *h, int n, const float *z, const float *L, float *gc) {
   if (!h || n < 0 || (n > 0 && (!z || !L || !gc))) return LGPU_ERR_ARG;
   if (n == 0) return LGPU_OK;

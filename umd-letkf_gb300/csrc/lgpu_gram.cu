@@ -382,6 +382,20 @@ __global__ void k_debug_gc(int n, const float *z, const float *L, float *fast, f
   exact[i] = gc_exact(z[i], L[i]);
 }
 
+// exact and fast (batched-path) distance and single-factor weight of point pairs
+__global__ void k_debug_weight(int n, const float *lat1, const float *lon1, const float *lat2, const float *lon2,
+                               const float *L, float *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 a = unitvec_exact(lat1[i], lon1[i]), b = unitvec_exact(lat2[i], lon2[i]);
+  const float de = dist_from_chord2(chord2_exact(a.x, a.y, a.z, b.x, b.y, b.z));
+  const float df = dist_fast(chord2_fast(a.x, a.y, a.z, b.x, b.y, b.z));
+  out[i] = de;
+  out[n + i] = df;
+  out[2 * n + i] = gc_exact(de, L[i]);
+  out[3 * n + i] = gc_branchless(df * inv_c_of(L[i]));
+}
+
 }  // namespace
 
 size_t gram_smem_bytes(int k) {
@@ -425,6 +439,13 @@ cudaError_t launch_debug_metric(cudaStream_t st, int n, const float *lat1, const
 cudaError_t launch_debug_gc(cudaStream_t st, int n, const float *z, const float *L, float *fast, float *exact) {
   if (n <= 0) return cudaSuccess;
   k_debug_gc<<<(n + 255) / 256, 256, 0, st>>>(n, z, L, fast, exact);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_debug_weight(cudaStream_t st, int n, const float *lat1, const float *lon1, const float *lat2,
+                                const float *lon2, const float *L, float *out) {
+  if (n <= 0) return cudaSuccess;
+  k_debug_weight<<<(n + 255) / 256, 256, 0, st>>>(n, lat1, lon1, lat2, lon2, L, out);
   return cudaGetLastError();
 }
 

@@ -61,7 +61,6 @@ constexpr int NSMAX = 3, NRMAX = 8;
 constexpr uint32_t CMB = 128;                 // bytes per core matrix (8 rows x 16 B)
 constexpr uint32_t SBO = (KC / 4) * CMB;      // bytes per 8-row group (all K of the chunk)
 constexpr uint32_t WB = (TM / 8) * SBO;       // bytes per W operand copy
-constexpr float kGuardFast = 3.0e-6f;         // keep-threshold band where the exact distance is re-evaluated
 constexpr size_t kSmemBudget = 227 * 1024 - 4096;   // dynamic shared memory (static part below 4 KB)
 constexpr int WT = 256;        // threads of the stream kernels
 constexpr int YS = 20;         // floats per member row of a chunk record (16 observations + 4: conflict-free rows)
@@ -300,44 +299,6 @@ struct TcSmem {
   unsigned char fj[NPMAX];
 };
 
-// asin(x), 0 <= x <= 0.5: Taylor series of asin to x^21 in Horner form with
-// fused multiply-adds (a few ulp)
-__device__ __forceinline__ float asin_fast(float x) {
-  const float x2 = x * x;
-  float p = 0.008390335366129875f;
-  p = __fmaf_rn(p, x2, 0.009761609137058258f);
-  p = __fmaf_rn(p, x2, 0.01155180111527443f);
-  p = __fmaf_rn(p, x2, 0.013964843936264515f);
-  p = __fmaf_rn(p, x2, 0.017352763563394547f);
-  p = __fmaf_rn(p, x2, 0.022372158244252205f);
-  p = __fmaf_rn(p, x2, 0.0303819440305233f);
-  p = __fmaf_rn(p, x2, 0.0446428582072258f);
-  p = __fmaf_rn(p, x2, 0.07500000298023224f);
-  p = __fmaf_rn(p, x2, 0.1666666716337204f);
-  return __fmaf_rn(x * x2, p, x);
-}
-
-// Gaspari-Cohn of zc = |z| / c without branches: the same two polynomials as
-// gc_fast (outer one in the shifted variable t = 2 - zc, divided by zc with
-// the approximate divide); within 1e-6 of gc_exact.
-__device__ __forceinline__ float gc_branchless(float zc) {
-  const float t = 2.0f - zc;
-  float q = 0.08333f;
-  q = __fmaf_rn(q, t, -0.49996f);
-  q = __fmaf_rn(q, t, 0.6248f);
-  q = __fmaf_rn(q, t, 0.0005299999999996974f);
-  q = __fmaf_rn(q, t, -0.0007799999999991147f);
-  q = __fmaf_rn(q, t, 0.0005999999999986017f);
-  q = __fmaf_rn(q, t, -0.0001899999999991353f);
-  const float qo = __fdividef(q, zc);
-  float p = -0.25f;
-  p = __fmaf_rn(p, zc, 0.5f);
-  p = __fmaf_rn(p, zc, 0.625f);
-  p = __fmaf_rn(p, zc, -1.66667f);
-  const float pi = __fmaf_rn(p, zc * zc, 1.0f);
-  return zc >= 2.0f ? 0.0f : (zc > 1.0f ? qo : pi);
-}
-
 // per-CTA constants of the localizer's fast path
 struct LocK {
   float icv, levg;            // vtgc: vertical 1/c, depth of the group's level
@@ -427,7 +388,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       const float sh = sinf(hq);
       c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
     }
-    const float rlo = cp.rmax * (1.0f - 2e-5f), rhi = cp.rmax * (1.0f + 2e-5f);
+    const float rlo = cp.rmax * (1.0f - kFastDistBand), rhi = cp.rmax * (1.0f + kFastDistBand);
     LocK lk;
     lk.icv = LOC == LOC_VTGC ? inv_c_of(a.loc.vloc) : 1.0f;
     lk.levg = LOC == LOC_VTGC ? a.loc.lev_depth[g] : 0.0f;
@@ -460,8 +421,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         const int e = wq * 4 + u;
         const float4 A = RA[e];
         const float4 B = RA[16 + e];
-        const float dx = __fsub_rn(cp.ux, A.x), dy = __fsub_rn(cp.uy, A.y), dz = __fsub_rn(cp.uz, A.z);
-        const float c2f = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
+        const float c2f = chord2_fast(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
         const bool cand = (ch * KC + e < ntile) && (c2f <= c2max);
         const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
         const float d = 12742000.0f * asin_fast(fminf(hf, 0.5f));

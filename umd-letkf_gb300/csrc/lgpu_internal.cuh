@@ -185,6 +185,68 @@ constexpr float kGuard1 = 1.0e-6f;        // fast-GC guard band, one factor
 constexpr float kGuard2 = 3.0e-6f;        // two-factor products
 constexpr float kStdev2Max = 3.65148377f; // SQRT(40.0/3.0) in REAL, src/letkf_solver.F90:47
 
+// ---------------------------------------------- fast weight path -----
+// The batched Gram evaluates distance and Gaspari-Cohn in float with fused
+// multiply-adds and approximate reciprocals, and falls back to the exact
+// metric and the per-column localizer for a pair whose fast distance lies
+// within kFastDistBand (relative) of the search radius or whose fast weight
+// lies within kGuardFast of the keep threshold.  Against the exact path the
+// fast distance is within 1e-6 relative and the fast weight within 2e-8
+// absolute near the keep threshold (tests/test_gpu_parity.py); the bands
+// hold a 5x margin over those bounds.
+constexpr float kFastDistBand = 5.0e-6f;
+constexpr float kGuardFast = 1.0e-7f;
+
+// squared chord between unit vectors, fused multiply-adds
+__device__ __forceinline__ float chord2_fast(float ax, float ay, float az, float bx, float by, float bz) {
+  const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+  return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
+}
+
+// asin(x), 0 <= x <= 0.5: Taylor series of asin to x^21 in Horner form with
+// fused multiply-adds (a few ulp)
+__device__ __forceinline__ float asin_fast(float x) {
+  const float x2 = x * x;
+  float p = 0.008390335366129875f;
+  p = __fmaf_rn(p, x2, 0.009761609137058258f);
+  p = __fmaf_rn(p, x2, 0.01155180111527443f);
+  p = __fmaf_rn(p, x2, 0.013964843936264515f);
+  p = __fmaf_rn(p, x2, 0.017352763563394547f);
+  p = __fmaf_rn(p, x2, 0.022372158244252205f);
+  p = __fmaf_rn(p, x2, 0.0303819440305233f);
+  p = __fmaf_rn(p, x2, 0.0446428582072258f);
+  p = __fmaf_rn(p, x2, 0.07500000298023224f);
+  p = __fmaf_rn(p, x2, 0.1666666716337204f);
+  return __fmaf_rn(x * x2, p, x);
+}
+
+// Gaspari-Cohn of zc = |z| / c without branches: the same two polynomials as
+// gc_fast (outer one in the shifted variable t = 2 - zc, divided by zc with
+// the approximate divide); within 1e-6 of gc_exact.
+__device__ __forceinline__ float gc_branchless(float zc) {
+  const float t = 2.0f - zc;
+  float q = 0.08333f;
+  q = __fmaf_rn(q, t, -0.49996f);
+  q = __fmaf_rn(q, t, 0.6248f);
+  q = __fmaf_rn(q, t, 0.0005299999999996974f);
+  q = __fmaf_rn(q, t, -0.0007799999999991147f);
+  q = __fmaf_rn(q, t, 0.0005999999999986017f);
+  q = __fmaf_rn(q, t, -0.0001899999999991353f);
+  const float qo = __fdividef(q, zc);
+  float p = -0.25f;
+  p = __fmaf_rn(p, zc, 0.5f);
+  p = __fmaf_rn(p, zc, 0.625f);
+  p = __fmaf_rn(p, zc, -1.66667f);
+  const float pi = __fmaf_rn(p, zc * zc, 1.0f);
+  return zc >= 2.0f ? 0.0f : (zc > 1.0f ? qo : pi);
+}
+
+// great-circle distance (m) from the squared chord, fast path (chord <= 1)
+__device__ __forceinline__ float dist_fast(float c2f) {
+  const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
+  return 12742000.0f * asin_fast(fminf(hf, 0.5f));
+}
+
 // Packed Gram layout of one unit: the upper triangle of G (i <= j, row-major)
 // followed by the right-hand side b; k(k+3)/2 floats.
 __host__ __device__ __forceinline__ int tri_off(int i, int k) { return i * k - (i * (i - 1)) / 2; }
@@ -382,5 +444,7 @@ cudaError_t launch_obslist(cudaStream_t st, int col, int gid, int group_slot, co
 cudaError_t launch_debug_metric(cudaStream_t st, int n, const float *lat1, const float *lon1,
                                 const float *lat2, const float *lon2, float *dist);
 cudaError_t launch_debug_gc(cudaStream_t st, int n, const float *z, const float *L, float *fast, float *exact);
+cudaError_t launch_debug_weight(cudaStream_t st, int n, const float *lat1, const float *lon1, const float *lat2,
+                                const float *lon2, const float *L, float *out);
 
 }  // namespace lgpu

@@ -33,6 +33,63 @@ __device__ __forceinline__ int slab_group(const UpdateArgs &a, int lev, int mld)
   return 0;
 }
 
+// Epilogue of one slab, one warp (lane owns members lane and lane + 32):
+// recenter, mean-increment clip, RTPS, RTPP, multiplicative inflation,
+// member bounds and re-mean, spread; writes the analysis members, mean and
+// spread of (col, s).  xr: X_b T row, br: background perturbation row.
+__device__ __forceinline__ void slab_epilogue(const UpdateArgs &a, int col, int s, const float *xr, const float *br,
+                                              int lane) {
+  const int k = a.k, ns = a.ns;
+  const float kf = (float)k, km1 = (float)(k - 1);
+  const size_t cbase = (size_t)col * ns * k;
+  const int v = a.slab_var[s];
+  const int j0 = lane, j1 = lane + 32;
+  float x0 = j0 < k ? xr[j0] : 0.0f, x1 = j1 < k ? xr[j1] : 0.0f;
+  const float xb0 = j0 < k ? br[j0] : 0.0f, xb1 = j1 < k ? br[j1] : 0.0f;
+  const float mb = a.mean_b[(size_t)col * ns + s], sb = a.sprd_b[(size_t)col * ns + s];
+  if (j0 < k) x0 = x0 + mb;
+  if (j1 < k) x1 = x1 + mb;
+  float m = bsum(x0 + x1) / kf;
+  if (j0 < k) x0 = x0 - m;
+  if (j1 < k) x1 = x1 - m;
+  const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
+  {
+    float r = m - mb;
+    r = fmaxf(r, -inc); r = fminf(r, inc);
+    r = fmaxf(r, lb - mb); r = fminf(r, ub - mb);
+    m = r + mb;
+  }
+  if (a.rtps > 0.0f) {
+    const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
+    if (sa > 0.0f) {
+      const float f = a.rtps * (sb - sa) / sa + 1.0f;
+      x0 = x0 * f; x1 = x1 * f;
+    }
+  }
+  if (a.rtpp > 0.0f) {
+    x0 = a.rtpp * xb0 + (1.0f - a.rtpp) * x0;
+    x1 = a.rtpp * xb1 + (1.0f - a.rtpp) * x1;
+  }
+  if (a.mul != 1.0f) { x0 = x0 * a.mul; x1 = x1 * a.mul; }
+  {
+    if (j0 < k) { x0 = fmaxf(x0, lb - m); x0 = fminf(x0, ub - m); }
+    if (j1 < k) { x1 = fmaxf(x1, lb - m); x1 = fminf(x1, ub - m); }
+    const float r = bsum(x0 + x1) / kf;
+    if (j0 < k) x0 = x0 - r;
+    if (j1 < k) x1 = x1 - r;
+    m = m + r;
+  }
+  const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
+  float *out = a.ana + cbase + (size_t)s * k;
+  if (j0 < k) out[j0] = x0 + m;
+  if (j1 < k) out[j1] = x1 + m;
+  if (lane == 0) {
+    a.mean_a[(size_t)col * ns + s] = m;
+    a.sprd_a[(size_t)col * ns + s] = sa;
+    if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
+  }
+}
+
 // smem: xb [ns][kp], xa [ns][kp], T [tg][k][kp]
 __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int kp) {
   extern __shared__ __align__(16) float sm[];
@@ -118,62 +175,162 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int
   }
   __syncthreads();
   // ---- epilogue, one warp per slab
-  const float kf = (float)k, km1 = (float)(k - 1);
-  for (int s = warp; s < ns; s += nw) {
-    const int v = a.slab_var[s];
-    const int j0 = lane, j1 = lane + 32;
-    const float *xr = xa + (size_t)s * kp, *br = xb + (size_t)s * kp;
-    float x0 = j0 < k ? xr[j0] : 0.0f, x1 = j1 < k ? xr[j1] : 0.0f;
-    const float xb0 = j0 < k ? br[j0] : 0.0f, xb1 = j1 < k ? br[j1] : 0.0f;
-    const float mb = a.mean_b[(size_t)col * ns + s], sb = a.sprd_b[(size_t)col * ns + s];
-    if (j0 < k) x0 = x0 + mb;
-    if (j1 < k) x1 = x1 + mb;
-    float m = bsum(x0 + x1) / kf;
-    if (j0 < k) x0 = x0 - m;
-    if (j1 < k) x1 = x1 - m;
-    const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
-    {
-      float r = m - mb;
-      r = fmaxf(r, -inc); r = fminf(r, inc);
-      r = fmaxf(r, lb - mb); r = fminf(r, ub - mb);
-      m = r + mb;
-    }
-    if (a.rtps > 0.0f) {
-      const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
-      if (sa > 0.0f) {
-        const float f = a.rtps * (sb - sa) / sa + 1.0f;
-        x0 = x0 * f; x1 = x1 * f;
-      }
-    }
-    if (a.rtpp > 0.0f) {
-      x0 = a.rtpp * xb0 + (1.0f - a.rtpp) * x0;
-      x1 = a.rtpp * xb1 + (1.0f - a.rtpp) * x1;
-    }
-    if (a.mul != 1.0f) { x0 = x0 * a.mul; x1 = x1 * a.mul; }
-    {
-      if (j0 < k) { x0 = fmaxf(x0, lb - m); x0 = fminf(x0, ub - m); }
-      if (j1 < k) { x1 = fmaxf(x1, lb - m); x1 = fminf(x1, ub - m); }
-      const float r = bsum(x0 + x1) / kf;
-      if (j0 < k) x0 = x0 - r;
-      if (j1 < k) x1 = x1 - r;
-      m = m + r;
-    }
-    const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
-    float *out = a.ana + cbase + (size_t)s * k;
-    if (j0 < k) out[j0] = x0 + m;
-    if (j1 < k) out[j1] = x1 + m;
-    if (lane == 0) {
-      a.mean_a[(size_t)col * ns + s] = m;
-      a.sprd_a[(size_t)col * ns + s] = sa;
-      if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
+  for (int s = warp; s < ns; s += nw) slab_epilogue(a, col, s, xa + (size_t)s * kp, xb + (size_t)s * kp, lane);
+}
+
+// Thread-per-slab form for k a multiple of 4 (k <= KMAX): one CTA per
+// column, thread s owns slab s.  The group transforms are staged in shared
+// memory (broadcast reads); the slab's analysis members stay in registers,
+// so the epilogue's member sums run sequentially in member order (the
+// reference's SUM) without shuffles.
+template <int KMAX>
+__global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
+  extern __shared__ __align__(16) float Tsm[];   // [groups][k][k]
+  const int col = a.col0 + blockIdx.x;
+  const int k = a.k, ns = a.ns, G = a.groups, kk = k * k, k4 = k >> 2;
+  const int s = threadIdx.x;
+  const size_t cbase = (size_t)col * ns * k;
+  const int act = a.col2act[col];
+  const bool skip = a.mask[col] || act < 0;
+  if (!skip) {
+    for (int g = 0; g < G; g++) {
+      if (a.nkept[(size_t)act * G + g] <= 0) continue;
+      const float4 *src = reinterpret_cast<const float4 *>(a.T + ((size_t)act * G + g) * kk);
+      float4 *dst = reinterpret_cast<float4 *>(Tsm + (size_t)g * kk);
+      for (int t = threadIdx.x; t < (kk >> 2); t += blockDim.x) dst[t] = src[t];
     }
   }
+  __syncthreads();
+  if (s >= ns) return;
+  const float4 *xb4 = reinterpret_cast<const float4 *>(a.bkg + cbase + (size_t)s * k);
+  float4 *out4 = reinterpret_cast<float4 *>(a.ana + cbase + (size_t)s * k);
+  const size_t ms = (size_t)col * ns + s;
+  if (skip) {   // src/letkf_solver.F90:207
+    for (int q = 0; q < k4; q++) out4[q] = xb4[q];
+    a.mean_a[ms] = a.mean_b[ms];
+    a.sprd_a[ms] = a.sprd_b[ms];
+    return;
+  }
+  const int g = slab_group(a, a.slab_lev[s], a.cp[col].mld);
+  const bool has = g < G && a.nkept[(size_t)act * G + g] > 0;
+  float x[KMAX];
+#pragma unroll
+  for (int j = 0; j < KMAX; j++) x[j] = 0.0f;
+  if (has) {
+    // x_a = x_b T_g (src/letkf_solver.F90:285-289), members accumulated in i order
+    const float *T = Tsm + (size_t)g * kk;
+    for (int i4 = 0; i4 < k4; i4++) {
+      const float4 xv = xb4[i4];
+      const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float4 *Tr = reinterpret_cast<const float4 *>(T + (size_t)(4 * i4 + u) * k);
+#pragma unroll
+        for (int q = 0; q < KMAX / 4; q++) {
+          if (q < k4) {
+            const float4 t = Tr[q];
+            x[4 * q + 0] = __fmaf_rn(xs[u], t.x, x[4 * q + 0]);
+            x[4 * q + 1] = __fmaf_rn(xs[u], t.y, x[4 * q + 1]);
+            x[4 * q + 2] = __fmaf_rn(xs[u], t.z, x[4 * q + 2]);
+            x[4 * q + 3] = __fmaf_rn(xs[u], t.w, x[4 * q + 3]);
+          }
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < KMAX / 4; q++)
+      if (q < k4) {
+        const float4 v = xb4[q];
+        x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+      }
+  }
+  const float kf = (float)k, km1 = (float)(k - 1);
+  const int v = a.slab_var[s];
+  const float mb = a.mean_b[ms], sb = a.sprd_b[ms];
+  // recenter (:299-303)
+  float m = 0.0f;
+#pragma unroll
+  for (int j = 0; j < KMAX; j++)
+    if (j < k) { x[j] = x[j] + mb; m = m + x[j]; }
+  m = m / kf;
+#pragma unroll
+  for (int j = 0; j < KMAX; j++) x[j] = x[j] - m;
+  // mean increment clip and bounds (:308-318)
+  const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
+  {
+    float r = m - mb;
+    r = fmaxf(r, -inc); r = fminf(r, inc);
+    r = fmaxf(r, lb - mb); r = fminf(r, ub - mb);
+    m = r + mb;
+  }
+  if (a.rtps > 0.0f) {   // (:322-335)
+    float q2 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < KMAX; j++)
+      if (j < k) q2 = q2 + x[j] * x[j];
+    const float sa = sqrtf(q2 / km1);
+    if (sa > 0.0f) {
+      const float f = a.rtps * (sb - sa) / sa + 1.0f;
+#pragma unroll
+      for (int j = 0; j < KMAX; j++) x[j] = x[j] * f;
+    }
+  }
+  if (a.rtpp > 0.0f) {   // (:339-344)
+#pragma unroll
+    for (int q = 0; q < KMAX / 4; q++)
+      if (q < k4) {
+        const float4 b = xb4[q];
+        x[4 * q + 0] = a.rtpp * b.x + (1.0f - a.rtpp) * x[4 * q + 0];
+        x[4 * q + 1] = a.rtpp * b.y + (1.0f - a.rtpp) * x[4 * q + 1];
+        x[4 * q + 2] = a.rtpp * b.z + (1.0f - a.rtpp) * x[4 * q + 2];
+        x[4 * q + 3] = a.rtpp * b.w + (1.0f - a.rtpp) * x[4 * q + 3];
+      }
+  }
+  if (a.mul != 1.0f) {   // (:347-349)
+#pragma unroll
+    for (int j = 0; j < KMAX; j++) x[j] = x[j] * a.mul;
+  }
+  {   // member bounds and re-mean (:357-371)
+    float r = 0.0f;
+#pragma unroll
+    for (int j = 0; j < KMAX; j++)
+      if (j < k) {
+        x[j] = fminf(fmaxf(x[j], lb - m), ub - m);
+        r = r + x[j];
+      }
+    r = r / kf;
+#pragma unroll
+    for (int j = 0; j < KMAX; j++) x[j] = x[j] - r;
+    m = m + r;
+  }
+  float q2 = 0.0f;   // spread (:375-379)
+#pragma unroll
+  for (int j = 0; j < KMAX; j++)
+    if (j < k) q2 = q2 + x[j] * x[j];
+  const float sa = sqrtf(q2 / km1);
+#pragma unroll
+  for (int q = 0; q < KMAX / 4; q++)
+    if (q < k4) out4[q] = make_float4(x[4 * q] + m, x[4 * q + 1] + m, x[4 * q + 2] + m, x[4 * q + 3] + m);
+  a.mean_a[ms] = m;
+  a.sprd_a[ms] = sa;
+  if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
 }
 
 }  // namespace
 
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   if (a.ncol <= 0 || a.ncols <= 0) return cudaSuccess;
+  const size_t tbytes = (size_t)a.groups * a.k * a.k * sizeof(float);
+  if (a.k % 4 == 0 && a.ns <= 256 && tbytes <= 48 * 1024) {
+    const int nt = (a.ns + 31) & ~31;
+    (*launches)++;
+    if (a.k <= 16) k_update_rows<16><<<a.ncols, nt, tbytes, st>>>(a);
+    else if (a.k <= 32) k_update_rows<32><<<a.ncols, nt, tbytes, st>>>(a);
+    else if (a.k <= 48) k_update_rows<48><<<a.ncols, nt, tbytes, st>>>(a);
+    else k_update_rows<64><<<a.ncols, nt, tbytes, st>>>(a);
+    return cudaGetLastError();
+  }
   const int kp = (a.k + 3) & ~3;
   const size_t xbytes = 2 * (size_t)a.ns * kp * sizeof(float);
   const size_t per = (size_t)a.k * kp * sizeof(float);

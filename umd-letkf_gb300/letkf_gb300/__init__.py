@@ -90,7 +90,8 @@ EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error",
            "lgpu_get_state", "lgpu_get_diag", "lgpu_get_timings", "lgpu_solver_final", "lgpu_get_obslist",
            "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2",
            "lgpu_get_obslist_noalloc", "lgpu_set_obs_raw", "lgpu_set_state_members", "lgpu_get_background",
-           "lgpu_get_obs_prepared", "lgpu_debug_transform", "lgpu_bind_state"]
+           "lgpu_get_obs_prepared", "lgpu_debug_transform", "lgpu_bind_state",
+           "lgpu_debug_weight"]
 
 _lib = None
 
@@ -125,6 +126,7 @@ def lib(path=None):
     L.lgpu_get_obslist.argtypes = [H, ctypes.c_int, ctypes.c_int, IP, FP, ctypes.c_int, IP, IP]
     L.lgpu_debug_metric.argtypes = [H, ctypes.c_int, FP, FP, FP, FP, FP]
     L.lgpu_debug_gc.argtypes = [H, ctypes.c_int, FP, FP, FP]
+    L.lgpu_debug_weight.argtypes = [H, ctypes.c_int, FP, FP, FP, FP, FP, FP]
     L.lgpu_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
     L.lgpu_host_free.argtypes = [ctypes.c_void_p]
     L.lgpu_flush_l2.argtypes = [H, ctypes.c_size_t]
@@ -479,6 +481,14 @@ class Solver:
         out = np.zeros((nunits, k, k), np.float32)
         self._ck(self.L.lgpu_debug_transform(self.h, nunits, k, _fp(g), _fp(out)))
         return out
+
+    def debug_weight(self, lat1, lon1, lat2, lon2, L):
+        """Batched-path fast weights: (exact dist, fast dist, exact GC, fast GC)."""
+        a = [_f32(x) for x in (lat1, lon1, lat2, lon2, L)]
+        n = len(a[0])
+        out = np.zeros(4 * n, np.float32)
+        self._ck(self.L.lgpu_debug_weight(self.h, n, *[_fp(x) for x in a], _fp(out)))
+        return out[:n], out[n:2 * n], out[2 * n:3 * n], out[3 * n:]
 
     def debug_gc(self, z, L):
         z, L = _f32(z), _f32(L)
