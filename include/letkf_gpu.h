@@ -258,9 +258,10 @@ int lgpu_debug_metric(lgpu_handle *h, int n, const float *lat1, const float *lon
                       const float *lat2, const float *lon2, float *dist);
 int lgpu_debug_gc(lgpu_handle *h, int n, const float *z, const float *L, float *gc);
 /* Verification of the batched Gram's fast weight path: for point pairs
- * (lat1, lon1)-(lat2, lon2) and horizontal scales L, out receives 4n floats:
+ * (lat1, lon1)-(lat2, lon2) and horizontal scales L, out receives 5n floats:
  * the exact distance, the fast distance, letkf_loc_gc of the exact distance
- * (REAL(8), rounded to REAL) and the fast weight of the fast distance. */
+ * (REAL(8), rounded to REAL), the fast weight of the fast distance, and the
+ * fast distance with the short asin series (valid for half-chords <= 0.25). */
 int lgpu_debug_weight(lgpu_handle *h, int n, const float *lat1, const float *lon1, const float *lat2,
                       const float *lon2, const float *L, float *out);
 

@@ -78,9 +78,13 @@ def test_fast_weight_path_bounds(solver):
     dlat = np.degrees(dist / 6371e3) * np.cos(brg)
     lat2 = np.clip(lat1 + dlat, -89.9, 89.9)
     lon2 = (lon1 + np.degrees(dist / 6371e3) * np.sin(brg) / np.cos(np.radians(lat1))) % 360.0
-    de, df, re, rf = solver.debug_weight(lat1, lon1, lat2, lon2, L)
+    de, df, re, rf, ds = solver.debug_weight(lat1, lon1, lat2, lon2, L)
     ok = de > 1.0
     assert np.max(np.abs(df[ok].astype(np.float64) / de[ok] - 1.0)) <= 1e-6
+    # short asin series: half-chords up to 0.25 (separations up to ~3,220 km)
+    sh = ok & (de < 2 * 6371e3 * np.arcsin(0.25))
+    assert sh.sum() > 100000
+    assert np.max(np.abs(ds[sh].astype(np.float64) / de[sh] - 1.0)) <= 1e-6
     near = (re > 2e-5) & (re < 5e-4)
     assert near.sum() > 10000
     assert np.max(np.abs(rf[near].astype(np.float64) - re[near])) <= 2e-8

@@ -744,6 +744,7 @@ int lgpu_solver_run(lgpu_handle *h) {
     ta.col2act = h->buf[B_COL2ACT].as<int>();
     ta.cp = h->buf[B_CP].as<ColPar>();
     ta.loc = h->loc;
+    ta.tp = h->buf[B_TILEPAR].as<TilePar>();
     ta.rec = h->buf[B_TILEREC].as<unsigned char>();
     ta.tile_off = h->buf[B_TILEOFF].as<int>();
     ta.tile_n = h->buf[B_TILEN].as<int>();
@@ -1070,14 +1071,14 @@ int lgpu_debug_weight(lgpu_handle *h, int n, const float *lat1, const float *lon
   if (n == 0) return LGPU_OK;
   CK(cudaSetDevice(h->device), "cudaSetDevice");
   float *d = nullptr;
-  CK(cudaMalloc(&d, 9 * sizeof(float) * (size_t)n), "alloc");
+  CK(cudaMalloc(&d, 10 * sizeof(float) * (size_t)n), "alloc");
   const float *src[5] = {lat1, lon1, lat2, lon2, L};
   cudaError_t e = cudaSuccess;
   for (int q = 0; q < 5 && e == cudaSuccess; q++)
     e = cudaMemcpyAsync(d + q * (size_t)n, src[q], 4 * (size_t)n, cudaMemcpyHostToDevice, h->st);
   if (e == cudaSuccess) e = launch_debug_weight(h->st, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n,
                                                 d + 4 * (size_t)n, d + 5 * (size_t)n);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + 5 * (size_t)n, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + 5 * (size_t)n, 20 * (size_t)n, cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_fail(h, e, "debug_weight");

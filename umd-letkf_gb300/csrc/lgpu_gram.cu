@@ -394,6 +394,7 @@ __global__ void k_debug_weight(int n, const float *lat1, const float *lon1, cons
   out[n + i] = df;
   out[2 * n + i] = gc_exact(de, L[i]);
   out[3 * n + i] = gc_branchless(df * inv_c_of(L[i]));
+  out[4 * n + i] = dist_fast(chord2_fast(a.x, a.y, a.z, b.x, b.y, b.z), true);
 }
 
 }  // namespace

@@ -17,7 +17,7 @@
 // Candidate streams.  Before the GEMM, three small kernels turn each tile's
 // search window (latitude bands x longitude range of its cap) into a record
 // stream: every observation inside the tile's cap, in window order, packed
-// per chunk of 16 as [16 x (ux,uy,uz,err)] [16 x (dep,time,zdim,surf)]
+// per chunk of 16 as [16 x (ux,uy,uz,1/err)] [16 x (dep,time,zdim,surf)]
 // [member-major y: (k+1 rounded to 4) rows x 16] -- one contiguous block per
 // chunk, read once per (group, pass) CTA with one bulk async copy.
 //
@@ -278,7 +278,9 @@ __global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps
     }
     const int q = base + before + __popc(m & ((1u << lane) - 1u));
     if (ok) {
-      if (q < cap) put_record(rec0, cb, k, kp, kr, q, A, obs.B[p], obs.hx + (size_t)p * kp);
+      if (q < cap)
+        put_record(rec0, cb, k, kp, kr, q, make_float4(A.x, A.y, A.z, __frcp_rn(A.w)), obs.B[p],
+                   obs.hx + (size_t)p * kp);
       else atomicOr(status, 16);
     }
     base += cnt;
@@ -389,6 +391,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
     }
     const float rlo = cp.rmax * (1.0f - kFastDistBand), rhi = cp.rmax * (1.0f + kFastDistBand);
+    const bool short_asin = a.tp[tile].hmax <= 0.25f;   // CTA-uniform
     LocK lk;
     lk.icv = LOC == LOC_VTGC ? inv_c_of(a.loc.vloc) : 1.0f;
     lk.levg = LOC == LOC_VTGC ? a.loc.lev_depth[g] : 0.0f;
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         const float c2f = chord2_fast(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
         const bool cand = (ch * KC + e < ntile) && (c2f <= c2max);
         const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
-        const float d = 12742000.0f * asin_fast(fminf(hf, 0.5f));
+        const float d = 12742000.0f * asin_fast(fminf(hf, 0.5f), short_asin);
         const float rl = loc_fast<LOC>(lk, cp, g, d, B);
         const bool in = cand && d <= cp.rmax;
         const bool uns = cand && (hf > 0.5f || (d >= rlo && d <= rhi) || (in && fabsf(rl - kKeep) <= kGuardFast));
@@ -460,7 +463,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
             nkeep++;
             rsum += rl;
             anyk = true;
-            wv = rl * __frcp_rn(RA[wq * 4 + u].w);
+            wv = rl * RA[wq * 4 + u].w;   // the record holds 1/err
           }
           tc::split_tf32(wv, h4[u], l4[u]);
         }
@@ -626,6 +629,16 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
     amax = fmax(amax, ang);
   }
   for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  // largest half-chord sqrt(c2max)/2 of a candidate pair (the weight producers' c2max)
+  float hm = 0.0f;
+  for (int c = lane; c < TM; c += 32) {
+    const int col = tile_cols[(size_t)tile * TM + c];
+    if (col < 0) continue;
+    const float hq = fminf(cp[col].rmax / 12742000.0f, 1.5707963f);
+    const float sh = sinf(hq);
+    hm = fmaxf(hm, sqrtf(4.0f * sh * sh * 1.0001f + 1e-12f) * 0.5f);
+  }
+  for (int o = 16; o > 0; o >>= 1) hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
   if (lane == 0) {
     TilePar t;
     const double lat = asin(fmax(-1.0, fmin(1.0, cz))) * 57.29577951308232;
@@ -647,6 +660,7 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
     t.cz = (float)cz;
     const double ch = 2.0 * sin(0.5 * fmin(alpha, 3.14159265358979));
     t.c2cap = (float)(ch * ch * 1.00001 + 1e-9);
+    t.hmax = hm * 1.0001f;
     t.b0 = band_of((float)(lat - adeg));
     t.b1 = band_of((float)(lat + adeg));
     tp[tile] = t;

@@ -203,15 +203,21 @@ __device__ __forceinline__ float chord2_fast(float ax, float ay, float az, float
   return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
 }
 
-// asin(x), 0 <= x <= 0.5: Taylor series of asin to x^21 in Horner form with
-// fused multiply-adds (a few ulp)
-__device__ __forceinline__ float asin_fast(float x) {
+// asin(x), 0 <= x <= 0.5: Taylor series of asin in Horner form with fused
+// multiply-adds (a few ulp).  x <= 0.25: terms to x^13 (truncation below
+// 2e-11 relative); otherwise to x^21.
+__device__ __forceinline__ float asin_fast(float x, bool short_series = false) {
   const float x2 = x * x;
-  float p = 0.008390335366129875f;
-  p = __fmaf_rn(p, x2, 0.009761609137058258f);
-  p = __fmaf_rn(p, x2, 0.01155180111527443f);
-  p = __fmaf_rn(p, x2, 0.013964843936264515f);
-  p = __fmaf_rn(p, x2, 0.017352763563394547f);
+  float p;
+  if (short_series) {
+    p = 0.017352763563394547f;
+  } else {
+    p = 0.008390335366129875f;
+    p = __fmaf_rn(p, x2, 0.009761609137058258f);
+    p = __fmaf_rn(p, x2, 0.01155180111527443f);
+    p = __fmaf_rn(p, x2, 0.013964843936264515f);
+    p = __fmaf_rn(p, x2, 0.017352763563394547f);
+  }
   p = __fmaf_rn(p, x2, 0.022372158244252205f);
   p = __fmaf_rn(p, x2, 0.0303819440305233f);
   p = __fmaf_rn(p, x2, 0.0446428582072258f);
@@ -241,10 +247,11 @@ __device__ __forceinline__ float gc_branchless(float zc) {
   return zc >= 2.0f ? 0.0f : (zc > 1.0f ? qo : pi);
 }
 
-// great-circle distance (m) from the squared chord, fast path (chord <= 1)
-__device__ __forceinline__ float dist_fast(float c2f) {
+// great-circle distance (m) from the squared chord, fast path (chord <= 1;
+// short_series for half-chords up to 0.25)
+__device__ __forceinline__ float dist_fast(float c2f, bool short_series = false) {
   const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
-  return 12742000.0f * asin_fast(fminf(hf, 0.5f));
+  return 12742000.0f * asin_fast(fminf(hf, 0.5f), short_series);
 }
 
 // Packed Gram layout of one unit: the upper triangle of G (i <= j, row-major)
@@ -378,6 +385,7 @@ struct TilePar {
   int b0, b1;        // latitude band range
   float cx, cy, cz;  // cap centre (unit vector)
   float c2cap;       // squared chord of the cap radius, with margin
+  float hmax;        // largest half-chord of a candidate pair of the tile
 };
 struct TcArgs {
   int ntiles, groups, k, kp, npass, np, nf, ncol;
@@ -385,6 +393,7 @@ struct TcArgs {
   const int *col2act;
   const ColPar *cp;
   DevLoc loc;
+  const TilePar *tp;         // per-tile cap parameters
   const unsigned char *rec;  // tile candidate streams (chunk records)
   const int *tile_off;       // [ntiles + 1] first chunk of each tile's stream
   const int *tile_n;         // [ntiles] candidates of each tile

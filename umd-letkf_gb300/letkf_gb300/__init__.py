@@ -483,12 +483,13 @@ class Solver:
         return out
 
     def debug_weight(self, lat1, lon1, lat2, lon2, L):
-        """Batched-path fast weights: (exact dist, fast dist, exact GC, fast GC)."""
+        """Batched-path fast weights: (exact dist, fast dist, exact GC, fast GC,
+        fast dist with the short asin series)."""
         a = [_f32(x) for x in (lat1, lon1, lat2, lon2, L)]
         n = len(a[0])
-        out = np.zeros(4 * n, np.float32)
+        out = np.zeros(5 * n, np.float32)
         self._ck(self.L.lgpu_debug_weight(self.h, n, *[_fp(x) for x in a], _fp(out)))
-        return out[:n], out[n:2 * n], out[2 * n:3 * n], out[3 * n:]
+        return tuple(out[q * n:(q + 1) * n] for q in range(5))
 
     def debug_gc(self, z, L):
         z, L = _f32(z), _f32(L)
