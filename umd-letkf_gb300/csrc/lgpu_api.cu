@@ -58,7 +58,7 @@ enum {
   B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID, B_HX, B_HXM, B_SATOBS, B_SATPLATS,
   B_GEOM, B_CELL, B_COUNT, B_FILL, B_POSTMP, B_ORDER, B_ATMP, B_BTMP, B_SA, B_SB, B_SHX, B_SIDX, B_CSTART,
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
-  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC,
+  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC, B_EIGSCR,
   B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7, B_RAWQC, B_RAWHX, B_RAWHXM, B_FLAG, B_POS,
   B_PTRS, B_TOTAL,
   B_COUNT_ALL
@@ -783,7 +783,30 @@ int lgpu_solver_run(lgpu_handle *h) {
   ea.nkept = h->buf[B_NKEPT].as<int>();
   ea.T = h->buf[B_T].as<float>();
   ea.status = h->buf[B_STATUS].as<int>();
-  CK(launch_eig(st, ea, &launches), "eigen kernel");
+  {
+    // split pipeline (scratch of at most 8 GB, units in batches); the fused
+    // one-warp kernel if the scratch cannot be had
+    const size_t per = eig_split_bytes_per_unit(k);
+    const size_t budget = (size_t)8 << 30;
+    int batch = (int)std::min<size_t>((size_t)std::max(1, h->nunits), std::max<size_t>(1024, budget / per));
+    const size_t need = per * (size_t)batch + 5 * 256;
+    if (h->buf[B_EIGSCR].cap >= need || h->buf[B_EIGSCR].ensure(need) == cudaSuccess) {
+      unsigned char *base = h->buf[B_EIGSCR].as<unsigned char>();
+      size_t off = 0;
+      auto take = [&](size_t bytes) { unsigned char *p = base + off; off += (bytes + 255) & ~(size_t)255; return p; };
+      EigSplit sp;
+      sp.Q = reinterpret_cast<float *>(take((size_t)batch * k * k * 4));
+      sp.DE = reinterpret_cast<float *>(take((size_t)batch * 2 * k * 4));
+      sp.log = reinterpret_cast<float2 *>(take((size_t)batch * eig_log_cap(k) * 8));
+      sp.logn = reinterpret_cast<int *>(take((size_t)batch * 4));
+      sp.lam = reinterpret_cast<float *>(take((size_t)batch * k * 4));
+      sp.cap = eig_log_cap(k);
+      CK(launch_eig_split(st, ea, sp, batch, &launches), "eigen kernels");
+    } else {
+      cudaGetLastError();   // clear the failed allocation
+      CK(launch_eig(st, ea, &launches), "eigen kernel");
+    }
+  }
   CK(cudaEventRecord(h->ev[4], st), "event");
   // ---- update + epilogue ----
   UpdateArgs ua;

@@ -31,22 +31,21 @@ __host__ __device__ __forceinline__ int eig_floats_per_warp(int k) {
   return k * ld + 8 * k + 8;
 }
 
-__global__ void k_eig(EigArgs a, int wpb) {
-  extern __shared__ __align__(16) float sm[];
+// Work arrays of one unit in shared memory: A (k x ld, ld = k + 1) holds A,
+// then Q, then V; then d, e, tau, bv, p, w, fl, gl (k each).
+struct EigWork {
+  float *A, *d, *e, *tau, *bv, *p, *w, *fl, *gl;
+  __device__ EigWork(float *base, int k) {
+    A = base;
+    d = A + k * (k + 1);
+    e = d + k; tau = e + k; bv = tau + k; p = bv + k; w = p + k; fl = w + k; gl = fl + k;
+  }
+};
+
+// A = G + (k-1)/infl I from the packed Gram block, b from its tail
+__device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork &W, int lane) {
   const int k = a.k, ld = k + 1;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int unit = blockIdx.x * wpb + warp;
-  if (unit >= a.nunits) return;           // whole warps exit; no block-level barriers below
-  if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
-  float *A = sm + (size_t)warp * eig_floats_per_warp(k);   // A, then Q, then V (one k x k matrix)
-  float *d = A + k * ld;
-  float *e = d + k;
-  float *tau = e + k;
-  float *bv = tau + k;
-  float *p = bv + k;
-  float *w = p + k;
-  float *fl = w + k;
-  float *gl = fl + k;
+  float *A = W.A, *bv = W.bv;
   const float *G = a.G + (size_t)unit * packed_size(k);
   // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
   const float shift = (float)(k - 1) * 1.0f / a.infl;
@@ -59,6 +58,13 @@ __global__ void k_eig(EigArgs a, int wpb) {
   for (int i = lane; i < k; i += 32) bv[i] = G[k * (k + 1) / 2 + i];
   __syncwarp();
 
+}
+
+// Householder tridiagonalisation (d, e, tau; reflector vectors in the
+// columns of A) and Q formed in place
+__device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
+  const int ld = k + 1;
+  float *A = W.A, *d = W.d, *e = W.e, *tau = W.tau, *p = W.p, *w = W.w;
   // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j];
   // its vector v_j = A[j+1:, j] stays in column j
   for (int j = 0; j < k - 2; j++) {
@@ -155,13 +161,69 @@ __global__ void k_eig(EigArgs a, int wpb) {
     __syncwarp();
   }
 
+}
+
+// spectral functions and T = U U^T + wbar 1^T (A holds V, d the eigenvalues)
+__device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWork &W, int lane, int &bad) {
+  const int k = a.k, ld = k + 1;
+  float *A = W.A, *d = W.d, *bv = W.bv, *p = W.p, *w = W.w, *fl = W.fl, *gl = W.gl;
+  // ---- spectral functions: f = sqrt((k-1)/lambda), g = 1/lambda
+  //      (src/letkf_core.F90:111-113, :128-131); fl holds sqrt(f)
+  for (int l = lane; l < k; l += 32) {
+    const float lam = d[l];
+    if (!(lam > 0.0f)) bad |= 2;
+    fl[l] = sqrtf(sqrtf((float)(k - 1) / lam));
+    gl[l] = 1.0f / lam;
+  }
+  __syncwarp();
+  // s_l = g_l * (V^T b)_l
+  for (int l = lane; l < k; l += 32) {
+    float acc = 0.0f;
+    for (int q = 0; q < k; q++) acc = __fmaf_rn(A[q * ld + l], bv[q], acc);
+    p[l] = gl[l] * acc;
+  }
+  __syncwarp();
+  // wbar_i = sum_l V[i][l] s_l
+  for (int i = lane; i < k; i += 32) {
+    float acc = 0.0f;
+    for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], p[l], acc);
+    w[i] = acc;
+  }
+  __syncwarp();
+  // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
+  for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] *= fl[l]; }
+  __syncwarp();
+  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; lane owns columns lane, lane + 32
+  float *T = a.T + (size_t)unit * k * k;
+  if (lane < k) {
+    const bool two = lane + 32 < k;
+    const int j0 = lane, j1 = two ? lane + 32 : lane;
+    const float *u0 = A + j0 * ld, *u1 = A + j1 * ld;
+    for (int i = 0; i < k; i++) {
+      const float *ur = A + i * ld;
+      float acc0 = 0.0f, acc1 = 0.0f;
+      for (int l = 0; l < k; l++) {
+        const float y = ur[l];
+        acc0 = __fmaf_rn(y, u0[l], acc0);
+        acc1 = __fmaf_rn(y, u1[l], acc1);
+      }
+      T[i * k + j0] = acc0 + w[i];
+      if (two) T[i * k + j1] = acc1 + w[i];
+    }
+  }
+}
+
+// implicit-shift QL on (d, e) with the rotations applied to the columns of
+// A (Q -> V), one warp
+__device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &bad) {
+  const int ld = k + 1;
+  float *A = W.A, *d = W.d, *e = W.e;
   // ---- implicit-shift QL on (d, e), rotations applied at once to the
   // columns (i, i+1) of Q (V = Q Z).  The scalar recurrence is evaluated
   // redundantly by every lane: d[i+1] is carried in a register and only e[i],
   // d[i] (not yet written in this sweep) are read, so lane 0 alone writes
   // results, without barriers inside the sweep.  Each lane owns rows lane and
   // lane + 32 of Q and carries the pending column i+1 of its rows.
-  int bad = 0;
   {
     const bool two = lane + 32 < k;
     const bool own = lane < k;
@@ -229,50 +291,189 @@ __global__ void k_eig(EigArgs a, int wpb) {
   }
   __syncwarp();
 
-  // ---- spectral functions: f = sqrt((k-1)/lambda), g = 1/lambda
-  //      (src/letkf_core.F90:111-113, :128-131); fl holds sqrt(f)
-  for (int l = lane; l < k; l += 32) {
-    const float lam = d[l];
-    if (!(lam > 0.0f)) bad |= 2;
-    fl[l] = sqrtf(sqrtf((float)(k - 1) / lam));
-    gl[l] = 1.0f / lam;
-  }
-  __syncwarp();
-  // s_l = g_l * (V^T b)_l
-  for (int l = lane; l < k; l += 32) {
-    float acc = 0.0f;
-    for (int q = 0; q < k; q++) acc = __fmaf_rn(A[q * ld + l], bv[q], acc);
-    p[l] = gl[l] * acc;
-  }
-  __syncwarp();
-  // wbar_i = sum_l V[i][l] s_l
-  for (int i = lane; i < k; i += 32) {
-    float acc = 0.0f;
-    for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], p[l], acc);
-    w[i] = acc;
-  }
-  __syncwarp();
-  // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
-  for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] *= fl[l]; }
-  __syncwarp();
-  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; lane owns columns lane, lane + 32
-  float *T = a.T + (size_t)unit * k * k;
-  if (lane < k) {
-    const bool two = lane + 32 < k;
-    const int j0 = lane, j1 = two ? lane + 32 : lane;
-    const float *u0 = A + j0 * ld, *u1 = A + j1 * ld;
-    for (int i = 0; i < k; i++) {
-      const float *ur = A + i * ld;
-      float acc0 = 0.0f, acc1 = 0.0f;
-      for (int l = 0; l < k; l++) {
-        const float y = ur[l];
-        acc0 = __fmaf_rn(y, u0[l], acc0);
-        acc1 = __fmaf_rn(y, u1[l], acc1);
+}
+
+__global__ void k_eig(EigArgs a, int wpb) {
+  extern __shared__ __align__(16) float sm[];
+  const int k = a.k, ld = k + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int unit = blockIdx.x * wpb + warp;
+  if (unit >= a.nunits) return;           // whole warps exit; no block-level barriers below
+  if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
+  EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
+  eig_load(a, unit, W, lane);
+  eig_tridiag_q(k, W, lane);
+  int bad = 0;
+  eig_ql_warp(k, W, lane, bad);
+  eig_transform(a, unit, W, lane, bad);
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  if (bad && lane == 0) atomicOr(a.status, bad);
+}
+
+// ---------------------------------------------------------------------------
+// Split pipeline (same arithmetic as k_eig, bit-identical results):
+//   k_eig_tri  warp per unit: Householder + Q (to global), d and e
+//   k_eig_ql   thread per unit: the QL recurrence on (d, e) alone, logging
+//              every sweep (start index, rotation count) and rotation (c, s)
+//   k_eig_vec  warp per unit: the logged rotations applied to Q's columns
+//              (V = Q Z), then the spectral functions and T
+// The scalar recurrence, which the fused kernel evaluates redundantly on all
+// 32 lanes, runs once per unit.
+
+__global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
+  extern __shared__ __align__(16) float sm[];
+  const int k = a.k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ub = blockIdx.x * wpb + warp;
+  if (ub >= nb) return;
+  const int unit = u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
+  eig_load(a, unit, W, lane);
+  eig_tridiag_q(k, W, lane);
+  const int ld = k + 1;
+  float *Q = sp.Q + (size_t)ub * k * k;
+  for (int t = lane; t < k * k; t += 32) Q[t] = W.A[(t / k) * ld + (t % k)];
+  float *de = sp.DE + (size_t)ub * 2 * k;
+  for (int t = lane; t < k; t += 32) { de[t] = W.d[t]; de[k + t] = W.e[t]; }
+}
+
+constexpr int QLT = 64;   // threads (units) per block of k_eig_ql
+
+__global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, int nb) {
+  extern __shared__ __align__(16) float qs[];   // d[k][QLT], e[k][QLT]
+  const int k = a.k, t = threadIdx.x;
+  const int ub = blockIdx.x * QLT + t;
+  float *d = qs + t, *e = qs + (size_t)k * QLT + t;   // element i at [i * QLT]
+#define D(i) d[(size_t)(i) * QLT]
+#define E(i) e[(size_t)(i) * QLT]
+  if (ub >= nb) return;
+  const int unit = u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  const float *de = sp.DE + (size_t)ub * 2 * k;
+  for (int i = 0; i < k; i++) { D(i) = de[i]; E(i) = de[k + i]; }
+  float2 *lg = sp.log + (size_t)ub * sp.cap;
+  int pos = 0, bad = 0;
+  for (int l = 0; l < k; l++) {
+    int iter = 0;
+    for (;;) {
+      int m = l;
+      while (m < k - 1 && !(fabsf(E(m)) <= 1.1920929e-7f * (fabsf(D(m)) + fabsf(D(m + 1))))) m++;
+      if (m == l) break;
+      if (++iter > 60) { bad |= 1; break; }
+      const float dl = D(l), el = E(l);
+      float g = (D(l + 1) - dl) / (2.0f * el);
+      float r = sqrtf(g * g + 1.0f);
+      g = D(m) - dl + el / (g + copysignf(r, g));
+      float s = 1.0f, c = 1.0f, pp = 0.0f;
+      float di1 = D(m);
+      const int hdr = pos++;
+      int cnt = 0;
+      bool deflate = false;
+      for (int i = m - 1; i >= l; i--) {
+        const float ei = E(i), di = D(i);
+        const float f = s * ei, b = c * ei;
+        r = sqrtf(f * f + g * g);
+        E(i + 1) = r;
+        if (r == 0.0f) {
+          D(i + 1) = di1 - pp;
+          E(m) = 0.0f;
+          deflate = true;
+          break;
+        }
+        const float ir = __frcp_rn(r);
+        s = f * ir;
+        c = g * ir;
+        g = di1 - pp;
+        const float rr = (di - g) * s + 2.0f * c * b;
+        pp = s * rr;
+        D(i + 1) = g + pp;
+        g = c * rr - b;
+        di1 = di;
+        if (pos < sp.cap) lg[pos] = make_float2(c, s);
+        pos++;
+        cnt++;
       }
-      T[i * k + j0] = acc0 + w[i];
-      if (two) T[i * k + j1] = acc1 + w[i];
+      if (hdr < sp.cap) lg[hdr] = make_float2(__int_as_float(m), __int_as_float(cnt));
+      if (!deflate) { D(l) = D(l) - pp; E(l) = g; E(m) = 0.0f; }
+    }
+    if (bad) break;
+  }
+#undef D
+#undef E
+  // -1: no convergence (status bit 1); -2: log overflow (k_eig_vec reruns the QL)
+  sp.logn[ub] = bad ? -1 : (pos > sp.cap ? -2 : pos);
+  float *lam = sp.lam + (size_t)ub * k;
+  for (int i = 0; i < k; i++) lam[i] = d[(size_t)i * QLT];
+  if (bad) atomicOr(a.status, bad);
+}
+
+__global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
+  extern __shared__ __align__(16) float sm[];
+  const int k = a.k, ld = k + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ub = blockIdx.x * wpb + warp;
+  if (ub >= nb) return;
+  const int unit = u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  const int total = sp.logn[ub];
+  if (total == -1) return;                // no convergence: status set by k_eig_ql
+  EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
+  float *A = W.A;
+  const float *Q = sp.Q + (size_t)ub * k * k;
+  for (int t = lane; t < k * k; t += 32) A[(t / k) * ld + (t % k)] = Q[t];
+  const float *lam = sp.lam + (size_t)ub * k;
+  for (int t = lane; t < k; t += 32) W.d[t] = lam[t];
+  const float *G = a.G + (size_t)unit * packed_size(k);
+  for (int i = lane; i < k; i += 32) W.bv[i] = G[k * (k + 1) / 2 + i];
+  __syncwarp();
+  int bad = 0;
+  if (total < 0) {
+    // the rotation log overflowed: run the QL here from the tridiagonal form
+    const float *de = sp.DE + (size_t)ub * 2 * k;
+    for (int t = lane; t < k; t += 32) { W.d[t] = de[t]; W.e[t] = de[k + t]; }
+    __syncwarp();
+    eig_ql_warp(k, W, lane, bad);
+  } else {
+    // replay the rotations on the lane's rows (lane, lane + 32); the log is
+    // read 32 entries at a time (lane j holds entry base + j) and broadcast
+    const float2 *lg = sp.log + (size_t)ub * sp.cap;
+    const bool two = lane + 32 < k, own = lane < k;
+    float *q0 = A + (own ? lane : 0) * ld, *q1 = A + (two ? lane + 32 : 0) * ld;
+    int base = 0;
+    float2 cur = lane < total ? lg[lane] : make_float2(0.f, 0.f);
+    float2 nxt = lane + 32 < total ? lg[32 + lane] : make_float2(0.f, 0.f);
+    auto get = [&](int idx) -> float2 {
+      if (idx >= base + 32) {   // warp-uniform
+        base += 32;
+        cur = nxt;
+        nxt = base + 32 + lane < total ? lg[base + 32 + lane] : make_float2(0.f, 0.f);
+      }
+      float2 v;
+      v.x = __shfl_sync(0xffffffffu, cur.x, idx - base);
+      v.y = __shfl_sync(0xffffffffu, cur.y, idx - base);
+      return v;
+    };
+    int pidx = 0;
+    while (pidx < total) {
+      const float2 h = get(pidx++);
+      const int m = __float_as_int(h.x), cnt = __float_as_int(h.y);
+      if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + cnt > total) { bad |= 1; break; }   // malformed log
+      float z0 = own ? q0[m] : 0.0f, z1 = two ? q1[m] : 0.0f;
+      for (int r = 0; r < cnt; r++) {
+        const float2 cs = get(pidx++);
+        const float c = cs.x, s = cs.y;
+        const int i = m - 1 - r;
+        const float a0 = own ? q0[i] : 0.0f, a1 = two ? q1[i] : 0.0f;
+        if (own) { q0[i + 1] = s * a0 + c * z0; z0 = c * a0 - s * z0; }
+        if (two) { q1[i + 1] = s * a1 + c * z1; z1 = c * a1 - s * z1; }
+      }
+      if (own) q0[m - cnt] = z0;
+      if (two) q1[m - cnt] = z1;
     }
   }
+  __syncwarp();
+  eig_transform(a, unit, W, lane, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);
   if (bad && lane == 0) atomicOr(a.status, bad);
 }
@@ -280,6 +481,51 @@ __global__ void k_eig(EigArgs a, int wpb) {
 }  // namespace
 
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
+
+static int eig_wpb(int k) {
+  // warps per block: the most resident warps per SM for this unit size
+  const size_t per = (size_t)eig_floats_per_warp(k) * sizeof(float);
+  const size_t sm_bytes = 227 * 1024;
+  int wpb = 1, best = 0;
+  for (int c = 1; c <= 8; c++) {
+    if ((size_t)c * per > sm_bytes) break;
+    int blocks = (int)(sm_bytes / ((size_t)c * per + 1024));   // 1 KB reserved per block
+    if (blocks > 32) blocks = 32;
+    int warps = blocks * c;
+    if (warps > 64) warps = 64;
+    if (warps > best) { best = warps; wpb = c; }
+  }
+  return wpb;
+}
+
+int eig_log_cap(int k) { return 2 * k * k + 4 * k + 64; }
+
+size_t eig_split_bytes_per_unit(int k) {
+  return (size_t)k * k * 4 + (size_t)2 * k * 4 + (size_t)eig_log_cap(k) * 8 + 4 + (size_t)k * 4;
+}
+
+cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int *launches) {
+  if (a.nunits <= 0) return cudaSuccess;
+  const int wpb = eig_wpb(a.k);
+  const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_eig_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_eig_vec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+    return e;
+  const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
+  if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
+    return e;
+  for (int u0 = 0; u0 < a.nunits; u0 += batch) {
+    const int nb = a.nunits - u0 < batch ? a.nunits - u0 : batch;
+    k_eig_tri<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
+    k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
+    k_eig_vec<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
+    (*launches) += 3;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
                              int *status) {
@@ -291,24 +537,32 @@ cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G,
   a.nkept = nkept;
   a.T = T;
   a.status = status;
+  // the split pipeline, as lgpu_solver_run uses it
+  const size_t per = eig_split_bytes_per_unit(k);
+  unsigned char *buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, per * (size_t)(nunits > 0 ? nunits : 1) + 256);
+  if (e != cudaSuccess) return e;
+  EigSplit sp;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { unsigned char *p = buf + off; off += (bytes + 255) & ~(size_t)255; return p; };
+  const size_t n = nunits > 0 ? nunits : 1;
+  sp.Q = reinterpret_cast<float *>(take(n * k * k * 4));
+  sp.DE = reinterpret_cast<float *>(take(n * 2 * k * 4));
+  sp.log = reinterpret_cast<float2 *>(take(n * (size_t)eig_log_cap(k) * 8));
+  sp.logn = reinterpret_cast<int *>(take(n * 4));
+  sp.lam = reinterpret_cast<float *>(take(n * k * 4));
+  sp.cap = eig_log_cap(k);
   int l = 0;
-  return launch_eig(st, a, &l);
+  e = launch_eig_split(st, a, sp, nunits, &l);
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaFree(buf);
+  return e != cudaSuccess ? e : e2;
 }
 
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches) {
   if (a.nunits <= 0) return cudaSuccess;
-  // warps per block: the most resident warps per SM for this unit size
+  const int wpb = eig_wpb(a.k);
   const size_t per = (size_t)eig_floats_per_warp(a.k) * sizeof(float);
-  const size_t sm_bytes = 227 * 1024;
-  int wpb = 1, best = 0;
-  for (int c = 1; c <= 8; c++) {
-    if ((size_t)c * per > sm_bytes) break;
-    int blocks = (int)(sm_bytes / ((size_t)c * per + 1024));   // 1 KB reserved per block
-    if (blocks > 32) blocks = 32;
-    int warps = blocks * c;
-    if (warps > 64) warps = 64;
-    if (warps > best) { best = warps; wpb = c; }
-  }
   const size_t smem = (size_t)wpb * per;
   cudaError_t e = cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -426,6 +426,18 @@ struct EigArgs {
   int *status;            // [1] accumulated error bits
 };
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
+// scratch of the split eigensolve pipeline, for `batch` units
+struct EigSplit {
+  float *Q;        // [batch][k][k] Householder Q, row-major
+  float *DE;       // [batch][2k] diagonal, off-diagonal
+  float2 *log;     // [batch][cap] sweep headers (start, count) and rotations (c, s)
+  int *logn;       // [batch] log entries, -1 no convergence, -2 overflow
+  float *lam;      // [batch][k] eigenvalues
+  int cap;
+};
+int eig_log_cap(int k);
+size_t eig_split_bytes_per_unit(int k);
+cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int *launches);
 
 struct UpdateArgs {
   int ncol, ns, k, groups;
