@@ -66,7 +66,7 @@ enum {
 
 }  // namespace
 
-constexpr int kOutChunks = 16;   // column chunks of the update / analysis download of a bound state
+constexpr int kOutChunks = 8;   // column chunks of eigensolve / update / analysis download of a bound state
 
 struct lgpu_handle {
   int device = 0;
@@ -74,7 +74,7 @@ struct lgpu_handle {
   cudaStream_t cst = nullptr;      // host<->device copies of a bound state
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev_in[2] = {};       // bound state: mean/spread, members uploaded
-  cudaEvent_t ev_out[kOutChunks] = {};
+  cudaEvent_t ev_chunk[kOutChunks][3] = {};   // per column chunk: eigensolve start, update start, update end
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
   std::string err;
   bool solver_ok = false, loc_ok = false, grid_ok = false, state_ok = false, obs_ok = false, ran = false;
@@ -223,8 +223,9 @@ int lgpu_create(int device, lgpu_handle **out) {
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_in)
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
-  for (auto &ev : h->ev_out)
-    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &row : h->ev_chunk)
+    for (auto &ev : row)
+      if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   build_geom(h->geom, h->ncell);
   if (h->buf[B_GEOM].ensure(sizeof(IndexGeom)) != cudaSuccess ||
       cudaMemcpy(h->buf[B_GEOM].p, &h->geom, sizeof(IndexGeom), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -243,7 +244,8 @@ void lgpu_destroy(lgpu_handle *h) {
   for (auto &b : h->buf) b.release();
   for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_in) if (ev) cudaEventDestroy(ev);
-  for (auto &ev : h->ev_out) if (ev) cudaEventDestroy(ev);
+  for (auto &row : h->ev_chunk)
+    for (auto &ev : row) if (ev) cudaEventDestroy(ev);
   if (h->st) cudaStreamDestroy(h->st);
   if (h->cst) cudaStreamDestroy(h->cst);
   delete h;
@@ -774,7 +776,10 @@ int lgpu_solver_run(lgpu_handle *h) {
   ga.ncol = h->ncol;
   if (!use_tc) CK(launch_gram(st, ga, &launches), "gram kernel");
   CK(cudaEventRecord(h->ev[3], st), "event");
-  // ---- eigensolve + transform ----
+  // ---- eigensolve + transform, update + epilogue, in column chunks ----
+  // A bound state is processed in kOutChunks column chunks: chunk c's
+  // analysis is downloaded into the caller's arrays while the eigensolve and
+  // update of the following chunks run.
   EigArgs ea;
   ea.nunits = h->nunits;
   ea.k = k;
@@ -783,32 +788,6 @@ int lgpu_solver_run(lgpu_handle *h) {
   ea.nkept = h->buf[B_NKEPT].as<int>();
   ea.T = h->buf[B_T].as<float>();
   ea.status = h->buf[B_STATUS].as<int>();
-  {
-    // split pipeline (scratch of at most 8 GB, units in batches); the fused
-    // one-warp kernel if the scratch cannot be had
-    const size_t per = eig_split_bytes_per_unit(k);
-    const size_t budget = (size_t)8 << 30;
-    int batch = (int)std::min<size_t>((size_t)std::max(1, h->nunits), std::max<size_t>(1024, budget / per));
-    const size_t need = per * (size_t)batch + 5 * 256;
-    if (h->buf[B_EIGSCR].cap >= need || h->buf[B_EIGSCR].ensure(need) == cudaSuccess) {
-      unsigned char *base = h->buf[B_EIGSCR].as<unsigned char>();
-      size_t off = 0;
-      auto take = [&](size_t bytes) { unsigned char *p = base + off; off += (bytes + 255) & ~(size_t)255; return p; };
-      EigSplit sp;
-      sp.Q = reinterpret_cast<float *>(take((size_t)batch * k * k * 4));
-      sp.DE = reinterpret_cast<float *>(take((size_t)batch * 2 * k * 4));
-      sp.log = reinterpret_cast<float2 *>(take((size_t)batch * eig_log_cap(k) * 8));
-      sp.logn = reinterpret_cast<int *>(take((size_t)batch * 4));
-      sp.lam = reinterpret_cast<float *>(take((size_t)batch * k * 4));
-      sp.cap = eig_log_cap(k);
-      CK(launch_eig_split(st, ea, sp, batch, &launches), "eigen kernels");
-    } else {
-      cudaGetLastError();   // clear the failed allocation
-      CK(launch_eig(st, ea, &launches), "eigen kernel");
-    }
-  }
-  CK(cudaEventRecord(h->ev[4], st), "event");
-  // ---- update + epilogue ----
   UpdateArgs ua;
   ua.ncol = h->ncol;
   ua.ns = ns;
@@ -836,24 +815,55 @@ int lgpu_solver_run(lgpu_handle *h) {
   ua.rtpp = h->scfg.rtpp;
   ua.mul = h->scfg.mul;
   ua.status = h->buf[B_STATUS].as<int>();
-  if (!bound) {
-    ua.col0 = 0;
-    ua.ncols = h->ncol;
+  // eigensolve scratch: the split pipeline (at most 8 GB, units in batches);
+  // the fused one-warp kernel over all units if the scratch cannot be had
+  EigSplit sp;
+  int batch = 0;
+  {
+    const size_t per = eig_split_bytes_per_unit(k);
+    const size_t budget = (size_t)8 << 30;
+    batch = (int)std::min<size_t>((size_t)std::max(1, h->nunits), std::max<size_t>(1024, budget / per));
+    const size_t need = per * (size_t)batch + 5 * 256;
+    if (h->buf[B_EIGSCR].cap >= need || h->buf[B_EIGSCR].ensure(need) == cudaSuccess) {
+      unsigned char *base = h->buf[B_EIGSCR].as<unsigned char>();
+      size_t off = 0;
+      auto take = [&](size_t bytes) { unsigned char *p = base + off; off += (bytes + 255) & ~(size_t)255; return p; };
+      sp.Q = reinterpret_cast<float *>(take((size_t)batch * k * k * 4));
+      sp.DE = reinterpret_cast<float *>(take((size_t)batch * 2 * k * 4));
+      sp.log = reinterpret_cast<float2 *>(take((size_t)batch * eig_log_cap(k) * 8));
+      sp.logn = reinterpret_cast<int *>(take((size_t)batch * 4));
+      sp.lam = reinterpret_cast<float *>(take((size_t)batch * k * 4));
+      sp.cap = eig_log_cap(k);
+    } else {
+      cudaGetLastError();   // clear the failed allocation
+      batch = 0;
+    }
+  }
+  if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
+  if (bound) CK(cudaStreamWaitEvent(st, h->ev_in[1], 0), "stream wait");
+  const int nch = bound ? kOutChunks : 1;
+  const int per = (h->ncol + nch - 1) / nch;
+  float eig_ms = 0.0f, upd_ms = 0.0f;
+  int nrec = 0;
+  for (int c = 0; c < nch; c++) {
+    const int c0 = c * per, c1 = std::min(h->ncol, (c + 1) * per);
+    if (c1 <= c0) break;
+    // units of the chunk's active columns
+    int a0 = -1, a1 = -1;
+    for (int j = c0; j < c1 && a0 < 0; j++) if (h->h_col2act[j] >= 0) a0 = h->h_col2act[j];
+    for (int j = c1 - 1; j >= c0 && a1 < 0; j--) if (h->h_col2act[j] >= 0) a1 = h->h_col2act[j] + 1;
+    CK(cudaEventRecord(h->ev_chunk[c][0], st), "event");
+    if (batch > 0 && a0 >= 0) CK(launch_eig_split(st, ea, sp, batch, a0 * G, (a1 - a0) * G, &launches), "eigen kernels");
+    CK(cudaEventRecord(h->ev_chunk[c][1], st), "event");
+    ua.col0 = c0;
+    ua.ncols = c1 - c0;
     CK(launch_update(st, ua, &launches), "update kernel");
-  } else {
-    // column chunks; each chunk's analysis is copied into the caller's
-    // arrays while the next chunks are updated
-    CK(cudaStreamWaitEvent(st, h->ev_in[1], 0), "stream wait");
-    const int per = (h->ncol + kOutChunks - 1) / kOutChunks;
-    for (int c = 0; c < kOutChunks; c++) {
-      ua.col0 = c * per;
-      ua.ncols = std::min(h->ncol, (c + 1) * per) - ua.col0;
-      if (ua.ncols <= 0) break;
-      CK(launch_update(st, ua, &launches), "update kernel");
-      CK(cudaEventRecord(h->ev_out[c], st), "event");
-      CK(cudaStreamWaitEvent(h->cst, h->ev_out[c], 0), "stream wait");
-      const size_t xo = (size_t)ua.col0 * ns * k, xn = (size_t)ua.ncols * ns * k;
-      const size_t mo = (size_t)ua.col0 * ns, mn = (size_t)ua.ncols * ns;
+    CK(cudaEventRecord(h->ev_chunk[c][2], st), "event");
+    nrec = c + 1;
+    if (bound) {
+      CK(cudaStreamWaitEvent(h->cst, h->ev_chunk[c][2], 0), "stream wait");
+      const size_t xo = (size_t)c0 * ns * k, xn = (size_t)(c1 - c0) * ns * k;
+      const size_t mo = (size_t)c0 * ns, mn = (size_t)(c1 - c0) * ns;
       CK(cudaMemcpyAsync(h->bound_state + xo, h->buf[B_ANA].as<float>() + xo, xn * 4, cudaMemcpyDeviceToHost, h->cst),
          "D2H state");
       CK(cudaMemcpyAsync(h->bound_mean + mo, h->buf[B_MEANA].as<float>() + mo, mn * 4, cudaMemcpyDeviceToHost, h->cst),
@@ -867,15 +877,22 @@ int lgpu_solver_run(lgpu_handle *h) {
   CK(cudaMemcpyAsync(&status, h->buf[B_STATUS].p, 4, cudaMemcpyDeviceToHost, st), "D2H status");
   CK(cudaStreamSynchronize(st), "solver_run");
   if (bound) CK(cudaStreamSynchronize(h->cst), "solver_run copies");
-  float ms[5];
-  for (int i = 0; i < 5; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
+  float ms[3];
+  for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
+  for (int c = 0; c < nrec; c++) {
+    float te = 0.0f, tu = 0.0f;
+    CK(cudaEventElapsedTime(&te, h->ev_chunk[c][0], h->ev_chunk[c][1]), "timing");
+    CK(cudaEventElapsedTime(&tu, h->ev_chunk[c][1], h->ev_chunk[c][2]), "timing");
+    eig_ms += te;
+    upd_ms += tu;
+  }
   h->tim.index_ms = ms[0];
   h->tim.prep_ms = ms[1];
   h->tim.gram_ms = ms[2];
   h->tim.tiles_ms = 0.0f;
   if (h->used_tc) CK(cudaEventElapsedTime(&h->tim.tiles_ms, h->ev[2], h->ev[6]), "timing");
-  h->tim.eig_ms = ms[3];
-  h->tim.update_ms = ms[4];
+  h->tim.eig_ms = eig_ms;
+  h->tim.update_ms = upd_ms;
   CK(cudaEventElapsedTime(&h->tim.total_ms, h->ev[0], h->ev[5]), "timing");
   h->tim.launches = launches;
   h->tim.variant = h->used_tc ? LGPU_VARIANT_BATCHED_TC : LGPU_VARIANT_PLAIN;

@@ -504,8 +504,9 @@ size_t eig_split_bytes_per_unit(int k) {
   return (size_t)k * k * 4 + (size_t)2 * k * 4 + (size_t)eig_log_cap(k) * 8 + 4 + (size_t)k * 4;
 }
 
-cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int *launches) {
-  if (a.nunits <= 0) return cudaSuccess;
+cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart, int ucount,
+                             int *launches) {
+  if (ucount <= 0) return cudaSuccess;
   const int wpb = eig_wpb(a.k);
   const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
   cudaError_t e;
@@ -516,8 +517,9 @@ cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &
   const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
   if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
     return e;
-  for (int u0 = 0; u0 < a.nunits; u0 += batch) {
-    const int nb = a.nunits - u0 < batch ? a.nunits - u0 : batch;
+  const int uend = ustart + ucount;
+  for (int u0 = ustart; u0 < uend; u0 += batch) {
+    const int nb = uend - u0 < batch ? uend - u0 : batch;
     k_eig_tri<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
     k_eig_vec<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
@@ -553,7 +555,7 @@ cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G,
   sp.lam = reinterpret_cast<float *>(take(n * k * 4));
   sp.cap = eig_log_cap(k);
   int l = 0;
-  e = launch_eig_split(st, a, sp, nunits, &l);
+  e = launch_eig_split(st, a, sp, nunits, 0, nunits, &l);
   cudaError_t e2 = cudaStreamSynchronize(st);
   cudaFree(buf);
   return e != cudaSuccess ? e : e2;

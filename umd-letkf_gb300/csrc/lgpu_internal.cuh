@@ -437,7 +437,9 @@ struct EigSplit {
 };
 int eig_log_cap(int k);
 size_t eig_split_bytes_per_unit(int k);
-cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int *launches);
+// units [ustart, ustart + ucount), in batches of at most `batch`
+cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart, int ucount,
+                             int *launches);
 
 struct UpdateArgs {
   int ncol, ns, k, groups;
