@@ -111,16 +111,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
 }
 
-// fp32 -> (hi, lo), both representable in tf32 and rounded to nearest:
-// hi = tf32(x), lo = tf32(x - hi).  x - hi is exact in fp32; rounding lo
-// (rather than letting the tensor core drop its low bits) keeps the split
-// unbiased, |x - hi - lo| <= 2^-22 |x|.
+// fp32 -> (hi, lo) for the three-term TF32 products: hi = tf32(x) rounded
+// to nearest, lo = x - hi (exact in fp32, |lo| <= 2^-11 |x|); the tensor
+// core reads lo's leading 19 bits (its truncation error is at most
+// 2^-10 |lo| <= 2^-21 |x|).
 __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
-  uint32_t h, l;
+  uint32_t h;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
   hi = __uint_as_float(h);
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - hi));
-  lo = __uint_as_float(l);
+  lo = x - hi;
 }
 
 }  // namespace tc
