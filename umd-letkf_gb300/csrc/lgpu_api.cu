@@ -58,7 +58,7 @@ enum {
   B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID, B_HX, B_HXM, B_SATOBS, B_SATPLATS,
   B_GEOM, B_CELL, B_COUNT, B_FILL, B_POSTMP, B_ORDER, B_ATMP, B_BTMP, B_SA, B_SB, B_SHX, B_SIDX, B_CSTART,
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
-  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC, B_EIGSCR,
+  B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC, B_EIGSCR, B_WCACHE,
   B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7, B_RAWQC, B_RAWHX, B_RAWHXM, B_FLAG, B_POS,
   B_PTRS, B_TOTAL,
   B_COUNT_ALL
@@ -756,6 +756,19 @@ int lgpu_solver_run(lgpu_handle *h) {
     ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
     ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
     ta.status = h->buf[B_STATUS].as<int>();
+    // weight cache for multi-pass tiles (at most 24 GB; without it every pass
+    // recomputes the weights)
+    ta.wcache = nullptr;
+    ta.nchunk_total = nchunk_total;
+    if (ta.npass >= 2) {
+      const size_t wb = gram_tc_wcache_bytes(G, nchunk_total);
+      if (wb <= ((size_t)24 << 30)) {
+        if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess)
+          ta.wcache = h->buf[B_WCACHE].as<float>();
+        else
+          cudaGetLastError();   // clear the failed allocation
+      }
+    }
     CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
   }
   GramArgs ga;

@@ -63,6 +63,7 @@ constexpr uint32_t SBO = (KC / 4) * CMB;      // bytes per 8-row group (all K of
 constexpr uint32_t WB = (TM / 8) * SBO;       // bytes per W operand copy
 constexpr size_t kSmemBudget = 227 * 1024 - 4096;   // dynamic shared memory (static part below 4 KB)
 constexpr int WT = 256;        // threads of the stream kernels
+constexpr int WCB = TM * KC * 4;   // bytes of one chunk's cached weights
 constexpr int YS = 20;         // floats per member row of a chunk record (16 observations + 4: conflict-free rows)
 
 __device__ __forceinline__ uint32_t kmaj(int row, int kk) {
@@ -328,20 +329,25 @@ __device__ __forceinline__ void bar_arrive(unsigned long long *b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(b)) : "memory");
 }
 
-template <int LOC, int NS, int NR>
+// WMODE: 0 = weights computed; 1 = weights computed and written to the
+// weight cache (first feature pass of a tile); 2 = weights read from the
+// cache (later passes: the producers form only the feature products)
+template <int LOC, int NS, int NR, int WMODE>
 __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(16) TcSmem S;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int pass = blockIdx.x % a.npass;
-  const int g = (blockIdx.x / a.npass) % a.groups;
-  const int tile = blockIdx.x / (a.npass * a.groups);
+  const int pass = a.pass0 + blockIdx.x % a.npl;
+  const int g = (blockIdx.x / a.npl) % a.groups;
+  const int tile = blockIdx.x / (a.npl * a.groups);
   const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
+  const int slotb = cb + (WMODE == 2 ? WCB : 0);   // ring slot: chunk record (+ cached weights)
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
   const uint32_t stage_bytes = 2 * WB + 2 * PB;
   auto stage_ptr = [&](int s) { return dsm + (size_t)s * stage_bytes; };
   unsigned char *ring = dsm + (size_t)NS * stage_bytes;
   const int c0 = a.tile_off[tile];
+  float *wcache = WMODE != 0 ? a.wcache + (size_t)g * a.nchunk_total * (TM * KC) : nullptr;
   const int nchunks = a.tile_off[tile + 1] - c0;
   const int ntile = a.tile_n[tile];
   const uint32_t tmem_cols = a.tmem_cols;
@@ -412,10 +418,23 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         S.fault = 1;
         break;
       }
-      const unsigned char *rec = ring + (size_t)r * cb;
+      const unsigned char *rec = ring + (size_t)r * slotb;
       const float4 *RA = reinterpret_cast<const float4 *>(rec);
       unsigned char *Whi = stage_ptr(s), *Wlo = Whi + WB, *Phi = Whi + 2 * WB, *Plo = Phi + PB;
-
+      bool anyk = false;
+      if (WMODE == 2) {
+        // ---- weights of this chunk from the cache
+        const float4 w4 = *reinterpret_cast<const float4 *>(rec + cb + (size_t)(wc * KC + wq * 4) * 4);
+        float h4[4], l4[4];
+        tc::split_tf32(w4.x, h4[0], l4[0]);
+        tc::split_tf32(w4.y, h4[1], l4[1]);
+        tc::split_tf32(w4.z, h4[2], l4[2]);
+        tc::split_tf32(w4.w, h4[3], l4[3]);
+        anyk = (w4.x != 0.0f) || (w4.y != 0.0f) || (w4.z != 0.0f) || (w4.w != 0.0f);
+        const uint32_t off = kmaj(wc, wq * 4);
+        *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+        *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+      } else {
       // ---- weights: four observations, fast path without branches
       float w[4];
       unsigned unsure = 0, inr = 0;
@@ -451,9 +470,8 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
           inr = (inr & ~(1u << u)) | ((in ? 1u : 0u) << u);
         }
       }
-      bool anyk = false;
       {
-        float h4[4], l4[4];
+        float h4[4], l4[4], wv4[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           const float rl = w[u];
@@ -465,11 +483,16 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
             anyk = true;
             wv = rl * RA[wq * 4 + u].w;   // the record holds 1/err
           }
+          wv4[u] = wv;
           tc::split_tf32(wv, h4[u], l4[u]);
         }
         const uint32_t off = kmaj(wc, wq * 4);
         *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
         *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+        if (WMODE == 1)
+          *reinterpret_cast<float4 *>(wcache + ((size_t)(c0 + ch) * TM + wc) * KC + wq * 4) =
+              make_float4(wv4[0], wv4[1], wv4[2], wv4[3]);
+      }
       }
       // ---- feature products: feature f over the 16 observations
       if (fin) {
@@ -498,8 +521,16 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     if (lane == 0) {
       const unsigned char *src = a.rec + (size_t)c0 * cb;
       auto load = [&](int ch) {
-        tc::bulk_load(ring + (size_t)(ch % NR) * cb, src + (size_t)ch * cb, (uint32_t)cb,
-                      reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]));
+        unsigned char *dst = ring + (size_t)(ch % NR) * slotb;
+        uint64_t *bar = reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]);
+        if (WMODE == 2) {   // record + the chunk's cached weights, one transaction count
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)),
+                       "r"((uint32_t)slotb) : "memory");
+          tc::bulk_copy_g2s(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
+          tc::bulk_copy_g2s(dst + cb, wcache + (size_t)(c0 + ch) * (TM * KC), (uint32_t)WCB, bar);
+        } else {
+          tc::bulk_load(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
+        }
       };
       int n_loaded = nchunks < NR ? nchunks : NR;
       for (int ch = 0; ch < n_loaded; ch++) load(ch);
@@ -669,10 +700,16 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
 
 // Stage / ring depths: three operand stages when they fit beside three record
 // slots, else two stages and eight slots.
-void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem) {
+void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem, bool wread = false) {
   const size_t PB = (size_t)(np / 8) * SBO;
   const size_t stage = 2 * WB + 2 * PB;
-  const size_t cb = record_bytes(k);
+  const size_t cb = record_bytes(k) + (wread ? (size_t)WCB : 0);
+  if (wread) {   // bigger ring slots: two operand stages, four slots
+    *ns = 2;
+    *nr = 4;
+    *smem = 2 * stage + 4 * cb;
+    return;
+  }
   if (3 * stage + 3 * cb <= kSmemBudget) { *ns = 3; *nr = 3; }
   else { *ns = 2; *nr = 8; }
   *smem = (size_t)*ns * stage + (size_t)*nr * cb;
@@ -719,18 +756,43 @@ cudaError_t launch_tile_fill(cudaStream_t st, int ntiles, const TilePar *tp, con
   return cudaGetLastError();
 }
 
-template <int LOC, int NS, int NR>
+template <int LOC, int NS, int NR, int WMODE>
 static cudaError_t launch_gram_tc_t(cudaStream_t st, const TcArgs &a, size_t smem, long long grid) {
   cudaError_t e =
-      cudaFuncSetAttribute(k_gram_tc<LOC, NS, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_gram_tc<LOC, NS, NR, WMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_gram_tc<LOC, NS, NR><<<(int)grid, NT, smem, st>>>(a);
+  k_gram_tc<LOC, NS, NR, WMODE><<<(int)grid, NT, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 template <int LOC>
-static cudaError_t launch_gram_tc_loc(cudaStream_t st, const TcArgs &a, int ns, size_t smem, long long grid) {
-  return ns == 3 ? launch_gram_tc_t<LOC, 3, 3>(st, a, smem, grid) : launch_gram_tc_t<LOC, 2, 8>(st, a, smem, grid);
+static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) {
+  int ns, nr;
+  size_t smem;
+  gram_tc_config(a.k, a.np, &ns, &nr, &smem);
+  const long long per_pass = (long long)a.ntiles * a.groups;
+  if (per_pass * a.npass > 0x7fffffffLL) return cudaErrorInvalidValue;
+  cudaError_t e;
+  if (a.npass >= 2 && a.wcache) {
+    // first pass computes the weights and caches them; later passes read them
+    a.pass0 = 0;
+    a.npl = 1;
+    e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 1>(st, a, smem, per_pass) : launch_gram_tc_t<LOC, 2, 8, 1>(st, a, smem, per_pass);
+    if (e != cudaSuccess) return e;
+    size_t smem2;
+    gram_tc_config(a.k, a.np, &ns, &nr, &smem2, true);
+    a.pass0 = 1;
+    a.npl = a.npass - 1;
+    e = launch_gram_tc_t<LOC, 2, 4, 2>(st, a, smem2, per_pass * a.npl);
+    (*launches) += 2;
+    return e;
+  }
+  a.pass0 = 0;
+  a.npl = a.npass;
+  e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 0>(st, a, smem, per_pass * a.npass)
+              : launch_gram_tc_t<LOC, 2, 8, 0>(st, a, smem, per_pass * a.npass);
+  (*launches)++;
+  return e;
 }
 
 cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
@@ -740,19 +802,13 @@ cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
   uint32_t tc = 32;
   while ((int)tc < a.np) tc <<= 1;
   a.tmem_cols = tc;
-  int ns, nr;
-  size_t smem;
-  gram_tc_config(a.k, a.np, &ns, &nr, &smem);
-  const long long grid = (long long)a.ntiles * a.groups * a.npass;
-  if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
-  cudaError_t e;
   switch (a.loc.cls) {
-  case LOC_OCEAN: e = launch_gram_tc_loc<LOC_OCEAN>(st, a, ns, smem, grid); break;
-  case LOC_VTGC: e = launch_gram_tc_loc<LOC_VTGC>(st, a, ns, smem, grid); break;
-  default: e = launch_gram_tc_loc<LOC_NOVRT>(st, a, ns, smem, grid); break;
+  case LOC_OCEAN: return launch_gram_tc_loc<LOC_OCEAN>(st, a, launches);
+  case LOC_VTGC: return launch_gram_tc_loc<LOC_VTGC>(st, a, launches);
+  default: return launch_gram_tc_loc<LOC_NOVRT>(st, a, launches);
   }
-  (*launches)++;
-  return e;
 }
+
+size_t gram_tc_wcache_bytes(int groups, int nchunk_total) { return (size_t)groups * nchunk_total * WCB; }
 
 }  // namespace lgpu

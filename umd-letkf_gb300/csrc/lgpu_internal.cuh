@@ -399,6 +399,9 @@ struct TcArgs {
   const int *tile_n;         // [ntiles] candidates of each tile
   int cb;                    // bytes per chunk record (set by the launcher)
   uint32_t tmem_cols;        // TMEM columns per CTA (set by the launcher)
+  float *wcache;             // weight cache [groups][chunks][128 columns][16 obs], or null
+  int nchunk_total;          // chunks over all tiles (weight cache indexing)
+  int pass0, npl;            // feature passes of one launch: [pass0, pass0 + npl) (set by the launcher)
   float *G;
   int *nkept;
   float *diag_obscount, *diag_lg_obscount, *diag_lg_obsloc;
@@ -415,6 +418,7 @@ cudaError_t launch_tile_fill(cudaStream_t st, int ntiles, const TilePar *tp, con
                              const ObsSorted &obs, int k, int kp, const int *tile_off, unsigned char *rec,
                              int *status, int *launches);
 cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a, int *launches);
+size_t gram_tc_wcache_bytes(int groups, int nchunk_total);
 void gram_tc_passes(int k, int *npass, int *np);
 
 struct EigArgs {
