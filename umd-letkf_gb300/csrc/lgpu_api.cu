@@ -756,17 +756,21 @@ int lgpu_solver_run(lgpu_handle *h) {
     ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
     ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
     ta.status = h->buf[B_STATUS].as<int>();
-    // weight cache for multi-pass tiles (at most 24 GB; without it every pass
+    // weight cache for multi-pass tiles (at most 48 GB; without it every pass
     // recomputes the weights)
     ta.wcache = nullptr;
     ta.nchunk_total = nchunk_total;
+    ta.wflag = nullptr;
     if (ta.npass >= 2) {
       const size_t wb = gram_tc_wcache_bytes(G, nchunk_total);
-      if (wb <= ((size_t)24 << 30)) {
-        if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess)
+      if (wb <= ((size_t)48 << 30)) {
+        if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess) {
           ta.wcache = h->buf[B_WCACHE].as<float>();
-        else
+          ta.wflag = reinterpret_cast<int *>(h->buf[B_WCACHE].as<unsigned char>() +
+                                             (wb - (size_t)G * nchunk_total * sizeof(int)));
+        } else {
           cudaGetLastError();   // clear the failed allocation
+        }
       }
     }
     CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");

@@ -63,7 +63,7 @@ constexpr uint32_t SBO = (KC / 4) * CMB;      // bytes per 8-row group (all K of
 constexpr uint32_t WB = (TM / 8) * SBO;       // bytes per W operand copy
 constexpr size_t kSmemBudget = 227 * 1024 - 4096;   // dynamic shared memory (static part below 4 KB)
 constexpr int WT = 256;        // threads of the stream kernels
-constexpr int WCB = TM * KC * 4;   // bytes of one chunk's cached weights
+constexpr int WCB = 2 * WB;   // bytes of one chunk's cached weight operand block (hi | lo)
 constexpr int YS = 20;         // floats per member row of a chunk record (16 observations + 4: conflict-free rows)
 
 __device__ __forceinline__ uint32_t kmaj(int row, int kk) {
@@ -330,8 +330,10 @@ __device__ __forceinline__ void bar_arrive(unsigned long long *b) {
 }
 
 // WMODE: 0 = weights computed; 1 = weights computed and written to the
-// weight cache (first feature pass of a tile); 2 = weights read from the
-// cache (later passes: the producers form only the feature products)
+// weight cache as the stage's TF32 hi/lo operand block, with the chunk's
+// MMA flag (first feature pass of a tile); 2 = the operand block is
+// bulk-copied from the cache into the stage (later passes: the producers
+// form only the feature products)
 template <int LOC, int NS, int NR, int WMODE>
 __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
@@ -341,13 +343,14 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   const int g = (blockIdx.x / a.npl) % a.groups;
   const int tile = blockIdx.x / (a.npl * a.groups);
   const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
-  const int slotb = cb + (WMODE == 2 ? WCB : 0);   // ring slot: chunk record (+ cached weights)
+  const int slotb = cb;   // ring slot: one chunk record
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
   const uint32_t stage_bytes = 2 * WB + 2 * PB;
   auto stage_ptr = [&](int s) { return dsm + (size_t)s * stage_bytes; };
   unsigned char *ring = dsm + (size_t)NS * stage_bytes;
   const int c0 = a.tile_off[tile];
-  float *wcache = WMODE != 0 ? a.wcache + (size_t)g * a.nchunk_total * (TM * KC) : nullptr;
+  float *wcache = WMODE != 0 ? a.wcache + (size_t)g * a.nchunk_total * (WCB / 4) : nullptr;
+  int *wflag = WMODE != 0 ? a.wflag + (size_t)g * a.nchunk_total : nullptr;
   const int nchunks = a.tile_off[tile + 1] - c0;
   const int ntile = a.tile_n[tile];
   const uint32_t tmem_cols = a.tmem_cols;
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   if (wid == 0) tc::tmem_alloc(&S.tmem, tmem_cols);
   if (tid == 0) {
     for (int s = 0; s < NS; s++) {
-      tc::mbar_init(reinterpret_cast<uint64_t *>(&S.full[s]), NPW);
+      tc::mbar_init(reinterpret_cast<uint64_t *>(&S.full[s]), WMODE == 2 ? NPW + 1 : NPW);
       tc::mbar_init(reinterpret_cast<uint64_t *>(&S.empty[s]), 1);
       S.anyk[s] = 0;
     }
@@ -423,17 +426,15 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       unsigned char *Whi = stage_ptr(s), *Wlo = Whi + WB, *Phi = Whi + 2 * WB, *Plo = Phi + PB;
       bool anyk = false;
       if (WMODE == 2) {
-        // ---- weights of this chunk from the cache
-        const float4 w4 = *reinterpret_cast<const float4 *>(rec + cb + (size_t)(wc * KC + wq * 4) * 4);
-        float h4[4], l4[4];
-        tc::split_tf32(w4.x, h4[0], l4[0]);
-        tc::split_tf32(w4.y, h4[1], l4[1]);
-        tc::split_tf32(w4.z, h4[2], l4[2]);
-        tc::split_tf32(w4.w, h4[3], l4[3]);
-        anyk = (w4.x != 0.0f) || (w4.y != 0.0f) || (w4.z != 0.0f) || (w4.w != 0.0f);
-        const uint32_t off = kmaj(wc, wq * 4);
-        *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
-        *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+        // ---- the chunk's weight operand block (hi | lo) from the cache into
+        // the stage, counted on the stage's full barrier (the stage is free:
+        // its empty barrier was waited on above)
+        if (tid == 0) {
+          uint64_t *fb = reinterpret_cast<uint64_t *>(&S.full[s]);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(fb)),
+                       "r"((uint32_t)WCB) : "memory");
+          tc::bulk_copy_g2s(Whi, wcache + (size_t)(c0 + ch) * (WCB / 4), (uint32_t)WCB, fb);
+        }
       } else {
       // ---- weights: four observations, fast path without branches
       float w[4];
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         }
       }
       {
-        float h4[4], l4[4], wv4[4];
+        float h4[4], l4[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           const float rl = w[u];
@@ -483,15 +484,18 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
             anyk = true;
             wv = rl * RA[wq * 4 + u].w;   // the record holds 1/err
           }
-          wv4[u] = wv;
           tc::split_tf32(wv, h4[u], l4[u]);
         }
         const uint32_t off = kmaj(wc, wq * 4);
         *reinterpret_cast<float4 *>(Whi + off) = make_float4(h4[0], h4[1], h4[2], h4[3]);
         *reinterpret_cast<float4 *>(Wlo + off) = make_float4(l4[0], l4[1], l4[2], l4[3]);
-        if (WMODE == 1)
-          *reinterpret_cast<float4 *>(wcache + ((size_t)(c0 + ch) * TM + wc) * KC + wq * 4) =
-              make_float4(wv4[0], wv4[1], wv4[2], wv4[3]);
+        if (WMODE == 1) {
+          float *blk = wcache + (size_t)(c0 + ch) * (WCB / 4);
+          *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(blk) + off) =
+              make_float4(h4[0], h4[1], h4[2], h4[3]);
+          *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(blk) + WB + off) =
+              make_float4(l4[0], l4[1], l4[2], l4[3]);
+        }
       }
       }
       // ---- feature products: feature f over the 16 observations
@@ -523,14 +527,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       auto load = [&](int ch) {
         unsigned char *dst = ring + (size_t)(ch % NR) * slotb;
         uint64_t *bar = reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]);
-        if (WMODE == 2) {   // record + the chunk's cached weights, one transaction count
-          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)),
-                       "r"((uint32_t)slotb) : "memory");
-          tc::bulk_copy_g2s(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
-          tc::bulk_copy_g2s(dst + cb, wcache + (size_t)(c0 + ch) * (TM * KC), (uint32_t)WCB, bar);
-        } else {
-          tc::bulk_load(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
-        }
+        tc::bulk_load(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
       };
       int n_loaded = nchunks < NR ? nchunks : NR;
       for (int ch = 0; ch < n_loaded; ch++) load(ch);
@@ -539,10 +536,13 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       bool issued = false;
       for (int ch = 0; ch < nchunks; ch++) {
         const int s = ch % NS;
+        const int cached_flag = WMODE == 2 ? wflag[c0 + ch] : 0;   // issued before the wait hides its latency
         if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.full[s]), (ch / NS) & 1)) { S.fault = 1; break; }
         // every producer is done with the records of chunk ch: refill the slot
         if (n_loaded < nchunks) load(n_loaded++);
-        if (S.anyk[s] == ch + 1) {
+        const bool mma = WMODE == 2 ? cached_flag != 0 : S.anyk[s] == ch + 1;
+        if (WMODE == 1) wflag[c0 + ch] = mma ? 1 : 0;
+        if (mma) {
           tc::fence_after();
           const uint32_t whi = tc::smem_u32(stage_ptr(s)), wlo = whi + WB, phi = whi + 2 * WB, plo = phi + PB;
 #pragma unroll
@@ -700,16 +700,11 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
 
 // Stage / ring depths: three operand stages when they fit beside three record
 // slots, else two stages and eight slots.
-void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem, bool wread = false) {
+void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem) {
   const size_t PB = (size_t)(np / 8) * SBO;
   const size_t stage = 2 * WB + 2 * PB;
-  const size_t cb = record_bytes(k) + (wread ? (size_t)WCB : 0);
-  if (wread) {   // bigger ring slots: two operand stages, four slots
-    *ns = 2;
-    *nr = 4;
-    *smem = 2 * stage + 4 * cb;
-    return;
-  }
+  const size_t cb = record_bytes(k);
+
   if (3 * stage + 3 * cb <= kSmemBudget) { *ns = 3; *nr = 3; }
   else { *ns = 2; *nr = 8; }
   *smem = (size_t)*ns * stage + (size_t)*nr * cb;
@@ -779,11 +774,10 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
     a.npl = 1;
     e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 1>(st, a, smem, per_pass) : launch_gram_tc_t<LOC, 2, 8, 1>(st, a, smem, per_pass);
     if (e != cudaSuccess) return e;
-    size_t smem2;
-    gram_tc_config(a.k, a.np, &ns, &nr, &smem2, true);
     a.pass0 = 1;
     a.npl = a.npass - 1;
-    e = launch_gram_tc_t<LOC, 2, 4, 2>(st, a, smem2, per_pass * a.npl);
+    e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 2>(st, a, smem, per_pass * a.npl)
+                : launch_gram_tc_t<LOC, 2, 8, 2>(st, a, smem, per_pass * a.npl);
     (*launches) += 2;
     return e;
   }
@@ -809,6 +803,8 @@ cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
   }
 }
 
-size_t gram_tc_wcache_bytes(int groups, int nchunk_total) { return (size_t)groups * nchunk_total * WCB; }
+size_t gram_tc_wcache_bytes(int groups, int nchunk_total) {
+  return (size_t)groups * nchunk_total * (WCB + sizeof(int));   // operand blocks, then the MMA flags
+}
 
 }  // namespace lgpu

@@ -399,7 +399,8 @@ struct TcArgs {
   const int *tile_n;         // [ntiles] candidates of each tile
   int cb;                    // bytes per chunk record (set by the launcher)
   uint32_t tmem_cols;        // TMEM columns per CTA (set by the launcher)
-  float *wcache;             // weight cache [groups][chunks][128 columns][16 obs], or null
+  float *wcache;             // weight cache [groups][chunks] TF32 hi | lo operand blocks, or null
+  int *wflag;                // [groups][chunks]: the chunk has a kept pair (MMA issued)
   int nchunk_total;          // chunks over all tiles (weight cache indexing)
   int pass0, npl;            // feature passes of one launch: [pass0, pass0 + npl) (set by the launcher)
   float *G;
