@@ -256,6 +256,9 @@ def gpu_arm(args, dist):
     eig_flop = 13.0 * k ** 3 * units
     upd_bytes = 2.0 * ncol * ns * k * 4 + 4.0 * ncol * ns * 4
     gram_kernel_ms = stage["gram_ms"] - stage["tiles_ms"]
+    # executed tensor work of the batched Gram: 3 TF32 products x 2 flop x
+    # M=128 x N=features per pass x K=16 per chunk that ran MMAs
+    mma_flop = float(tims[-1]["mma_chunks"]) * 3 * 2 * 128 * tims[-1]["mma_n"] * 16
     stages = {
         "tile_streams": {"ms": stage["tiles_ms"]},
         "gram": {"ms": gram_kernel_ms, "tflops": gram_flop / (gram_kernel_ms * 1e-3) / 1e12},
@@ -282,6 +285,12 @@ def gpu_arm(args, dist):
                          "the MMAs, so bf16/6 bounds this kernel's algorithmic rate" if dom == "gram" else
                          "FP32 on the CUDA cores (no tensor work); nominal FP32 SIMT peak %.1f TFLOP/s, "
                          "frac of it %.4f" % (simt, ach / simt))}
+    if dom == "gram" and mma_flop > 0:
+        ex = mma_flop / (gram_kernel_ms * 1e-3) / 1e12
+        roof["tensor_executed"] = {"tflops": ex, "peak_tf32_tflops": bf16 / 2, "frac": ex / (bf16 / 2),
+                                   "note": "MMA work issued (3 TF32 products per FP32 product, zero weights "
+                                           "and padding included) over the Gram kernels' time; TF32 dense "
+                                           "peak taken as half the measured bf16 peak"}
     variant = {1: "plain", 2: "batched_tc"}.get(tims[-1]["variant"], "?")
     plain = None
     if variant != "plain" and not args.no_plain:

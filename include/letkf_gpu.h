@@ -140,6 +140,9 @@ typedef struct lgpu_timings {
   long long kept_pairs;   /* sum over units of kept local observations (only when counted) */
   int variant;       /* Gram variant that ran (LGPU_VARIANT_PLAIN / _BATCHED_TC) */
   float tiles_ms;    /* BATCHED_TC: part of gram_ms spent building the tile candidate streams */
+  long long mma_chunks;  /* BATCHED_TC: (tile, group, pass, 16-observation chunk) steps that ran MMAs */
+  int mma_n;         /* BATCHED_TC: features per pass (MMA N); executed TF32 flops =
+                        mma_chunks * 3 products * 2 * 128 * mma_n * 16 */
 } lgpu_timings;
 
 /* Gram variants.  PLAIN: one CTA per (column, group), FP32 on the CUDA

@@ -94,6 +94,7 @@ struct lgpu_handle {
   int variant = LGPU_VARIANT_AUTO;
   int ntiles = 0;
   bool used_tc = false;
+  int mma_n = 0;
   DevBuf buf[B_COUNT_ALL];
   lgpu_timings tim{};
 };
@@ -740,6 +741,7 @@ int lgpu_solver_run(lgpu_handle *h) {
     ta.k = k;
     ta.kp = kp;
     gram_tc_passes(k, &ta.npass, &ta.np);
+    h->mma_n = ta.np;
     ta.nf = packed_size(k);
     ta.ncol = h->ncol;
     ta.tile_cols = h->buf[B_TILECOLS].as<int>();
@@ -890,8 +892,8 @@ int lgpu_solver_run(lgpu_handle *h) {
     }
   }
   CK(cudaEventRecord(h->ev[5], st), "event");
-  int status = 0;
-  CK(cudaMemcpyAsync(&status, h->buf[B_STATUS].p, 4, cudaMemcpyDeviceToHost, st), "D2H status");
+  int stat4[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(stat4, h->buf[B_STATUS].p, 16, cudaMemcpyDeviceToHost, st), "D2H status");
   CK(cudaStreamSynchronize(st), "solver_run");
   if (bound) CK(cudaStreamSynchronize(h->cst), "solver_run copies");
   float ms[3];
@@ -915,6 +917,9 @@ int lgpu_solver_run(lgpu_handle *h) {
   h->tim.variant = h->used_tc ? LGPU_VARIANT_BATCHED_TC : LGPU_VARIANT_PLAIN;
   h->tim.units = h->nunits;
   h->tim.kept_pairs = -1;
+  h->tim.mma_chunks = h->used_tc ? stat4[2] : 0;
+  h->tim.mma_n = h->used_tc ? h->mma_n : 0;
+  const int status = stat4[0];
   h->ran = true;
   if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
   if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");

@@ -534,6 +534,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       const int nb0 = NP < 256 ? NP : 256, nb1 = NP - nb0;
       const uint32_t id0 = tc::idesc_tf32(TM, nb0), id1 = nb1 > 0 ? tc::idesc_tf32(TM, nb1) : 0u;
       bool issued = false;
+      int nmma = 0;
       for (int ch = 0; ch < nchunks; ch++) {
         const int s = ch % NS;
         const int cached_flag = WMODE == 2 ? wflag[c0 + ch] : 0;   // issued before the wait hides its latency
@@ -561,6 +562,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
             }
           tc::commit(reinterpret_cast<uint64_t *>(&S.empty[s]));
           issued = true;
+          nmma++;
         } else {
           bar_arrive(&S.empty[s]);
         }
@@ -569,6 +571,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       tc::commit(reinterpret_cast<uint64_t *>(&S.done));
       if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.done), 0)) S.fault = 1;
       S.issued = issued ? 1 : 0;
+      if (nmma) atomicAdd(a.status + 2, nmma);   // chunks whose MMAs ran (executed-work counter)
       // no record copy may still be in flight when the CTA exits
       for (int ch = n_loaded > NR ? n_loaded - NR : 0; ch < n_loaded; ch++)
         if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]), (ch / NR) & 1)) S.fault = 1;

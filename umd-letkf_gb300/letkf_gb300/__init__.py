@@ -76,7 +76,8 @@ class Timings(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_float), ("index_ms", ctypes.c_float), ("prep_ms", ctypes.c_float),
                 ("gram_ms", ctypes.c_float), ("eig_ms", ctypes.c_float), ("update_ms", ctypes.c_float),
                 ("launches", ctypes.c_int), ("units", ctypes.c_int), ("kept_pairs", ctypes.c_longlong),
-                ("variant", ctypes.c_int), ("tiles_ms", ctypes.c_float)]
+                ("variant", ctypes.c_int), ("tiles_ms", ctypes.c_float), ("mma_chunks", ctypes.c_longlong),
+                ("mma_n", ctypes.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
