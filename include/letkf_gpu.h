@@ -148,8 +148,11 @@ typedef struct lgpu_timings {
 /* Gram variants.  PLAIN: one CTA per (column, group), FP32 on the CUDA
  * cores.  BATCHED_TC: tiles of 128 neighbouring columns share their
  * observations; the Gram of a tile is one GEMM on the tensor cores (tcgen05,
- * TF32 with a three-term hi/lo split, FP32 accumulation).  AUTO picks
- * BATCHED_TC.  Both give bit-identical observation lists. */
+ * TF32 with a three-term hi/lo split, FP32 accumulation).  AUTO (default)
+ * runs both forms, timed, on the first analysis after lgpu_set_grid,
+ * lgpu_loc_init or a change of ensemble size, and keeps the faster one
+ * (PLAIN below k = 8); the first analysis therefore takes longer.  Both
+ * forms give bit-identical observation lists and keep decisions. */
 #define LGPU_VARIANT_AUTO 0
 #define LGPU_VARIANT_PLAIN 1
 #define LGPU_VARIANT_BATCHED_TC 2

@@ -200,6 +200,29 @@ def test_ocean_groups_with_k_multiple_of_4(k):
         _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label="ocean k=%d" % k, variant=gram)
 
 
+@pytest.mark.parametrize("name", ["c2small", "c3small"])
+def test_auto_variant_choice(name):
+    """AUTO times both Gram forms on the first analysis and keeps the faster;
+    its analysis, on the first run and on the next (which reuses the choice),
+    is bit-identical to an explicit run of the chosen form."""
+    cfg = workload_cfg(name)
+    prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
+    res = gpu_run(prob, cfg["localization"], cfg["solver"], variant="auto", keep_open=True)
+    s = res["solver"]
+    try:
+        chosen = res["timings"]["variant"]
+        assert chosen in (1, 2)
+        s.run()
+        assert s.timings()["variant"] == chosen
+        second = s.get_state()
+    finally:
+        s.close()
+    ref = gpu_run(prob, cfg["localization"], cfg["solver"], variant="plain" if chosen == 1 else "batched")
+    for got in ((res["state"], res["mean"], res["sprd"]), second):
+        for a, b in zip(got, (ref["state"], ref["mean"], ref["sprd"])):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
 def test_single_observation_closed_form():
     """One obs, one column in range: the GPU mean increment at the observed
     slab equals the scalar Kalman update."""

@@ -74,6 +74,7 @@ struct lgpu_handle {
   cudaStream_t cst = nullptr;      // host<->device copies of a bound state
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev_in[2] = {};       // bound state: mean/spread, members uploaded
+  cudaEvent_t ev_tune[3] = {};     // AUTO: timing of the two Gram forms
   cudaEvent_t ev_chunk[kOutChunks][3] = {};   // per column chunk: eigensolve start, update start, update end
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
   std::string err;
@@ -95,6 +96,7 @@ struct lgpu_handle {
   int ntiles = 0;
   bool used_tc = false;
   int mma_n = 0;
+  int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
   DevBuf buf[B_COUNT_ALL];
   lgpu_timings tim{};
 };
@@ -224,6 +226,8 @@ int lgpu_create(int device, lgpu_handle **out) {
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_in)
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_tune)
+    if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &row : h->ev_chunk)
     for (auto &ev : row)
       if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
@@ -245,6 +249,7 @@ void lgpu_destroy(lgpu_handle *h) {
   for (auto &b : h->buf) b.release();
   for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_in) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : h->ev_tune) if (ev) cudaEventDestroy(ev);
   for (auto &row : h->ev_chunk)
     for (auto &ev : row) if (ev) cudaEventDestroy(ev);
   if (h->st) cudaStreamDestroy(h->st);
@@ -324,6 +329,7 @@ int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *c) {
   if (L.groups <= 0) return fail(h, LGPU_ERR_CONFIG, "localizer class needs to properly define 'maxgroups'");
   h->loc = L;
   h->loc_ok = true;
+  h->auto_choice = 0;
   h->ran = false;
   return LGPU_OK;
 }
@@ -371,6 +377,7 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
        "H2D tiles");
   CK(cudaStreamSynchronize(h->st), "set_grid sync");
   h->ntiles = (int)(tiles.size() / 128);
+  h->auto_choice = 0;
   h->ncol = nij;
   h->nact = (int)act.size();
   h->h_col2act = c2a;
@@ -430,6 +437,7 @@ int prepare_state(lgpu_handle *h, int k, int ns, const float *state, const float
   CK(cudaMemcpyAsync(h->buf[B_VARLB].p, lb.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D lb");
   CK(cudaMemcpyAsync(h->buf[B_VARUB].p, ub.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D ub");
   CK(cudaStreamSynchronize(h->st), "set_state sync");
+  if (h->k != k) h->auto_choice = 0;
   h->k = k;
   h->ns = ns;
   h->kp = (k + 3) & ~3;
@@ -716,84 +724,113 @@ int lgpu_solver_run(lgpu_handle *h) {
   CK(cudaMemsetAsync(h->buf[B_STATUS].p, 0, 16, st), "memset");
   CK(cudaEventRecord(h->ev[2], st), "event");
   // ---- search + localize + Gram ----
-  const bool use_tc = h->variant == LGPU_VARIANT_BATCHED_TC || (h->variant == LGPU_VARIANT_AUTO && k >= 8);
-  h->used_tc = use_tc;
-  if (use_tc) {
-    CK(launch_tile_prep(st, h->ntiles, h->buf[B_TILECOLS].as<int>(), h->buf[B_CP].as<ColPar>(),
-                        h->buf[B_TILEPAR].as<TilePar>(), &launches), "tile prep");
-    // tile candidate streams: count, size the record buffer, fill
-    CK(launch_tile_count(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os,
-                         h->buf[B_TILEN].as<int>(), h->buf[B_TILEOFF].as<int>(), &launches),
-       "tile count");
-    int nchunk_total = 0;
-    CK(cudaMemcpyAsync(&nchunk_total, h->buf[B_TILEOFF].as<int>() + h->ntiles, sizeof(int), cudaMemcpyDeviceToHost, st),
-       "D2H stream size");
-    CK(cudaStreamSynchronize(st), "stream size sync");
-    CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
-    CK(launch_tile_fill(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
-                        h->buf[B_TILEOFF].as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
-                        h->buf[B_STATUS].as<int>(), &launches),
-       "tile fill");
-    CK(cudaEventRecord(h->ev[6], st), "event");
-    TcArgs ta;
-    ta.ntiles = h->ntiles;
-    ta.groups = G;
-    ta.k = k;
-    ta.kp = kp;
-    gram_tc_passes(k, &ta.npass, &ta.np);
-    h->mma_n = ta.np;
-    ta.nf = packed_size(k);
-    ta.ncol = h->ncol;
-    ta.tile_cols = h->buf[B_TILECOLS].as<int>();
-    ta.col2act = h->buf[B_COL2ACT].as<int>();
-    ta.cp = h->buf[B_CP].as<ColPar>();
-    ta.loc = h->loc;
-    ta.tp = h->buf[B_TILEPAR].as<TilePar>();
-    ta.rec = h->buf[B_TILEREC].as<unsigned char>();
-    ta.tile_off = h->buf[B_TILEOFF].as<int>();
-    ta.tile_n = h->buf[B_TILEN].as<int>();
-    ta.G = h->buf[B_G].as<float>();
-    ta.nkept = h->buf[B_NKEPT].as<int>();
-    ta.diag_obscount = h->buf[B_DOBSC].as<float>();
-    ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
-    ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
-    ta.status = h->buf[B_STATUS].as<int>();
-    // weight cache for multi-pass tiles (at most 48 GB; without it every pass
-    // recomputes the weights)
-    ta.wcache = nullptr;
-    ta.nchunk_total = nchunk_total;
-    ta.wflag = nullptr;
-    if (ta.npass >= 2) {
-      const size_t wb = gram_tc_wcache_bytes(G, nchunk_total);
-      if (wb <= ((size_t)48 << 30)) {
-        if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess) {
-          ta.wcache = h->buf[B_WCACHE].as<float>();
-          ta.wflag = reinterpret_cast<int *>(h->buf[B_WCACHE].as<unsigned char>() +
-                                             (wb - (size_t)G * nchunk_total * sizeof(int)));
-        } else {
-          cudaGetLastError();   // clear the failed allocation
+  // ---- Gram: the batched tensor-core form or the plain per-column form ----
+  auto run_batched = [&]() -> int {
+      CK(launch_tile_prep(st, h->ntiles, h->buf[B_TILECOLS].as<int>(), h->buf[B_CP].as<ColPar>(),
+                          h->buf[B_TILEPAR].as<TilePar>(), &launches), "tile prep");
+      // tile candidate streams: count, size the record buffer, fill
+      CK(launch_tile_count(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os,
+                           h->buf[B_TILEN].as<int>(), h->buf[B_TILEOFF].as<int>(), &launches),
+         "tile count");
+      int nchunk_total = 0;
+      CK(cudaMemcpyAsync(&nchunk_total, h->buf[B_TILEOFF].as<int>() + h->ntiles, sizeof(int), cudaMemcpyDeviceToHost, st),
+         "D2H stream size");
+      CK(cudaStreamSynchronize(st), "stream size sync");
+      CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
+      CK(launch_tile_fill(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
+                          h->buf[B_TILEOFF].as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
+                          h->buf[B_STATUS].as<int>(), &launches),
+         "tile fill");
+      CK(cudaEventRecord(h->ev[6], st), "event");
+      TcArgs ta;
+      ta.ntiles = h->ntiles;
+      ta.groups = G;
+      ta.k = k;
+      ta.kp = kp;
+      gram_tc_passes(k, &ta.npass, &ta.np);
+      h->mma_n = ta.np;
+      ta.nf = packed_size(k);
+      ta.ncol = h->ncol;
+      ta.tile_cols = h->buf[B_TILECOLS].as<int>();
+      ta.col2act = h->buf[B_COL2ACT].as<int>();
+      ta.cp = h->buf[B_CP].as<ColPar>();
+      ta.loc = h->loc;
+      ta.tp = h->buf[B_TILEPAR].as<TilePar>();
+      ta.rec = h->buf[B_TILEREC].as<unsigned char>();
+      ta.tile_off = h->buf[B_TILEOFF].as<int>();
+      ta.tile_n = h->buf[B_TILEN].as<int>();
+      ta.G = h->buf[B_G].as<float>();
+      ta.nkept = h->buf[B_NKEPT].as<int>();
+      ta.diag_obscount = h->buf[B_DOBSC].as<float>();
+      ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
+      ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
+      ta.status = h->buf[B_STATUS].as<int>();
+      // weight cache for multi-pass tiles (at most 48 GB; without it every pass
+      // recomputes the weights)
+      ta.wcache = nullptr;
+      ta.nchunk_total = nchunk_total;
+      ta.wflag = nullptr;
+      if (ta.npass >= 2) {
+        const size_t wb = gram_tc_wcache_bytes(G, nchunk_total);
+        if (wb <= ((size_t)48 << 30)) {
+          if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess) {
+            ta.wcache = h->buf[B_WCACHE].as<float>();
+            ta.wflag = reinterpret_cast<int *>(h->buf[B_WCACHE].as<unsigned char>() +
+                                               (wb - (size_t)G * nchunk_total * sizeof(int)));
+          } else {
+            cudaGetLastError();   // clear the failed allocation
+          }
         }
       }
-    }
-    CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+      CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+  
+    return LGPU_OK;
+  };
+  auto run_plain = [&]() -> int {
+    GramArgs ga;
+    ga.nunits = h->nunits;
+    ga.groups = G;
+    ga.k = k;
+    ga.kp = kp;
+    ga.active = h->buf[B_ACTIVE].as<int>();
+    ga.cp = h->buf[B_CP].as<ColPar>();
+    ga.loc = h->loc;
+    ga.obs = os;
+    ga.geom = h->buf[B_GEOM].as<IndexGeom>();
+    ga.G = h->buf[B_G].as<float>();
+    ga.nkept = h->buf[B_NKEPT].as<int>();
+    ga.diag_obscount = h->buf[B_DOBSC].as<float>();
+    ga.diag_lg_obscount = h->buf[B_DLGC].as<float>();
+    ga.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
+    ga.ncol = h->ncol;
+    CK(launch_gram(st, ga, &launches), "gram kernel");
+    return LGPU_OK;
+  };
+  // AUTO: the first analysis of a configuration (grid, localizer, k) runs
+  // both forms, timed, and keeps the faster; the plain form wins below k = 8
+  int choice = h->variant;
+  if (choice == LGPU_VARIANT_AUTO) choice = k < 8 ? LGPU_VARIANT_PLAIN : h->auto_choice;
+  int rc = LGPU_OK;
+  if (choice == 0) {
+    CK(cudaEventRecord(h->ev_tune[0], st), "event");
+    if ((rc = run_plain()) != LGPU_OK) return rc;
+    CK(cudaEventRecord(h->ev_tune[1], st), "event");
+    if ((rc = run_batched()) != LGPU_OK) return rc;
+    CK(cudaEventRecord(h->ev_tune[2], st), "event");
+    CK(cudaEventSynchronize(h->ev_tune[2]), "tune sync");
+    float tp = 0.0f, tb = 0.0f;
+    CK(cudaEventElapsedTime(&tp, h->ev_tune[0], h->ev_tune[1]), "timing");
+    CK(cudaEventElapsedTime(&tb, h->ev_tune[1], h->ev_tune[2]), "timing");
+    h->auto_choice = tb <= tp ? LGPU_VARIANT_BATCHED_TC : LGPU_VARIANT_PLAIN;
+    // the kept result is the chosen form's
+    if (h->auto_choice == LGPU_VARIANT_PLAIN && (rc = run_plain()) != LGPU_OK) return rc;
+    choice = h->auto_choice;
+  } else if (choice == LGPU_VARIANT_BATCHED_TC) {
+    if ((rc = run_batched()) != LGPU_OK) return rc;
+  } else {
+    if ((rc = run_plain()) != LGPU_OK) return rc;
   }
-  GramArgs ga;
-  ga.nunits = h->nunits;
-  ga.groups = G;
-  ga.k = k;
-  ga.kp = kp;
-  ga.active = h->buf[B_ACTIVE].as<int>();
-  ga.cp = h->buf[B_CP].as<ColPar>();
-  ga.loc = h->loc;
-  ga.obs = os;
-  ga.geom = h->buf[B_GEOM].as<IndexGeom>();
-  ga.G = h->buf[B_G].as<float>();
-  ga.nkept = h->buf[B_NKEPT].as<int>();
-  ga.diag_obscount = h->buf[B_DOBSC].as<float>();
-  ga.diag_lg_obscount = h->buf[B_DLGC].as<float>();
-  ga.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
-  ga.ncol = h->ncol;
-  if (!use_tc) CK(launch_gram(st, ga, &launches), "gram kernel");
+  h->used_tc = choice == LGPU_VARIANT_BATCHED_TC;
   CK(cudaEventRecord(h->ev[3], st), "event");
   // ---- eigensolve + transform, update + epilogue, in column chunks ----
   // A bound state is processed in kOutChunks column chunks: chunk c's

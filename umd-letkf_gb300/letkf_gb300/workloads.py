@@ -35,6 +35,10 @@ WORKLOADS = {
                localization={"class": "loc_novrt",
                              "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
                solver={}),
+    "c3k64": dict(gen=dict(workload="c3", k=64),
+                  localization={"class": "loc_novrt",
+                                "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
+                  solver={}),
     "c3small": dict(gen=dict(workload="c3", nx=180, ny=90, nz=10, n_obs=40000),
                     localization={"class": "loc_novrt",
                                   "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
