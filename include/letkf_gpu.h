@@ -72,7 +72,7 @@ typedef enum lgpu_status {
 #define LGPU_MAX_INTERP 16   /* linearinterp_lat points per table */
 #define LGPU_MAX_IDS 32      /* sat_obs / sat_plats list entries */
 #define LGPU_MAX_LEVELS 128  /* loc_vtgc level groups */
-#define LGPU_MAX_K 64        /* ensemble size supported by this build */
+#define LGPU_MAX_K 128       /* ensemble size supported by this build */
 
 /* Solver settings: the keys letkf_solver_init reads (src/letkf_solver.F90:86-101).
  * Validation matches :113-125 (0<=rtps<=1, 0<=rtpp<=1, not both, mul>=1). */

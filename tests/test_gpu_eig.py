@@ -59,7 +59,7 @@ def cases(k, rng):
     return out
 
 
-@pytest.mark.parametrize("k", [5, 20, 40, 64])
+@pytest.mark.parametrize("k", [5, 20, 40, 64, 65, 100, 128])
 def test_transform_against_float64(k):
     from letkf_gb300 import Solver
     rng = np.random.default_rng(k)

@@ -223,6 +223,43 @@ def test_auto_variant_choice(name):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
+@pytest.mark.parametrize("k", [65, 99, 100, 128])
+def test_large_ensembles(k):
+    """Ensembles past 64 members: four rows per lane in the eigensolver, up
+    to five register tile sets in the plain Gram, the k > 64 update forms
+    (thread per slab for k a multiple of 4 with one group, the shuffle form
+    for the per-level groups of loc_vtgc and for odd k)."""
+    c1 = workload_cfg("c1")
+    p = workload("c1", k=k)
+    cols = np.arange(0, p.ncol, 53)
+    for gram in ("plain", "batched"):
+        _check_analysis(p, c1["localization"], c1["solver"], cols, label="c1 k=%d %s" % (k, gram), variant=gram)
+
+
+@pytest.mark.parametrize("name", ["c4small", "ocean"])
+def test_k100_workloads(name):
+    """k = 100 (the 0.25-degree configuration's ensemble): clustered obs with
+    one group (thread-per-slab update, 40 KB of transforms) and loc_ocean's
+    two groups (80 KB of transforms in shared memory)."""
+    cfg = workload_cfg(name)
+    gen = {kk: v for kk, v in cfg["gen"].items() if kk != "workload"}
+    if name == "ocean":
+        gen["k"] = 100
+    prob = workload(cfg["gen"]["workload"], **gen)
+    active = np.nonzero(prob.mask == 0)[0]
+    rng = np.random.default_rng(5)
+    cols = rng.choice(active, size=min(300, len(active)), replace=False)
+    if name == "ocean":   # five observations: add the columns within 600 km of one
+        la, lo = np.radians(prob.lat[active])[:, None], np.radians(prob.lon[active])[:, None]
+        ola, olo = np.radians(prob.olat)[None, :], np.radians(prob.olon)[None, :]
+        c = np.sin(la) * np.sin(ola) + np.cos(la) * np.cos(ola) * np.cos(lo - olo)
+        near = active[np.any(np.arccos(np.clip(c, -1, 1)) * 6.371e6 < 6e5, axis=1)]
+        cols = np.concatenate([cols, near[:: max(1, len(near) // 300)]])
+    cols = np.unique(cols)
+    for gram in ("plain", "batched"):
+        _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label="%s k=100" % name, variant=gram)
+
+
 def test_single_observation_closed_form():
     """One obs, one column in range: the GPU mean increment at the observed
     slab equals the scalar Kalman update."""
@@ -286,7 +323,7 @@ def test_errors_and_validation():
             s.set_state(prob.state, prob.mean, prob.sprd, prob.vars)
         assert e.value.code == 6          # state before grid
         s.set_grid(prob.lat, prob.lon, prob.mask)
-        big = np.zeros((prob.ncol, 1, 65), np.float32)
+        big = np.zeros((prob.ncol, 1, 129), np.float32)
         with pytest.raises(LgpuError) as e:
             s.set_state(big, np.zeros((prob.ncol, 1), np.float32), np.zeros((prob.ncol, 1), np.float32),
                         [dict(grid_s_idx=0, levels=1)])

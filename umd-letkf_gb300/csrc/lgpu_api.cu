@@ -109,6 +109,10 @@ int fail(lgpu_handle *h, int code, const std::string &msg) {
 }
 
 int cuda_fail(lgpu_handle *h, cudaError_t e, const char *what) {
+  // a failed runtime call also leaves the thread's last-error state set;
+  // clear it so that the next call's launch checks do not report it again
+  // (a sticky context error stays and is reported by every later call)
+  (void)cudaGetLastError();
   return fail(h, e == cudaErrorMemoryAllocation ? LGPU_ERR_NOMEM : LGPU_ERR_CUDA,
               std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -395,7 +399,7 @@ int prepare_state(lgpu_handle *h, int k, int ns, const float *state, const float
   if (!h->grid_ok) return fail(h, LGPU_ERR_ORDER, "set_state before set_grid");
   if (!state || !mean || !sprd || !vars || nvars <= 0 || ns <= 0) return fail(h, LGPU_ERR_ARG, "set_state: bad arguments");
   if (k < 2) return fail(h, LGPU_ERR_ARG, "ensemble size must be >= 2");
-  if (k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "ensemble size > 64 is not supported by this build");
+  if (k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "ensemble size > 128 is not supported by this build");
   if ((size_t)ns * ((k + 3) & ~3) * 8 > 200 * 1024)
     return fail(h, LGPU_ERR_UNSUPPORTED, "a column's state (ns x k) exceeds the 100 KB the update kernel stages");
   // slab -> (variable, level); every slab must belong to exactly one variable
@@ -1096,7 +1100,7 @@ int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float 
 
 int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, float *trans) {
   if (!h || nunits < 0 || (nunits > 0 && (!gram || !trans))) return LGPU_ERR_ARG;
-  if (k < 2 || k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "debug_transform: k outside [2, 64]");
+  if (k < 2 || k > kMaxK) return fail(h, LGPU_ERR_UNSUPPORTED, "debug_transform: k outside [2, 128]");
   if (nunits == 0) return LGPU_OK;
   CK(cudaSetDevice(h->device), "cudaSetDevice");
   const size_t nf = packed_size(k), nt = (size_t)k * k;

@@ -12,7 +12,8 @@
 // QL iteration with Wilkinson shifts on the tridiagonal matrix (the
 // tql2 scheme of Bowdler, Martin, Reinsch & Wilkinson, Numer. Math. 11,
 // 1968), accumulating the rotations into Z, and back-transformation
-// V = Q Z.  Rows of the k x k work matrices are spread over the 32 lanes;
+// V = Q Z.  Rows of the k x k work matrices are spread over the 32 lanes
+// (lane + 32 q: two per lane for k <= 64, four for k <= 128);
 // the QL scalar recurrence is evaluated redundantly by every lane (shared
 // memory broadcasts) with lane 0 as the only writer.
 #include "lgpu_internal.cuh"
@@ -61,7 +62,9 @@ __device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork &W,
 }
 
 // Householder tridiagonalisation (d, e, tau; reflector vectors in the
-// columns of A) and Q formed in place
+// columns of A) and Q formed in place.  NQ: rows / columns per lane
+// (lane + 32 q, q < NQ): 2 for k <= 64, 4 for k <= 128.
+template <int NQ>
 __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
   const int ld = k + 1;
   float *A = W.A, *d = W.d, *e = W.e, *tau = W.tau, *p = W.p, *w = W.w;
@@ -122,14 +125,15 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
   // ---- Q = H_0 H_1 ... H_{k-3} formed in place, last reflector first: the
   // trailing block [j+1:, j+1:] holds H_{j+1}..H_{k-3} (identity on row and
   // column j+1); v_j is still in column j, outside the block.  Each lane owns
-  // columns lane and lane + 32.
+  // columns lane + 32 q.
   {
-    const bool two = lane + 32 < k;
-    const int c0 = lane, c1 = two ? lane + 32 : lane;
     for (int j = k - 2; j >= 0; j--) {
       // identity on row and column j + 1 of the block
-      if (c0 > j + 1 && c0 < k) { A[(j + 1) * ld + c0] = 0.0f; A[c0 * ld + (j + 1)] = 0.0f; }
-      if (two && c1 > j + 1) { A[(j + 1) * ld + c1] = 0.0f; A[c1 * ld + (j + 1)] = 0.0f; }
+#pragma unroll
+      for (int q = 0; q < NQ; q++) {
+        const int c = lane + 32 * q;
+        if (c > j + 1 && c < k) { A[(j + 1) * ld + c] = 0.0f; A[c * ld + (j + 1)] = 0.0f; }
+      }
       if (lane == 0) A[(j + 1) * ld + (j + 1)] = 1.0f;
       __syncwarp();
       if (j > k - 3) continue;                 // the last block (2 x 2) has no reflector
@@ -137,26 +141,37 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
       if (t == 0.0f) continue;
       const int m = k - j - 1;
       // w_c = t * sum_r v_r Q[r][c]; Q[r][c] -= v_r w_c  (rows, columns j+1..k-1)
-      float w0 = 0.0f, w1 = 0.0f;
-      const bool in0 = c0 > j && c0 < k, in1 = two && c1 > j;
+      float wc[NQ];
+      bool in[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; q++) {
+        const int c = lane + 32 * q;
+        wc[q] = 0.0f;
+        in[q] = c > j && c < k;
+      }
       for (int r = 0; r < m; r++) {
         const float v = A[(j + 1 + r) * ld + j];
-        if (in0) w0 = __fmaf_rn(v, A[(j + 1 + r) * ld + c0], w0);
-        if (in1) w1 = __fmaf_rn(v, A[(j + 1 + r) * ld + c1], w1);
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+          if (in[q]) wc[q] = __fmaf_rn(v, A[(j + 1 + r) * ld + lane + 32 * q], wc[q]);
       }
-      w0 *= t;
-      w1 *= t;
+#pragma unroll
+      for (int q = 0; q < NQ; q++) wc[q] *= t;
       __syncwarp();
       for (int r = 0; r < m; r++) {
         const float v = A[(j + 1 + r) * ld + j];
-        if (in0) A[(j + 1 + r) * ld + c0] -= v * w0;
-        if (in1) A[(j + 1 + r) * ld + c1] -= v * w1;
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+          if (in[q]) A[(j + 1 + r) * ld + lane + 32 * q] -= v * wc[q];
       }
       __syncwarp();
     }
     // row and column 0: Q e_0 = e_0
-    if (c0 > 0 && c0 < k) { A[c0] = 0.0f; A[c0 * ld] = 0.0f; }
-    if (two) { A[c1] = 0.0f; A[c1 * ld] = 0.0f; }
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int c = lane + 32 * q;
+      if (c > 0 && c < k) { A[c] = 0.0f; A[c * ld] = 0.0f; }
+    }
     if (lane == 0) A[0] = 1.0f;
     __syncwarp();
   }
@@ -164,6 +179,7 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
 }
 
 // spectral functions and T = U U^T + wbar 1^T (A holds V, d the eigenvalues)
+template <int NQ>
 __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWork &W, int lane, int &bad) {
   const int k = a.k, ld = k + 1;
   float *A = W.A, *d = W.d, *bv = W.bv, *p = W.p, *w = W.w, *fl = W.fl, *gl = W.gl;
@@ -193,28 +209,33 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
   // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
   for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] *= fl[l]; }
   __syncwarp();
-  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; lane owns columns lane, lane + 32
+  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; lane owns columns lane + 32 q
+  // (a column past k repeats the lane's first column and is not stored)
   float *T = a.T + (size_t)unit * k * k;
   if (lane < k) {
-    const bool two = lane + 32 < k;
-    const int j0 = lane, j1 = two ? lane + 32 : lane;
-    const float *u0 = A + j0 * ld, *u1 = A + j1 * ld;
+    const float *u[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) u[q] = A + (lane + 32 * q < k ? lane + 32 * q : lane) * ld;
     for (int i = 0; i < k; i++) {
       const float *ur = A + i * ld;
-      float acc0 = 0.0f, acc1 = 0.0f;
+      float acc[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; q++) acc[q] = 0.0f;
       for (int l = 0; l < k; l++) {
         const float y = ur[l];
-        acc0 = __fmaf_rn(y, u0[l], acc0);
-        acc1 = __fmaf_rn(y, u1[l], acc1);
+#pragma unroll
+        for (int q = 0; q < NQ; q++) acc[q] = __fmaf_rn(y, u[q][l], acc[q]);
       }
-      T[i * k + j0] = acc0 + w[i];
-      if (two) T[i * k + j1] = acc1 + w[i];
+#pragma unroll
+      for (int q = 0; q < NQ; q++)
+        if (lane + 32 * q < k) T[i * k + lane + 32 * q] = acc[q] + w[i];
     }
   }
 }
 
 // implicit-shift QL on (d, e) with the rotations applied to the columns of
 // A (Q -> V), one warp
+template <int NQ>
 __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &bad) {
   const int ld = k + 1;
   float *A = W.A, *d = W.d, *e = W.e;
@@ -222,12 +243,16 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
   // columns (i, i+1) of Q (V = Q Z).  The scalar recurrence is evaluated
   // redundantly by every lane: d[i+1] is carried in a register and only e[i],
   // d[i] (not yet written in this sweep) are read, so lane 0 alone writes
-  // results, without barriers inside the sweep.  Each lane owns rows lane and
-  // lane + 32 of Q and carries the pending column i+1 of its rows.
+  // results, without barriers inside the sweep.  Each lane owns rows
+  // lane + 32 q of Q and carries the pending column i+1 of its rows.
   {
-    const bool two = lane + 32 < k;
-    const bool own = lane < k;
-    float *q0 = A + (own ? lane : 0) * ld, *q1 = A + (two ? lane + 32 : 0) * ld;
+    bool own[NQ];
+    float *qr[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      own[q] = lane + 32 * q < k;
+      qr[q] = A + (own[q] ? lane + 32 * q : 0) * ld;
+    }
     for (int l = 0; l < k; l++) {
       int iter = 0;
       for (;;) {
@@ -249,14 +274,18 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
         g = d[m] - dl + el / (g + copysignf(r, g));
         float s = 1.0f, c = 1.0f, pp = 0.0f;
         float di1 = d[m];
-        float z0 = own ? q0[m] : 0.0f, z1 = two ? q1[m] : 0.0f;   // pending column i+1
+        float z[NQ];   // pending column i+1
+#pragma unroll
+        for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : 0.0f;
         float ei = e[m - 1], di = d[m - 1];
         int i = m - 1;
         bool deflate = false;
         for (; i >= l; i--) {
           const int in = i > 0 ? i - 1 : 0;
           const float ei_n = e[in], di_n = d[in];           // next step's operands
-          const float a0 = own ? q0[i] : 0.0f, a1 = two ? q1[i] : 0.0f;
+          float av[NQ];
+#pragma unroll
+          for (int q = 0; q < NQ; q++) av[q] = own[q] ? qr[q][i] : 0.0f;
           const float f = s * ei, b = c * ei;
           r = sqrtf(f * f + g * g);
           if (lane == 0) e[i + 1] = r;
@@ -275,14 +304,16 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
           g = c * rr - b;
           di1 = di;
           // rotation (c, s) on columns (i, i+1) of the lane's rows
-          if (own) { q0[i + 1] = s * a0 + c * z0; z0 = c * a0 - s * z0; }
-          if (two) { q1[i + 1] = s * a1 + c * z1; z1 = c * a1 - s * z1; }
+#pragma unroll
+          for (int q = 0; q < NQ; q++)
+            if (own[q]) { qr[q][i + 1] = s * av[q] + c * z[q]; z[q] = c * av[q] - s * z[q]; }
           ei = ei_n;
           di = di_n;
         }
         const int ilo = deflate ? i + 1 : l;
-        if (own) q0[ilo] = z0;
-        if (two) q1[ilo] = z1;
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+          if (own[q]) qr[q][ilo] = z[q];
         if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
         __syncwarp();
       }
@@ -293,6 +324,7 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
 
 }
 
+template <int NQ>
 __global__ void k_eig(EigArgs a, int wpb) {
   extern __shared__ __align__(16) float sm[];
   const int k = a.k, ld = k + 1;
@@ -302,10 +334,10 @@ __global__ void k_eig(EigArgs a, int wpb) {
   if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
   EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
   eig_load(a, unit, W, lane);
-  eig_tridiag_q(k, W, lane);
+  eig_tridiag_q<NQ>(k, W, lane);
   int bad = 0;
-  eig_ql_warp(k, W, lane, bad);
-  eig_transform(a, unit, W, lane, bad);
+  eig_ql_warp<NQ>(k, W, lane, bad);
+  eig_transform<NQ>(a, unit, W, lane, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);
   if (bad && lane == 0) atomicOr(a.status, bad);
 }
@@ -320,6 +352,7 @@ __global__ void k_eig(EigArgs a, int wpb) {
 // The scalar recurrence, which the fused kernel evaluates redundantly on all
 // 32 lanes, runs once per unit.
 
+template <int NQ>
 __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
   const int k = a.k;
@@ -330,7 +363,7 @@ __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   if (a.nkept[unit] <= 0) return;
   EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
   eig_load(a, unit, W, lane);
-  eig_tridiag_q(k, W, lane);
+  eig_tridiag_q<NQ>(k, W, lane);
   const int ld = k + 1;
   float *Q = sp.Q + (size_t)ub * k * k;
   for (int t = lane; t < k * k; t += 32) Q[t] = W.A[(t / k) * ld + (t % k)];
@@ -408,6 +441,7 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
   if (bad) atomicOr(a.status, bad);
 }
 
+template <int NQ>
 __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
   const int k = a.k, ld = k + 1;
@@ -433,13 +467,18 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
     const float *de = sp.DE + (size_t)ub * 2 * k;
     for (int t = lane; t < k; t += 32) { W.d[t] = de[t]; W.e[t] = de[k + t]; }
     __syncwarp();
-    eig_ql_warp(k, W, lane, bad);
+    eig_ql_warp<NQ>(k, W, lane, bad);
   } else {
-    // replay the rotations on the lane's rows (lane, lane + 32); the log is
+    // replay the rotations on the lane's rows (lane + 32 q); the log is
     // read 32 entries at a time (lane j holds entry base + j) and broadcast
     const float2 *lg = sp.log + (size_t)ub * sp.cap;
-    const bool two = lane + 32 < k, own = lane < k;
-    float *q0 = A + (own ? lane : 0) * ld, *q1 = A + (two ? lane + 32 : 0) * ld;
+    bool own[NQ];
+    float *qr[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      own[q] = lane + 32 * q < k;
+      qr[q] = A + (own[q] ? lane + 32 * q : 0) * ld;
+    }
     int base = 0;
     float2 cur = lane < total ? lg[lane] : make_float2(0.f, 0.f);
     float2 nxt = lane + 32 < total ? lg[32 + lane] : make_float2(0.f, 0.f);
@@ -459,21 +498,26 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
       const float2 h = get(pidx++);
       const int m = __float_as_int(h.x), cnt = __float_as_int(h.y);
       if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + cnt > total) { bad |= 1; break; }   // malformed log
-      float z0 = own ? q0[m] : 0.0f, z1 = two ? q1[m] : 0.0f;
+      float z[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : 0.0f;
       for (int r = 0; r < cnt; r++) {
         const float2 cs = get(pidx++);
         const float c = cs.x, s = cs.y;
         const int i = m - 1 - r;
-        const float a0 = own ? q0[i] : 0.0f, a1 = two ? q1[i] : 0.0f;
-        if (own) { q0[i + 1] = s * a0 + c * z0; z0 = c * a0 - s * z0; }
-        if (two) { q1[i + 1] = s * a1 + c * z1; z1 = c * a1 - s * z1; }
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+          const float av = own[q] ? qr[q][i] : 0.0f;
+          if (own[q]) { qr[q][i + 1] = s * av + c * z[q]; z[q] = c * av - s * z[q]; }
+        }
       }
-      if (own) q0[m - cnt] = z0;
-      if (two) q1[m - cnt] = z1;
+#pragma unroll
+      for (int q = 0; q < NQ; q++)
+        if (own[q]) qr[q][m - cnt] = z[q];
     }
   }
   __syncwarp();
-  eig_transform(a, unit, W, lane, bad);
+  eig_transform<NQ>(a, unit, W, lane, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);
   if (bad && lane == 0) atomicOr(a.status, bad);
 }
@@ -509,10 +553,13 @@ cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &
   if (ucount <= 0) return cudaSuccess;
   const int wpb = eig_wpb(a.k);
   const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
+  const bool wide = a.k > 64;
+  auto tri = wide ? k_eig_tri<4> : k_eig_tri<2>;
+  auto vec = wide ? k_eig_vec<4> : k_eig_vec<2>;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_eig_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(k_eig_vec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(vec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
     return e;
   const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
   if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
@@ -520,9 +567,9 @@ cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &
   const int uend = ustart + ucount;
   for (int u0 = ustart; u0 < uend; u0 += batch) {
     const int nb = uend - u0 < batch ? uend - u0 : batch;
-    k_eig_tri<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
+    tri<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
-    k_eig_vec<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
+    vec<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
     (*launches) += 3;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -566,10 +613,11 @@ cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches) {
   const int wpb = eig_wpb(a.k);
   const size_t per = (size_t)eig_floats_per_warp(a.k) * sizeof(float);
   const size_t smem = (size_t)wpb * per;
-  cudaError_t e = cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto fused = a.k > 64 ? k_eig<4> : k_eig<2>;
+  cudaError_t e = cudaFuncSetAttribute(fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int grid = (a.nunits + wpb - 1) / wpb;
-  k_eig<<<grid, 32 * wpb, smem, st>>>(a, wpb);
+  fused<<<grid, 32 * wpb, smem, st>>>(a, wpb);
   (*launches)++;
   return cudaGetLastError();
 }

@@ -45,7 +45,10 @@ struct __align__(16) GramSmem {
   int ncand_chunk;
 };
 
-template <bool TWO>
+// NSET register tile sets per thread: 1 while the k x (k+1) block has at most
+// GT 4x4 tiles (k <= 60), else ceil(tiles / GT) with thread t owning tiles
+// t, t + GT, ... (k <= 128: at most 5 sets)
+template <int NSET>
 __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
   extern __shared__ __align__(16) float dyn[];
   __shared__ GramSmem S;
@@ -62,9 +65,15 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
   const int tile = gram_thread ? tid % ntiles : 0;
   const int slice = gram_thread ? tid / ntiles : 0;
   const int mi = tile / ntn, ni = tile % ntn;
-  // more tiles than threads (k > 60): threads also own tile tid + GT
-  const bool tile2 = TWO && ntiles > GT && tid + GT < ntiles;
-  const int mi2 = tile2 ? (tid + GT) / ntn : 0, ni2 = tile2 ? (tid + GT) % ntn : 0;
+  // more tiles than threads (k > 60): threads also own tiles tid + s GT
+  int mix[NSET > 1 ? NSET : 1], nix[NSET > 1 ? NSET : 1];
+  bool tset[NSET > 1 ? NSET : 1];
+#pragma unroll
+  for (int q = 1; q < NSET; q++) {
+    tset[q] = ntiles > GT && tid + q * GT < ntiles;
+    mix[q] = tset[q] ? (tid + q * GT) / ntn : 0;
+    nix[q] = tset[q] ? (tid + q * GT) % ntn : 0;
+  }
 
   for (int unit = blockIdx.x; unit < a.nunits; unit += gridDim.x) {
     const int act = unit / a.groups, g = unit % a.groups;
@@ -147,15 +156,17 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
     const int total = S.total;
 
     // ---- 2. stream candidates, localize, compact, accumulate
-    float acc[4][4], acc2[TWO ? 4 : 1][4];
+    float acc[4][4], accx[NSET > 1 ? NSET : 1][4][4];
 #pragma unroll
     for (int r = 0; r < 4; r++)
 #pragma unroll
       for (int c = 0; c < 4; c++) acc[r][c] = 0.0f;
 #pragma unroll
-    for (int r = 0; r < (TWO ? 4 : 1); r++)
+    for (int q = 1; q < NSET; q++)
 #pragma unroll
-      for (int c = 0; c < 4; c++) acc2[r][c] = 0.0f;
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) accx[q][r][c] = 0.0f;
     int head = 0, tail = 0;          // ring indices (monotone)
     int ncand = 0, nkept = 0;        // block totals
     float rsum = 0.0f;               // per-thread partial sum of kept weights
@@ -260,9 +271,11 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
 #pragma unroll
               for (int c = 0; c < 4; c++) acc[r2][c] = __fmaf_rn(ar[r2], br[c], acc[r2][c]);
           }
-          if constexpr (TWO) if (tile2) {
-            const float *ap2 = As + 4 * mi2;
-            const float *bp2 = Bs + 4 * ni2;
+#pragma unroll
+          for (int q = 1; q < NSET; q++) {
+            if (!tset[q]) continue;
+            const float *ap2 = As + 4 * mix[q];
+            const float *bp2 = Bs + 4 * nix[q];
             for (int e = 0; e < cnt; e++) {
               const float4 av = *reinterpret_cast<const float4 *>(ap2 + e * kp);
               const float4 bv = *reinterpret_cast<const float4 *>(bp2 + e * kb);
@@ -271,7 +284,7 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
 #pragma unroll
               for (int r2 = 0; r2 < 4; r2++)
 #pragma unroll
-                for (int c = 0; c < 4; c++) acc2[TWO ? r2 : 0][c] = __fmaf_rn(ar[r2], br[c], acc2[TWO ? r2 : 0][c]);
+                for (int c = 0; c < 4; c++) accx[q][r2][c] = __fmaf_rn(ar[r2], br[c], accx[q][r2][c]);
             }
           }
         }
@@ -294,11 +307,13 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
       }
       __syncthreads();
     }
-    if constexpr (TWO) if (tile2) {
+#pragma unroll
+    for (int q = 1; q < NSET; q++) {
+      if (!tset[q]) continue;
 #pragma unroll
       for (int r2 = 0; r2 < 4; r2++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) red[(tid + GT) * 16 + r2 * 4 + c] = acc2[TWO ? r2 : 0][c];
+        for (int c = 0; c < 4; c++) red[(tid + q * GT) * 16 + r2 * 4 + c] = accx[q][r2][c];
     }
     __syncthreads();
     float *G = a.G + (size_t)unit * packed_size(k);
@@ -403,22 +418,37 @@ size_t gram_smem_bytes(int k) {
   const int kp = (k + 3) & ~3;
   const int ntn = (k + 1 + 3) / 4;
   const int kb = 4 * ntn > kp ? 4 * ntn : kp;
-  return sizeof(float) * (size_t)BUF * (kp + kb);
+  const size_t stage = (size_t)BUF * (kp + kb);        // A and B staging rows
+  const size_t red = (size_t)(kp / 4) * ntn * 16;      // the tile reduction reuses the area
+  return sizeof(float) * (stage > red ? stage : red);
+}
+
+static int gram_sets(int k) {
+  const int kp = (k + 3) & ~3;
+  const int ntiles = (kp / 4) * ((k + 1 + 3) / 4);
+  return ntiles <= GT ? 1 : (ntiles + GT - 1) / GT;
+}
+
+template <int NSET>
+static cudaError_t launch_gram_t(cudaStream_t st, const GramArgs &a, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_gram<NSET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_gram<NSET><<<a.nunits, GT, smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_gram(cudaStream_t st, const GramArgs &a, int *launches) {
   if (a.nunits <= 0) return cudaSuccess;
   const size_t smem = gram_smem_bytes(a.k);
-  const int kp = (a.k + 3) & ~3;
-  const bool two = (kp / 4) * ((a.k + 1 + 3) / 4) > GT;
-  cudaError_t e = two ? cudaFuncSetAttribute(k_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                      : cudaFuncSetAttribute(k_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  int grid = a.nunits;
-  if (two) k_gram<true><<<grid, GT, smem, st>>>(a);
-  else k_gram<false><<<grid, GT, smem, st>>>(a);
   (*launches)++;
-  return cudaGetLastError();
+  switch (gram_sets(a.k)) {
+  case 1: return launch_gram_t<1>(st, a, smem);
+  case 2: return launch_gram_t<2>(st, a, smem);
+  case 3: return launch_gram_t<3>(st, a, smem);
+  case 4: return launch_gram_t<4>(st, a, smem);
+  case 5: return launch_gram_t<5>(st, a, smem);
+  default: return cudaErrorInvalidValue;   // k > 128 is rejected at set-up
+  }
 }
 
 cudaError_t launch_obslist(cudaStream_t st, int col, int gid, int group_slot, const ColPar *cp_col, const DevLoc &loc,

@@ -702,14 +702,14 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
 }
 
 // Stage / ring depths: three operand stages when they fit beside three record
-// slots, else two stages and eight slots.
+// slots, else two stages and six slots (k <= 128: 2 x 70 KB + 6 x 10.8 KB).
 void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem) {
   const size_t PB = (size_t)(np / 8) * SBO;
   const size_t stage = 2 * WB + 2 * PB;
   const size_t cb = record_bytes(k);
 
   if (3 * stage + 3 * cb <= kSmemBudget) { *ns = 3; *nr = 3; }
-  else { *ns = 2; *nr = 8; }
+  else { *ns = 2; *nr = 6; }
   *smem = (size_t)*ns * stage + (size_t)*nr * cb;
 }
 
@@ -775,19 +775,19 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
     // first pass computes the weights and caches them; later passes read them
     a.pass0 = 0;
     a.npl = 1;
-    e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 1>(st, a, smem, per_pass) : launch_gram_tc_t<LOC, 2, 8, 1>(st, a, smem, per_pass);
+    e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 1>(st, a, smem, per_pass) : launch_gram_tc_t<LOC, 2, 6, 1>(st, a, smem, per_pass);
     if (e != cudaSuccess) return e;
     a.pass0 = 1;
     a.npl = a.npass - 1;
     e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 2>(st, a, smem, per_pass * a.npl)
-                : launch_gram_tc_t<LOC, 2, 8, 2>(st, a, smem, per_pass * a.npl);
+                : launch_gram_tc_t<LOC, 2, 6, 2>(st, a, smem, per_pass * a.npl);
     (*launches) += 2;
     return e;
   }
   a.pass0 = 0;
   a.npl = a.npass;
   e = ns == 3 ? launch_gram_tc_t<LOC, 3, 3, 0>(st, a, smem, per_pass * a.npass)
-              : launch_gram_tc_t<LOC, 2, 8, 0>(st, a, smem, per_pass * a.npass);
+              : launch_gram_tc_t<LOC, 2, 6, 0>(st, a, smem, per_pass * a.npass);
   (*launches)++;
   return e;
 }

@@ -33,25 +33,41 @@ __device__ __forceinline__ int slab_group(const UpdateArgs &a, int lev, int mld)
   return 0;
 }
 
-// Epilogue of one slab, one warp (lane owns members lane and lane + 32):
-// recenter, mean-increment clip, RTPS, RTPP, multiplicative inflation,
-// member bounds and re-mean, spread; writes the analysis members, mean and
-// spread of (col, s).  xr: X_b T row, br: background perturbation row.
+// Epilogue of one slab, one warp (lane owns members lane + 32 q, q < NQ:
+// NQ = 2 for k <= 64, 4 for k <= 128): recenter, mean-increment clip, RTPS,
+// RTPP, multiplicative inflation, member bounds and re-mean, spread; writes
+// the analysis members, mean and spread of (col, s).  xr: X_b T row, br:
+// background perturbation row.
+template <int NQ>
 __device__ __forceinline__ void slab_epilogue(const UpdateArgs &a, int col, int s, const float *xr, const float *br,
                                               int lane) {
   const int k = a.k, ns = a.ns;
   const float kf = (float)k, km1 = (float)(k - 1);
   const size_t cbase = (size_t)col * ns * k;
   const int v = a.slab_var[s];
-  const int j0 = lane, j1 = lane + 32;
-  float x0 = j0 < k ? xr[j0] : 0.0f, x1 = j1 < k ? xr[j1] : 0.0f;
-  const float xb0 = j0 < k ? br[j0] : 0.0f, xb1 = j1 < k ? br[j1] : 0.0f;
+  float x[NQ], xb[NQ];
+  bool on[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int j = lane + 32 * q;
+    on[q] = j < k;
+    x[q] = on[q] ? xr[j] : 0.0f;
+    xb[q] = on[q] ? br[j] : 0.0f;
+  }
+  auto lsum = [&](auto f) {
+    float t = f(0);
+#pragma unroll
+    for (int q = 1; q < NQ; q++) t = t + f(q);
+    return bsum(t);
+  };
   const float mb = a.mean_b[(size_t)col * ns + s], sb = a.sprd_b[(size_t)col * ns + s];
-  if (j0 < k) x0 = x0 + mb;
-  if (j1 < k) x1 = x1 + mb;
-  float m = bsum(x0 + x1) / kf;
-  if (j0 < k) x0 = x0 - m;
-  if (j1 < k) x1 = x1 - m;
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+    if (on[q]) x[q] = x[q] + mb;
+  float m = lsum([&](int q) { return x[q]; }) / kf;
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+    if (on[q]) x[q] = x[q] - m;
   const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
   {
     float r = m - mb;
@@ -60,29 +76,36 @@ __device__ __forceinline__ void slab_epilogue(const UpdateArgs &a, int col, int 
     m = r + mb;
   }
   if (a.rtps > 0.0f) {
-    const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
+    const float sa = sqrtf(lsum([&](int q) { return x[q] * x[q]; }) / km1);
     if (sa > 0.0f) {
       const float f = a.rtps * (sb - sa) / sa + 1.0f;
-      x0 = x0 * f; x1 = x1 * f;
+#pragma unroll
+      for (int q = 0; q < NQ; q++) x[q] = x[q] * f;
     }
   }
   if (a.rtpp > 0.0f) {
-    x0 = a.rtpp * xb0 + (1.0f - a.rtpp) * x0;
-    x1 = a.rtpp * xb1 + (1.0f - a.rtpp) * x1;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) x[q] = a.rtpp * xb[q] + (1.0f - a.rtpp) * x[q];
   }
-  if (a.mul != 1.0f) { x0 = x0 * a.mul; x1 = x1 * a.mul; }
+  if (a.mul != 1.0f) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) x[q] = x[q] * a.mul;
+  }
   {
-    if (j0 < k) { x0 = fmaxf(x0, lb - m); x0 = fminf(x0, ub - m); }
-    if (j1 < k) { x1 = fmaxf(x1, lb - m); x1 = fminf(x1, ub - m); }
-    const float r = bsum(x0 + x1) / kf;
-    if (j0 < k) x0 = x0 - r;
-    if (j1 < k) x1 = x1 - r;
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+      if (on[q]) { x[q] = fmaxf(x[q], lb - m); x[q] = fminf(x[q], ub - m); }
+    const float r = lsum([&](int q) { return x[q]; }) / kf;
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+      if (on[q]) x[q] = x[q] - r;
     m = m + r;
   }
-  const float sa = sqrtf(bsum(x0 * x0 + x1 * x1) / km1);
+  const float sa = sqrtf(lsum([&](int q) { return x[q] * x[q]; }) / km1);
   float *out = a.ana + cbase + (size_t)s * k;
-  if (j0 < k) out[j0] = x0 + m;
-  if (j1 < k) out[j1] = x1 + m;
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+    if (on[q]) out[lane + 32 * q] = x[q] + m;
   if (lane == 0) {
     a.mean_a[(size_t)col * ns + s] = m;
     a.sprd_a[(size_t)col * ns + s] = sa;
@@ -91,6 +114,7 @@ __device__ __forceinline__ void slab_epilogue(const UpdateArgs &a, int col, int 
 }
 
 // smem: xb [ns][kp], xa [ns][kp], T [tg][k][kp]
+template <int NQ>
 __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int kp) {
   extern __shared__ __align__(16) float sm[];
   const int col = a.col0 + blockIdx.x;
@@ -175,7 +199,7 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int
   }
   __syncthreads();
   // ---- epilogue, one warp per slab
-  for (int s = warp; s < ns; s += nw) slab_epilogue(a, col, s, xa + (size_t)s * kp, xb + (size_t)s * kp, lane);
+  for (int s = warp; s < ns; s += nw) slab_epilogue<NQ>(a, col, s, xa + (size_t)s * kp, xb + (size_t)s * kp, lane);
 }
 
 // Thread-per-slab form for k a multiple of 4 (k <= KMAX): one CTA per
@@ -322,13 +346,20 @@ __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   if (a.ncol <= 0 || a.ncols <= 0) return cudaSuccess;
   const size_t tbytes = (size_t)a.groups * a.k * a.k * sizeof(float);
-  if (a.k % 4 == 0 && a.ns <= 256 && tbytes <= 48 * 1024) {
+  if (a.k % 4 == 0 && a.ns <= 256 && tbytes <= 160 * 1024) {
     const int nt = (a.ns + 31) & ~31;
+    auto kern = a.k <= 16   ? k_update_rows<16>
+                : a.k <= 32 ? k_update_rows<32>
+                : a.k <= 48 ? k_update_rows<48>
+                : a.k <= 64 ? k_update_rows<64>
+                : a.k <= 96 ? k_update_rows<96>
+                            : k_update_rows<128>;
+    if (tbytes > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tbytes);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<a.ncols, nt, tbytes, st>>>(a);
     (*launches)++;
-    if (a.k <= 16) k_update_rows<16><<<a.ncols, nt, tbytes, st>>>(a);
-    else if (a.k <= 32) k_update_rows<32><<<a.ncols, nt, tbytes, st>>>(a);
-    else if (a.k <= 48) k_update_rows<48><<<a.ncols, nt, tbytes, st>>>(a);
-    else k_update_rows<64><<<a.ncols, nt, tbytes, st>>>(a);
     return cudaGetLastError();
   }
   const int kp = (a.k + 3) & ~3;
@@ -339,9 +370,10 @@ cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   int tg = a.groups;
   while (tg > 0 && xbytes + tg * per > budget) tg--;
   const size_t smem = xbytes + tg * per;
-  cudaError_t e = cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kern = a.k > 64 ? k_update<4> : k_update<2>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_update<<<a.ncols, UT, smem, st>>>(a, tg, kp);
+  kern<<<a.ncols, UT, smem, st>>>(a, tg, kp);
   (*launches)++;
   return cudaGetLastError();
 }

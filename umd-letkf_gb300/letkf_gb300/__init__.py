@@ -29,7 +29,7 @@ __all__ = ["Solver", "LgpuError", "ConfigError", "normalize_loc", "normalize_sol
 LGPU_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_UNSUPPORTED_LOCALIZER", 5: "ERR_CONFIG",
           6: "ERR_ORDER", 7: "ERR_CAPACITY", 8: "ERR_NONFINITE", 9: "ERR_EIG", 10: "ERR_UNSUPPORTED"}
-MAX_INTERP, MAX_IDS, MAX_LEVELS, MAX_K = 16, 32, 128, 64
+MAX_INTERP, MAX_IDS, MAX_LEVELS, MAX_K = 16, 32, 128, 128
 
 FP = ctypes.POINTER(ctypes.c_float)
 IP = ctypes.POINTER(ctypes.c_int)

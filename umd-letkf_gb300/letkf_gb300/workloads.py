@@ -8,13 +8,16 @@ sections a reference YAML configuration would carry for them.
             200 km (poles), default inflation
   c3        720x360x40 ocean, k=32 (or 64), 500,000 clustered obs, loc_novrt
             with a constant 60 km length scale (support ~219 km)
+  c4        1440x720x50 (T, S; 100 slabs), k=100, 1,000,000 clustered obs,
+            loc_novrt 60 km as c3
   c2mid     c2 observations on a 360x180x10 grid (profiling-sized: the same
             local observation counts per column, a fifth of the columns)
   simple3d  test/simple3d-style (k=50, three 3-D variables, two synthetic
             obs, loc_novrt 500 km -> 50 km)
   ocean     test/ocean/vtloc-style (k=10, T/S/u/v, five synthetic obs,
             loc_ocean with the mixed-layer split)
-  c2small / c1small  reduced grids with the same generators for fast tests
+  c2small / c1small / c3small / c4small  reduced grids with the same
+            generators for fast tests
 """
 
 C2_LOC = {"class": "loc_novrt",
@@ -39,6 +42,14 @@ WORKLOADS = {
                   localization={"class": "loc_novrt",
                                 "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
                   solver={}),
+    "c4": dict(gen=dict(workload="c4"),
+               localization={"class": "loc_novrt",
+                             "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
+               solver={}),
+    "c4small": dict(gen=dict(workload="c4", nx=180, ny=90, nz=5, n_obs=40000),
+                    localization={"class": "loc_novrt",
+                                  "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
+                    solver={}),
     "c3small": dict(gen=dict(workload="c3", nx=180, ny=90, nz=10, n_obs=40000),
                     localization={"class": "loc_novrt",
                                   "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
