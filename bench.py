@@ -336,13 +336,14 @@ def gpu_arm(args, dist):
         refill()
         e2e_step()
     dist.barrier()
-    et = []
+    et, ev = [], []
     for _ in range(args.steps):
         refill()
         s.flush_l2(256 << 20)
         t0 = time.perf_counter()
         e2e_step()
         et.append(time.perf_counter() - t0)
+        ev.append(s.timings()["variant"])
     dist.barrier()
     e2e_ms = dist.max(1000.0 * statistics.mean(et))
     e2e_val = dist.world * nact / (e2e_ms / 1000.0)
@@ -355,7 +356,8 @@ def gpu_arm(args, dist):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no public dataset)",
             "config": workload_config(args, prob, cfg), "clocks": ck, "gpu_launches": launches * args.steps,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": e2e_ms},
+                    "ms_per_step": e2e_ms, "step_ms": [round(1000.0 * t, 3) for t in et],
+                    "variant": [{1: "plain", 2: "batched_tc"}.get(v, "?") for v in ev]},
             "roofline": roof, "stages": stages, "analysis_finite": ok, "variant": variant, "plain_variant": plain}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         rate, n, nth, dt = cpu_rate(prob, cfg)

@@ -966,6 +966,7 @@ int lgpu_solver_run(lgpu_handle *h) {
   if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");
   if (status & 4) return fail(h, LGPU_ERR_NONFINITE, "non-finite analysis mean or spread");
   if (status & 16) return fail(h, LGPU_ERR_CUDA, "tensor-core pipeline wait timed out");
+  if (status & 32) return fail(h, LGPU_ERR_CUDA, "internal: malformed eigensolver rotation log");
   return LGPU_OK;
 }
 
@@ -1124,6 +1125,7 @@ int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, f
   if (e != cudaSuccess) return cuda_fail(h, e, "debug_transform");
   if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
   if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");
+  if (status & 32) return fail(h, LGPU_ERR_CUDA, "internal: malformed eigensolver rotation log");
   return LGPU_OK;
 }
 

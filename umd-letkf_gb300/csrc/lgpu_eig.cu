@@ -12,10 +12,12 @@
 // QL iteration with Wilkinson shifts on the tridiagonal matrix (the
 // tql2 scheme of Bowdler, Martin, Reinsch & Wilkinson, Numer. Math. 11,
 // 1968), accumulating the rotations into Z, and back-transformation
-// V = Q Z.  Rows of the k x k work matrices are spread over the 32 lanes
-// (lane + 32 q: two per lane for k <= 64, four for k <= 128);
-// the QL scalar recurrence is evaluated redundantly by every lane (shared
-// memory broadcasts) with lane 0 as the only writer.
+// V = Q Z.  A unit is worked on by a team: one warp for k <= 64, two warps
+// (one unit per CTA) for k <= 128; rows of the k x k work matrices are
+// spread over the team's threads (tt + TS q, two per thread).  The fused
+// kernel evaluates the QL scalar recurrence redundantly on every lane of its
+// warp (shared memory broadcasts) with lane 0 as the only writer; the split
+// pipeline runs it once per unit and replays the logged rotations.
 #include "lgpu_internal.cuh"
 
 namespace lgpu {
@@ -32,6 +34,36 @@ __host__ __device__ __forceinline__ int eig_floats_per_warp(int k) {
   return k * ld + 8 * k + 8;
 }
 
+// A team of NW warps works on one unit: thread tt of TS = 32 NW owns rows /
+// columns tt + TS q of the work matrices.  NW = 1 is one warp per unit
+// (several units per CTA); NW > 1 is one unit per CTA, so the CTA barrier is
+// the team barrier.  Sums run over the warp's butterfly, then over the warps
+// in warp order (deterministic).
+template <int NW>
+struct Team {
+  static constexpr int TS = 32 * NW;
+  int tt, lane, warp;
+  float *red;   // NW floats in shared memory (NW > 1)
+  __device__ __forceinline__ void sync() const {
+    if constexpr (NW == 1) __syncwarp();
+    else __syncthreads();
+  }
+  __device__ __forceinline__ float sum(float v) const {
+    v = wsum(v);
+    if constexpr (NW == 1) {
+      return v;
+    } else {
+      if (lane == 0) red[warp] = v;
+      __syncthreads();
+      float t = red[0];
+#pragma unroll
+      for (int q = 1; q < NW; q++) t += red[q];
+      __syncthreads();
+      return t;
+    }
+  }
+};
+
 // Work arrays of one unit in shared memory: A (k x ld, ld = k + 1) holds A,
 // then Q, then V; then d, e, tau, bv, p, w, fl, gl (k each).
 struct EigWork {
@@ -44,65 +76,66 @@ struct EigWork {
 };
 
 // A = G + (k-1)/infl I from the packed Gram block, b from its tail
-__device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork &W, int lane) {
-  const int k = a.k, ld = k + 1;
+template <int NW>
+__device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork &W, const Team<NW> &T) {
+  const int k = a.k, ld = k + 1, tt = T.tt, TS = T.TS;
   float *A = W.A, *bv = W.bv;
   const float *G = a.G + (size_t)unit * packed_size(k);
   // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
   const float shift = (float)(k - 1) * 1.0f / a.infl;
-  for (int t = lane; t < k * k; t += 32) {
+  for (int t = tt; t < k * k; t += TS) {
     const int i = t / k, j = t % k;
     float v = (i <= j) ? G[tri_idx(i, j, k)] : G[tri_idx(j, i, k)];
     if (i == j) v += shift;
     A[i * ld + j] = v;
   }
-  for (int i = lane; i < k; i += 32) bv[i] = G[k * (k + 1) / 2 + i];
-  __syncwarp();
+  for (int i = tt; i < k; i += TS) bv[i] = G[k * (k + 1) / 2 + i];
+  T.sync();
 
 }
 
 // Householder tridiagonalisation (d, e, tau; reflector vectors in the
 // columns of A) and Q formed in place.  NQ: rows / columns per lane
-// (lane + 32 q, q < NQ): 2 for k <= 64, 4 for k <= 128.
-template <int NQ>
-__device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
-  const int ld = k + 1;
+// (tt + TS q, q < NQ).
+template <int NQ, int NW>
+__device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> &T) {
+  const int ld = k + 1, tt = T.tt, TS = T.TS;
   float *A = W.A, *d = W.d, *e = W.e, *tau = W.tau, *p = W.p, *w = W.w;
   // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j];
   // its vector v_j = A[j+1:, j] stays in column j
   for (int j = 0; j < k - 2; j++) {
     const int m = k - j - 1;                 // length of x = A[j+1:, j]
     float s = 0.0f;
-    for (int r = lane; r < m; r += 32) { float x = A[(j + 1 + r) * ld + j]; s += x * x; }
-    const float sig = wsum(s);
+    for (int r = tt; r < m; r += TS) { float x = A[(j + 1 + r) * ld + j]; s += x * x; }
+    const float sig = T.sum(s);
     const float x0 = A[(j + 1) * ld + j];
     const float s1 = sig - x0 * x0;
     if (!(s1 > 1e-30f * sig) || sig == 0.0f) {
-      if (lane == 0) { tau[j] = 0.0f; e[j] = x0; d[j] = A[j * ld + j]; }
-      __syncwarp();
+      if (tt == 0) { tau[j] = 0.0f; e[j] = x0; d[j] = A[j * ld + j]; }
+      T.sync();
       continue;
     }
     const float alpha = -copysignf(sqrtf(sig), x0);
     const float v0 = x0 - alpha;
     const float t = 2.0f / (v0 * v0 + s1);
-    __syncwarp();
-    if (lane == 0) { A[(j + 1) * ld + j] = v0; tau[j] = t; e[j] = alpha; d[j] = A[j * ld + j]; }
-    __syncwarp();
+    T.sync();
+    if (tt == 0) { A[(j + 1) * ld + j] = v0; tau[j] = t; e[j] = alpha; d[j] = A[j * ld + j]; }
+    T.sync();
     // p = t * A22 v
-    for (int r = lane; r < m; r += 32) {
+    for (int r = tt; r < m; r += TS) {
       const float *row = A + (j + 1 + r) * ld + (j + 1);
       float acc = 0.0f;
       for (int c = 0; c < m; c++) acc = __fmaf_rn(row[c], A[(j + 1 + c) * ld + j], acc);
       p[r] = t * acc;
     }
-    __syncwarp();
+    T.sync();
     float pv = 0.0f;
-    for (int r = lane; r < m; r += 32) pv = __fmaf_rn(p[r], A[(j + 1 + r) * ld + j], pv);
-    const float beta = 0.5f * t * wsum(pv);
-    for (int r = lane; r < m; r += 32) w[r] = p[r] - beta * A[(j + 1 + r) * ld + j];
-    __syncwarp();
+    for (int r = tt; r < m; r += TS) pv = __fmaf_rn(p[r], A[(j + 1 + r) * ld + j], pv);
+    const float beta = 0.5f * t * T.sum(pv);
+    for (int r = tt; r < m; r += TS) w[r] = p[r] - beta * A[(j + 1 + r) * ld + j];
+    T.sync();
     // A22 -= v w^T + w v^T
-    for (int r = lane; r < m; r += 32) {
+    for (int r = tt; r < m; r += TS) {
       float *row = A + (j + 1 + r) * ld + (j + 1);
       const float vr = A[(j + 1 + r) * ld + j], wr = w[r];
       for (int c = 0; c < m; c++) {
@@ -110,9 +143,9 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
         row[c] = row[c] - __fmaf_rn(vr, wc, wr * vc);
       }
     }
-    __syncwarp();
+    T.sync();
   }
-  if (lane == 0) {
+  if (tt == 0) {
     if (k >= 2) {
       d[k - 2] = A[(k - 2) * ld + (k - 2)];
       e[k - 2] = A[(k - 1) * ld + (k - 2)];
@@ -120,22 +153,22 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
     d[k - 1] = A[(k - 1) * ld + (k - 1)];
     e[k - 1] = 0.0f;
   }
-  __syncwarp();
+  T.sync();
 
   // ---- Q = H_0 H_1 ... H_{k-3} formed in place, last reflector first: the
   // trailing block [j+1:, j+1:] holds H_{j+1}..H_{k-3} (identity on row and
-  // column j+1); v_j is still in column j, outside the block.  Each lane owns
-  // columns lane + 32 q.
+  // column j+1); v_j is still in column j, outside the block.  Each thread
+  // owns columns tt + TS q.
   {
     for (int j = k - 2; j >= 0; j--) {
       // identity on row and column j + 1 of the block
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
-        const int c = lane + 32 * q;
+        const int c = tt + TS * q;
         if (c > j + 1 && c < k) { A[(j + 1) * ld + c] = 0.0f; A[c * ld + (j + 1)] = 0.0f; }
       }
-      if (lane == 0) A[(j + 1) * ld + (j + 1)] = 1.0f;
-      __syncwarp();
+      if (tt == 0) A[(j + 1) * ld + (j + 1)] = 1.0f;
+      T.sync();
       if (j > k - 3) continue;                 // the last block (2 x 2) has no reflector
       const float t = tau[j];
       if (t == 0.0f) continue;
@@ -145,7 +178,7 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
       bool in[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
-        const int c = lane + 32 * q;
+        const int c = tt + TS * q;
         wc[q] = 0.0f;
         in[q] = c > j && c < k;
       }
@@ -153,69 +186,68 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, int lane) {
         const float v = A[(j + 1 + r) * ld + j];
 #pragma unroll
         for (int q = 0; q < NQ; q++)
-          if (in[q]) wc[q] = __fmaf_rn(v, A[(j + 1 + r) * ld + lane + 32 * q], wc[q]);
+          if (in[q]) wc[q] = __fmaf_rn(v, A[(j + 1 + r) * ld + tt + TS * q], wc[q]);
       }
 #pragma unroll
       for (int q = 0; q < NQ; q++) wc[q] *= t;
-      __syncwarp();
       for (int r = 0; r < m; r++) {
         const float v = A[(j + 1 + r) * ld + j];
 #pragma unroll
         for (int q = 0; q < NQ; q++)
-          if (in[q]) A[(j + 1 + r) * ld + lane + 32 * q] -= v * wc[q];
+          if (in[q]) A[(j + 1 + r) * ld + tt + TS * q] -= v * wc[q];
       }
-      __syncwarp();
+      T.sync();
     }
     // row and column 0: Q e_0 = e_0
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
-      const int c = lane + 32 * q;
+      const int c = tt + TS * q;
       if (c > 0 && c < k) { A[c] = 0.0f; A[c * ld] = 0.0f; }
     }
-    if (lane == 0) A[0] = 1.0f;
-    __syncwarp();
+    if (tt == 0) A[0] = 1.0f;
+    T.sync();
   }
 
 }
 
 // spectral functions and T = U U^T + wbar 1^T (A holds V, d the eigenvalues)
-template <int NQ>
-__device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWork &W, int lane, int &bad) {
-  const int k = a.k, ld = k + 1;
+template <int NQ, int NW>
+__device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWork &W, const Team<NW> &TM, int &bad) {
+  const int k = a.k, ld = k + 1, tt = TM.tt, TS = TM.TS;
   float *A = W.A, *d = W.d, *bv = W.bv, *p = W.p, *w = W.w, *fl = W.fl, *gl = W.gl;
   // ---- spectral functions: f = sqrt((k-1)/lambda), g = 1/lambda
   //      (src/letkf_core.F90:111-113, :128-131); fl holds sqrt(f)
-  for (int l = lane; l < k; l += 32) {
+  for (int l = tt; l < k; l += TS) {
     const float lam = d[l];
     if (!(lam > 0.0f)) bad |= 2;
     fl[l] = sqrtf(sqrtf((float)(k - 1) / lam));
     gl[l] = 1.0f / lam;
   }
-  __syncwarp();
+  TM.sync();
   // s_l = g_l * (V^T b)_l
-  for (int l = lane; l < k; l += 32) {
+  for (int l = tt; l < k; l += TS) {
     float acc = 0.0f;
     for (int q = 0; q < k; q++) acc = __fmaf_rn(A[q * ld + l], bv[q], acc);
     p[l] = gl[l] * acc;
   }
-  __syncwarp();
+  TM.sync();
   // wbar_i = sum_l V[i][l] s_l
-  for (int i = lane; i < k; i += 32) {
+  for (int i = tt; i < k; i += TS) {
     float acc = 0.0f;
     for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], p[l], acc);
     w[i] = acc;
   }
-  __syncwarp();
+  TM.sync();
   // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
-  for (int t = lane; t < k * k; t += 32) { const int i = t / k, l = t % k; A[i * ld + l] *= fl[l]; }
-  __syncwarp();
-  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; lane owns columns lane + 32 q
-  // (a column past k repeats the lane's first column and is not stored)
+  for (int t = tt; t < k * k; t += TS) { const int i = t / k, l = t % k; A[i * ld + l] *= fl[l]; }
+  TM.sync();
+  // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; thread owns columns tt + TS q
+  // (a column past k repeats the thread's first column and is not stored)
   float *T = a.T + (size_t)unit * k * k;
-  if (lane < k) {
+  if (tt < k) {
     const float *u[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; q++) u[q] = A + (lane + 32 * q < k ? lane + 32 * q : lane) * ld;
+    for (int q = 0; q < NQ; q++) u[q] = A + (tt + TS * q < k ? tt + TS * q : tt) * ld;
     for (int i = 0; i < k; i++) {
       const float *ur = A + i * ld;
       float acc[NQ];
@@ -228,9 +260,29 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
       }
 #pragma unroll
       for (int q = 0; q < NQ; q++)
-        if (lane + 32 * q < k) T[i * k + lane + 32 * q] = acc[q] + w[i];
+        if (tt + TS * q < k) T[i * k + tt + TS * q] = acc[q] + w[i];
     }
   }
+}
+
+// Deflation test of the QL iteration: e_m is negligible when it is below
+// eps32 of its two diagonal neighbours (the local test of LAPACK's ssteqr /
+// EISPACK's tql2 family) or below eps32 times the norm of the whole
+// tridiagonal matrix (tql2's absolute test).  The second test ends the
+// iteration where rounding at the eps32 ||T|| level (already present in T
+// from the Householder reduction) keeps a strongly graded block from
+// meeting the local test; it leaves the eigenvalues within the backward
+// error the reduction has already made.
+__device__ __forceinline__ bool ql_negligible(float em, float dm, float dm1, float tabs) {
+  const float ae = fabsf(em);
+  return ae <= 1.1920929e-7f * (fabsf(dm) + fabsf(dm1)) || ae <= tabs;
+}
+
+// eps32 * max_i (|d_i| + |e_i|), elements at stride `st`
+__device__ __forceinline__ float ql_abs_tol(int k, const float *d, const float *e, int st) {
+  float an = 0.0f;
+  for (int i = 0; i < k; i++) an = fmaxf(an, fabsf(d[(size_t)i * st]) + fabsf(e[(size_t)i * st]));
+  return 1.1920929e-7f * an;
 }
 
 // implicit-shift QL on (d, e) with the rotations applied to the columns of
@@ -253,6 +305,7 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
       own[q] = lane + 32 * q < k;
       qr[q] = A + (own[q] ? lane + 32 * q : 0) * ld;
     }
+    const float tabs = ql_abs_tol(k, d, e, 1);
     for (int l = 0; l < k; l++) {
       int iter = 0;
       for (;;) {
@@ -262,7 +315,7 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
         for (int base = l; base < k - 1; base += 32) {
           const int mm = base + lane;
           bool small = false;
-          if (mm < k - 1) small = fabsf(e[mm]) <= 1.1920929e-7f * (fabsf(d[mm]) + fabsf(d[mm + 1]));
+          if (mm < k - 1) small = ql_negligible(e[mm], d[mm], d[mm + 1], tabs);
           const unsigned bal = __ballot_sync(0xffffffffu, small);
           if (bal) { m = base + __ffs(bal) - 1; break; }
         }
@@ -327,17 +380,18 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
 template <int NQ>
 __global__ void k_eig(EigArgs a, int wpb) {
   extern __shared__ __align__(16) float sm[];
-  const int k = a.k, ld = k + 1;
+  const int k = a.k;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int unit = blockIdx.x * wpb + warp;
   if (unit >= a.nunits) return;           // whole warps exit; no block-level barriers below
   if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
   EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
-  eig_load(a, unit, W, lane);
-  eig_tridiag_q<NQ>(k, W, lane);
+  const Team<1> T{lane, lane, warp, nullptr};
+  eig_load(a, unit, W, T);
+  eig_tridiag_q<NQ>(k, W, T);
   int bad = 0;
   eig_ql_warp<NQ>(k, W, lane, bad);
-  eig_transform<NQ>(a, unit, W, lane, bad);
+  eig_transform<NQ>(a, unit, W, T, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);
   if (bad && lane == 0) atomicOr(a.status, bad);
 }
@@ -352,23 +406,28 @@ __global__ void k_eig(EigArgs a, int wpb) {
 // The scalar recurrence, which the fused kernel evaluates redundantly on all
 // 32 lanes, runs once per unit.
 
-template <int NQ>
+// NW = 1: wpb units per CTA, one warp each; NW > 1: one unit per CTA of NW
+// warps (wpb = 1)
+template <int NQ, int NW>
 __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
+  __shared__ float tred[NW];
   const int k = a.k;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ub = blockIdx.x * wpb + warp;
+  const int slot = NW == 1 ? warp : 0;
+  const int ub = blockIdx.x * wpb + slot;
   if (ub >= nb) return;
   const int unit = u0 + ub;
   if (a.nkept[unit] <= 0) return;
-  EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
-  eig_load(a, unit, W, lane);
-  eig_tridiag_q<NQ>(k, W, lane);
+  EigWork W(sm + (size_t)slot * eig_floats_per_warp(k), k);
+  const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
+  eig_load(a, unit, W, T);
+  eig_tridiag_q<NQ>(k, W, T);
   const int ld = k + 1;
   float *Q = sp.Q + (size_t)ub * k * k;
-  for (int t = lane; t < k * k; t += 32) Q[t] = W.A[(t / k) * ld + (t % k)];
+  for (int t = T.tt; t < k * k; t += T.TS) Q[t] = W.A[(t / k) * ld + (t % k)];
   float *de = sp.DE + (size_t)ub * 2 * k;
-  for (int t = lane; t < k; t += 32) { de[t] = W.d[t]; de[k + t] = W.e[t]; }
+  for (int t = T.tt; t < k; t += T.TS) { de[t] = W.d[t]; de[k + t] = W.e[t]; }
 }
 
 constexpr int QLT = 64;   // threads (units) per block of k_eig_ql
@@ -385,13 +444,14 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
   if (a.nkept[unit] <= 0) return;
   const float *de = sp.DE + (size_t)ub * 2 * k;
   for (int i = 0; i < k; i++) { D(i) = de[i]; E(i) = de[k + i]; }
+  const float tabs = ql_abs_tol(k, d, e, QLT);
   float2 *lg = sp.log + (size_t)ub * sp.cap;
   int pos = 0, bad = 0;
   for (int l = 0; l < k; l++) {
     int iter = 0;
     for (;;) {
       int m = l;
-      while (m < k - 1 && !(fabsf(E(m)) <= 1.1920929e-7f * (fabsf(D(m)) + fabsf(D(m + 1))))) m++;
+      while (m < k - 1 && !ql_negligible(E(m), D(m), D(m + 1), tabs)) m++;
       if (m == l) break;
       if (++iter > 60) { bad |= 1; break; }
       const float dl = D(l), el = E(l);
@@ -441,43 +501,50 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
   if (bad) atomicOr(a.status, bad);
 }
 
-template <int NQ>
+template <int NQ, int NW>
 __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
+  __shared__ float tred[NW];
   const int k = a.k, ld = k + 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ub = blockIdx.x * wpb + warp;
+  const int slot = NW == 1 ? warp : 0;
+  const int ub = blockIdx.x * wpb + slot;
   if (ub >= nb) return;
   const int unit = u0 + ub;
   if (a.nkept[unit] <= 0) return;
   const int total = sp.logn[ub];
   if (total == -1) return;                // no convergence: status set by k_eig_ql
-  EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
+  EigWork W(sm + (size_t)slot * eig_floats_per_warp(k), k);
+  const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
+  const int tt = T.tt, TS = T.TS;
   float *A = W.A;
   const float *Q = sp.Q + (size_t)ub * k * k;
-  for (int t = lane; t < k * k; t += 32) A[(t / k) * ld + (t % k)] = Q[t];
+  for (int t = tt; t < k * k; t += TS) A[(t / k) * ld + (t % k)] = Q[t];
   const float *lam = sp.lam + (size_t)ub * k;
-  for (int t = lane; t < k; t += 32) W.d[t] = lam[t];
+  for (int t = tt; t < k; t += TS) W.d[t] = lam[t];
   const float *G = a.G + (size_t)unit * packed_size(k);
-  for (int i = lane; i < k; i += 32) W.bv[i] = G[k * (k + 1) / 2 + i];
-  __syncwarp();
+  for (int i = tt; i < k; i += TS) W.bv[i] = G[k * (k + 1) / 2 + i];
+  T.sync();
   int bad = 0;
   if (total < 0) {
-    // the rotation log overflowed: run the QL here from the tridiagonal form
+    // the rotation log overflowed: the first warp runs the QL here from the
+    // tridiagonal form, on all rows
     const float *de = sp.DE + (size_t)ub * 2 * k;
-    for (int t = lane; t < k; t += 32) { W.d[t] = de[t]; W.e[t] = de[k + t]; }
-    __syncwarp();
-    eig_ql_warp<NQ>(k, W, lane, bad);
+    for (int t = tt; t < k; t += TS) { W.d[t] = de[t]; W.e[t] = de[k + t]; }
+    T.sync();
+    constexpr int NQW = 32 * NW * NQ <= 64 ? 2 : 4;
+    if (warp == 0 || NW == 1) eig_ql_warp<NQW>(k, W, lane, bad);
   } else {
-    // replay the rotations on the lane's rows (lane + 32 q); the log is
+    // replay the rotations on the thread's rows (tt + TS q); the log is
     // read 32 entries at a time (lane j holds entry base + j) and broadcast
+    // within each warp
     const float2 *lg = sp.log + (size_t)ub * sp.cap;
     bool own[NQ];
     float *qr[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
-      own[q] = lane + 32 * q < k;
-      qr[q] = A + (own[q] ? lane + 32 * q : 0) * ld;
+      own[q] = tt + TS * q < k;
+      qr[q] = A + (own[q] ? tt + TS * q : 0) * ld;
     }
     int base = 0;
     float2 cur = lane < total ? lg[lane] : make_float2(0.f, 0.f);
@@ -497,7 +564,7 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
     while (pidx < total) {
       const float2 h = get(pidx++);
       const int m = __float_as_int(h.x), cnt = __float_as_int(h.y);
-      if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + cnt > total) { bad |= 1; break; }   // malformed log
+      if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + cnt > total) { bad |= 32; break; }   // malformed log
       float z[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : 0.0f;
@@ -516,8 +583,8 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
         if (own[q]) qr[q][m - cnt] = z[q];
     }
   }
-  __syncwarp();
-  eig_transform<NQ>(a, unit, W, lane, bad);
+  T.sync();
+  eig_transform<NQ>(a, unit, W, T, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);
   if (bad && lane == 0) atomicOr(a.status, bad);
 }
@@ -542,6 +609,40 @@ static int eig_wpb(int k) {
   return wpb;
 }
 
+// warps per unit of the split kernels, measured on GB300 (206k units per
+// analysis): k <= 64 one warp (two rows per lane; k = 40: 26 ms, against 33
+// with two warps), k > 64 two warps (two rows per thread; k = 100: 273 ms,
+// against 414 with one warp and 308 / 359 with four / eight)
+static int eig_team(int k) { return k <= 64 ? 1 : 2; }
+
+template <int NQ, int NW>
+static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart,
+                                  int ucount, int *launches) {
+  const int wpb = NW == 1 ? eig_wpb(a.k) : 1;
+  const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
+  const int threads = NW == 1 ? 32 * wpb : 32 * NW;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_eig_tri<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+      cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_eig_vec<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+      cudaSuccess)
+    return e;
+  const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
+  if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
+    return e;
+  const int uend = ustart + ucount;
+  for (int u0 = ustart; u0 < uend; u0 += batch) {
+    const int nb = uend - u0 < batch ? uend - u0 : batch;
+    k_eig_tri<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
+    k_eig_vec<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    (*launches) += 3;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 int eig_log_cap(int k) { return 2 * k * k + 4 * k + 64; }
 
 size_t eig_split_bytes_per_unit(int k) {
@@ -551,29 +652,9 @@ size_t eig_split_bytes_per_unit(int k) {
 cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart, int ucount,
                              int *launches) {
   if (ucount <= 0) return cudaSuccess;
-  const int wpb = eig_wpb(a.k);
-  const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
-  const bool wide = a.k > 64;
-  auto tri = wide ? k_eig_tri<4> : k_eig_tri<2>;
-  auto vec = wide ? k_eig_vec<4> : k_eig_vec<2>;
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(vec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-    return e;
-  const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
-  if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
-    return e;
-  const int uend = ustart + ucount;
-  for (int u0 = ustart; u0 < uend; u0 += batch) {
-    const int nb = uend - u0 < batch ? uend - u0 : batch;
-    tri<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
-    k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
-    vec<<<(nb + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, sp, wpb, u0, nb);
-    (*launches) += 3;
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  const int k = a.k, nw = eig_team(k);
+  if (nw == 1) return launch_split_t<2, 1>(st, a, sp, batch, ustart, ucount, launches);   // k <= 64
+  return launch_split_t<2, 2>(st, a, sp, batch, ustart, ucount, launches);   // k <= 128
 }
 
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
