@@ -332,7 +332,7 @@ def gpu_arm(args, dist):
                   pin["hx_mean"].array)
         s.run()
 
-    for _ in range(max(1, min(args.warmup, 2))):
+    for _ in range(max(3, args.warmup)):
         refill()
         e2e_step()
     dist.barrier()

@@ -967,6 +967,7 @@ int lgpu_solver_run(lgpu_handle *h) {
   if (status & 4) return fail(h, LGPU_ERR_NONFINITE, "non-finite analysis mean or spread");
   if (status & 16) return fail(h, LGPU_ERR_CUDA, "tensor-core pipeline wait timed out");
   if (status & 32) return fail(h, LGPU_ERR_CUDA, "internal: malformed eigensolver rotation log");
+  if (status & 64) return fail(h, LGPU_ERR_CUDA, "update stage copy wait timed out");
   return LGPU_OK;
 }
 

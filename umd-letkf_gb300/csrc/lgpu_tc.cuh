@@ -98,6 +98,17 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
                : "memory");
 }
 
+// Bulk async copy shared -> global (16-byte aligned addresses, size a
+// multiple of 16), tracked by the issuing thread's bulk async-group.
+__device__ __forceinline__ void bulk_store_s2g(void *dst, const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// all of this thread's committed bulk stores complete (writes performed)
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // 32 lanes x 16 consecutive 32-bit TMEM columns -> 16 registers per thread.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   uint32_t r[16];

@@ -15,6 +15,7 @@
 // four members per thread from float4 rows of T; the epilogue runs one warp
 // per slab with a fixed butterfly order for the member sums.
 #include "lgpu_internal.cuh"
+#include "lgpu_tc.cuh"
 
 namespace lgpu {
 
@@ -203,162 +204,192 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int
 }
 
 // Thread-per-slab form for k a multiple of 4 (k <= KMAX): one CTA per
-// column, thread s owns slab s.  The group transforms are staged in shared
-// memory (broadcast reads); the slab's analysis members stay in registers,
-// so the epilogue's member sums run sequentially in member order (the
-// reference's SUM) without shuffles.
+// column, thread s owns slab s.  The column's background block (ns x k
+// floats, contiguous) and its group transforms arrive in shared memory by
+// two bulk async copies completing on one mbarrier; the slab's analysis
+// members stay in registers, so the epilogue's member sums run sequentially
+// in member order (the reference's SUM) without shuffles; the analysis block
+// is written back over the background block in shared memory and leaves by
+// one bulk async store.  A copy wait that runs out sets status bit 64.
 template <int KMAX>
 __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
-  extern __shared__ __align__(16) float Tsm[];   // [groups][k][k]
+  extern __shared__ __align__(128) float usm[];   // X [ns][k] | T [groups][k][k]
+  __shared__ __align__(8) uint64_t bar;
   const int col = a.col0 + blockIdx.x;
   const int k = a.k, ns = a.ns, G = a.groups, kk = k * k, k4 = k >> 2;
   const int s = threadIdx.x;
   const size_t cbase = (size_t)col * ns * k;
   const int act = a.col2act[col];
   const bool skip = a.mask[col] || act < 0;
-  if (!skip) {
-    for (int g = 0; g < G; g++) {
-      if (a.nkept[(size_t)act * G + g] <= 0) continue;
-      const float4 *src = reinterpret_cast<const float4 *>(a.T + ((size_t)act * G + g) * kk);
-      float4 *dst = reinterpret_cast<float4 *>(Tsm + (size_t)g * kk);
-      for (int t = threadIdx.x; t < (kk >> 2); t += blockDim.x) dst[t] = src[t];
-    }
+  float *Xs = usm;
+  const float *Tsm = usm + (size_t)ns * k;
+  const uint32_t xbytes = (uint32_t)(ns * k * 4), tbytes = skip ? 0u : (uint32_t)(G * kk * 4);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::mbar_fence_init();
   }
   __syncthreads();
-  if (s >= ns) return;
-  const float4 *xb4 = reinterpret_cast<const float4 *>(a.bkg + cbase + (size_t)s * k);
-  float4 *out4 = reinterpret_cast<float4 *>(a.ana + cbase + (size_t)s * k);
-  const size_t ms = (size_t)col * ns + s;
-  if (skip) {   // src/letkf_solver.F90:207
-    for (int q = 0; q < k4; q++) out4[q] = xb4[q];
-    a.mean_a[ms] = a.mean_b[ms];
-    a.sprd_a[ms] = a.sprd_b[ms];
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(&bar)),
+                 "r"(xbytes + tbytes) : "memory");
+    tc::bulk_copy_g2s(Xs, a.bkg + cbase, xbytes, &bar);
+    if (tbytes) tc::bulk_copy_g2s(usm + (size_t)ns * k, a.T + (size_t)act * G * kk, tbytes, &bar);
+  }
+  const bool landed = __syncthreads_and(tc::mbar_wait(&bar, 0));
+  if (!landed) {
+    if (threadIdx.x == 0) {
+      atomicOr(a.status, 64);
+      tc::mbar_wait(&bar, 0);   // the copies in flight land before the CTA exits
+    }
     return;
   }
-  const int g = slab_group(a, a.slab_lev[s], a.cp[col].mld);
-  const bool has = g < G && a.nkept[(size_t)act * G + g] > 0;
-  float x[KMAX];
+  const size_t ms = (size_t)col * ns + s;
+  if (s < ns) {
+    const float4 *xb4 = reinterpret_cast<const float4 *>(Xs + (size_t)s * k);
+    float4 *out4 = reinterpret_cast<float4 *>(Xs + (size_t)s * k);
+    if (skip) {   // src/letkf_solver.F90:207: the block leaves unchanged
+      a.mean_a[ms] = a.mean_b[ms];
+      a.sprd_a[ms] = a.sprd_b[ms];
+    } else {
+      const int g = slab_group(a, a.slab_lev[s], a.cp[col].mld);
+      const bool has = g < G && a.nkept[(size_t)act * G + g] > 0;
+      float x[KMAX];
 #pragma unroll
-  for (int j = 0; j < KMAX; j++) x[j] = 0.0f;
-  if (has) {
-    // x_a = x_b T_g (src/letkf_solver.F90:285-289), members accumulated in i order
-    const float *T = Tsm + (size_t)g * kk;
-    for (int i4 = 0; i4 < k4; i4++) {
-      const float4 xv = xb4[i4];
-      const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+      for (int j = 0; j < KMAX; j++) x[j] = 0.0f;
+      if (has) {
+        // x_a = x_b T_g (src/letkf_solver.F90:285-289), members accumulated in i order
+        const float *T = Tsm + (size_t)g * kk;
+        for (int i4 = 0; i4 < k4; i4++) {
+          const float4 xv = xb4[i4];
+          const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const float4 *Tr = reinterpret_cast<const float4 *>(T + (size_t)(4 * i4 + u) * k);
+          for (int u = 0; u < 4; u++) {
+            const float4 *Tr = reinterpret_cast<const float4 *>(T + (size_t)(4 * i4 + u) * k);
 #pragma unroll
-        for (int q = 0; q < KMAX / 4; q++) {
-          if (q < k4) {
-            const float4 t = Tr[q];
-            x[4 * q + 0] = __fmaf_rn(xs[u], t.x, x[4 * q + 0]);
-            x[4 * q + 1] = __fmaf_rn(xs[u], t.y, x[4 * q + 1]);
-            x[4 * q + 2] = __fmaf_rn(xs[u], t.z, x[4 * q + 2]);
-            x[4 * q + 3] = __fmaf_rn(xs[u], t.w, x[4 * q + 3]);
+            for (int q = 0; q < KMAX / 4; q++) {
+              if (q < k4) {
+                const float4 t = Tr[q];
+                x[4 * q + 0] = __fmaf_rn(xs[u], t.x, x[4 * q + 0]);
+                x[4 * q + 1] = __fmaf_rn(xs[u], t.y, x[4 * q + 1]);
+                x[4 * q + 2] = __fmaf_rn(xs[u], t.z, x[4 * q + 2]);
+                x[4 * q + 3] = __fmaf_rn(xs[u], t.w, x[4 * q + 3]);
+              }
+            }
           }
         }
+      } else {
+#pragma unroll
+        for (int q = 0; q < KMAX / 4; q++)
+          if (q < k4) {
+            const float4 v = xb4[q];
+            x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+          }
       }
+      const float kf = (float)k, km1 = (float)(k - 1);
+      const int v = a.slab_var[s];
+      const float mb = a.mean_b[ms], sb = a.sprd_b[ms];
+      // recenter (:299-303)
+      float m = 0.0f;
+#pragma unroll
+      for (int j = 0; j < KMAX; j++)
+        if (j < k) { x[j] = x[j] + mb; m = m + x[j]; }
+      m = m / kf;
+#pragma unroll
+      for (int j = 0; j < KMAX; j++) x[j] = x[j] - m;
+      // mean increment clip and bounds (:308-318)
+      const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
+      {
+        float r = m - mb;
+        r = fmaxf(r, -inc); r = fminf(r, inc);
+        r = fmaxf(r, lb - mb); r = fminf(r, ub - mb);
+        m = r + mb;
+      }
+      if (a.rtps > 0.0f) {   // (:322-335)
+        float q2 = 0.0f;
+#pragma unroll
+        for (int j = 0; j < KMAX; j++)
+          if (j < k) q2 = q2 + x[j] * x[j];
+        const float sa = sqrtf(q2 / km1);
+        if (sa > 0.0f) {
+          const float f = a.rtps * (sb - sa) / sa + 1.0f;
+#pragma unroll
+          for (int j = 0; j < KMAX; j++) x[j] = x[j] * f;
+        }
+      }
+      if (a.rtpp > 0.0f) {   // (:339-344)
+#pragma unroll
+        for (int q = 0; q < KMAX / 4; q++)
+          if (q < k4) {
+            const float4 b = xb4[q];
+            x[4 * q + 0] = a.rtpp * b.x + (1.0f - a.rtpp) * x[4 * q + 0];
+            x[4 * q + 1] = a.rtpp * b.y + (1.0f - a.rtpp) * x[4 * q + 1];
+            x[4 * q + 2] = a.rtpp * b.z + (1.0f - a.rtpp) * x[4 * q + 2];
+            x[4 * q + 3] = a.rtpp * b.w + (1.0f - a.rtpp) * x[4 * q + 3];
+          }
+      }
+      if (a.mul != 1.0f) {   // (:347-349)
+#pragma unroll
+        for (int j = 0; j < KMAX; j++) x[j] = x[j] * a.mul;
+      }
+      {   // member bounds and re-mean (:357-371)
+        float r = 0.0f;
+#pragma unroll
+        for (int j = 0; j < KMAX; j++)
+          if (j < k) {
+            x[j] = fminf(fmaxf(x[j], lb - m), ub - m);
+            r = r + x[j];
+          }
+        r = r / kf;
+#pragma unroll
+        for (int j = 0; j < KMAX; j++) x[j] = x[j] - r;
+        m = m + r;
+      }
+      float q2 = 0.0f;   // spread (:375-379)
+#pragma unroll
+      for (int j = 0; j < KMAX; j++)
+        if (j < k) q2 = q2 + x[j] * x[j];
+      const float sa = sqrtf(q2 / km1);
+#pragma unroll
+      for (int q = 0; q < KMAX / 4; q++)
+        if (q < k4) out4[q] = make_float4(x[4 * q] + m, x[4 * q + 1] + m, x[4 * q + 2] + m, x[4 * q + 3] + m);
+      a.mean_a[ms] = m;
+      a.sprd_a[ms] = sa;
+      if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
     }
-  } else {
-#pragma unroll
-    for (int q = 0; q < KMAX / 4; q++)
-      if (q < k4) {
-        const float4 v = xb4[q];
-        x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
-      }
   }
-  const float kf = (float)k, km1 = (float)(k - 1);
-  const int v = a.slab_var[s];
-  const float mb = a.mean_b[ms], sb = a.sprd_b[ms];
-  // recenter (:299-303)
-  float m = 0.0f;
-#pragma unroll
-  for (int j = 0; j < KMAX; j++)
-    if (j < k) { x[j] = x[j] + mb; m = m + x[j]; }
-  m = m / kf;
-#pragma unroll
-  for (int j = 0; j < KMAX; j++) x[j] = x[j] - m;
-  // mean increment clip and bounds (:308-318)
-  const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
-  {
-    float r = m - mb;
-    r = fmaxf(r, -inc); r = fminf(r, inc);
-    r = fmaxf(r, lb - mb); r = fminf(r, ub - mb);
-    m = r + mb;
+  // the analysis block (generic-proxy writes) -> global by the async proxy
+  tc::fence_proxy_async();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc::bulk_store_s2g(a.ana + cbase, Xs, xbytes);
+    tc::bulk_commit();
+    tc::bulk_wait_all();
   }
-  if (a.rtps > 0.0f) {   // (:322-335)
-    float q2 = 0.0f;
-#pragma unroll
-    for (int j = 0; j < KMAX; j++)
-      if (j < k) q2 = q2 + x[j] * x[j];
-    const float sa = sqrtf(q2 / km1);
-    if (sa > 0.0f) {
-      const float f = a.rtps * (sb - sa) / sa + 1.0f;
-#pragma unroll
-      for (int j = 0; j < KMAX; j++) x[j] = x[j] * f;
-    }
-  }
-  if (a.rtpp > 0.0f) {   // (:339-344)
-#pragma unroll
-    for (int q = 0; q < KMAX / 4; q++)
-      if (q < k4) {
-        const float4 b = xb4[q];
-        x[4 * q + 0] = a.rtpp * b.x + (1.0f - a.rtpp) * x[4 * q + 0];
-        x[4 * q + 1] = a.rtpp * b.y + (1.0f - a.rtpp) * x[4 * q + 1];
-        x[4 * q + 2] = a.rtpp * b.z + (1.0f - a.rtpp) * x[4 * q + 2];
-        x[4 * q + 3] = a.rtpp * b.w + (1.0f - a.rtpp) * x[4 * q + 3];
-      }
-  }
-  if (a.mul != 1.0f) {   // (:347-349)
-#pragma unroll
-    for (int j = 0; j < KMAX; j++) x[j] = x[j] * a.mul;
-  }
-  {   // member bounds and re-mean (:357-371)
-    float r = 0.0f;
-#pragma unroll
-    for (int j = 0; j < KMAX; j++)
-      if (j < k) {
-        x[j] = fminf(fmaxf(x[j], lb - m), ub - m);
-        r = r + x[j];
-      }
-    r = r / kf;
-#pragma unroll
-    for (int j = 0; j < KMAX; j++) x[j] = x[j] - r;
-    m = m + r;
-  }
-  float q2 = 0.0f;   // spread (:375-379)
-#pragma unroll
-  for (int j = 0; j < KMAX; j++)
-    if (j < k) q2 = q2 + x[j] * x[j];
-  const float sa = sqrtf(q2 / km1);
-#pragma unroll
-  for (int q = 0; q < KMAX / 4; q++)
-    if (q < k4) out4[q] = make_float4(x[4 * q] + m, x[4 * q + 1] + m, x[4 * q + 2] + m, x[4 * q + 3] + m);
-  a.mean_a[ms] = m;
-  a.sprd_a[ms] = sa;
-  if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
 }
 
 }  // namespace
 
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   if (a.ncol <= 0 || a.ncols <= 0) return cudaSuccess;
-  const size_t tbytes = (size_t)a.groups * a.k * a.k * sizeof(float);
-  if (a.k % 4 == 0 && a.ns <= 256 && tbytes <= 160 * 1024) {
+  const size_t rbytes = ((size_t)a.ns * a.k + (size_t)a.groups * a.k * a.k) * sizeof(float);
+  if (a.k % 4 == 0 && a.ns <= 256 && rbytes <= 200 * 1024) {
     const int nt = (a.ns + 31) & ~31;
-    auto kern = a.k <= 16   ? k_update_rows<16>
-                : a.k <= 32 ? k_update_rows<32>
-                : a.k <= 48 ? k_update_rows<48>
-                : a.k <= 64 ? k_update_rows<64>
-                : a.k <= 96 ? k_update_rows<96>
-                            : k_update_rows<128>;
-    if (tbytes > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tbytes);
-      if (e != cudaSuccess) return e;
-    }
-    kern<<<a.ncols, nt, tbytes, st>>>(a);
+    const int k = a.k;
+    auto kern = k <= 8    ? k_update_rows<8>
+                : k <= 16 ? k_update_rows<16>
+                : k <= 24 ? k_update_rows<24>
+                : k <= 32 ? k_update_rows<32>
+                : k <= 40 ? k_update_rows<40>
+                : k <= 48 ? k_update_rows<48>
+                : k <= 56 ? k_update_rows<56>
+                : k <= 64 ? k_update_rows<64>
+                : k <= 80 ? k_update_rows<80>
+                : k <= 96 ? k_update_rows<96>
+                : k <= 112 ? k_update_rows<112>
+                           : k_update_rows<128>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbytes);
+    if (e != cudaSuccess) return e;
+    kern<<<a.ncols, nt, rbytes, st>>>(a);
     (*launches)++;
     return cudaGetLastError();
   }
