@@ -202,14 +202,27 @@ def reference_arm(args, dist):
     return 0
 
 
+def describe_loc(loc):
+    """One-line description of a localization section."""
+    pts = loc.get("hzloc", loc.get("hzloc_prof", {})).get("value", [])
+    rad = " -> ".join("%g km (%g deg)" % (p["radius"] / 1e3, p["lat"]) for p in pts)
+    out = "%s %s" % (loc["class"], rad)
+    if "vtloc" in loc:
+        out += ", vertical GC %g m" % loc["vtloc"]
+    return out
+
+
 def workload_config(args, prob, cfg):
     nact = int(np.sum(prob.mask == 0))
-    return {"workload": "%s: ocean %dx%dx%d grid, T/S/SSH (%d slabs), k=%d, %d obs (T/S profiles + SSH/SST swaths), "
-                        "loc_novrt 800 km (equator) -> 200 km (poles)" % (args.workload, prob.nx, prob.ny, prob.nz,
-                                                                         prob.ns, prob.k, prob.nobs),
+    names = "/".join(v["name"] for v in prob.vars) if prob.vars and "name" in prob.vars[0] else "%d variables" % len(
+        prob.vars)
+    state_gb = 2.0 * prob.ncol * prob.ns * prob.k * 4 / 1e9
+    return {"workload": "%s: %dx%dx%d grid, %s (%d slabs), k=%d, %d obs, %s" % (
+                args.workload, prob.nx, prob.ny, prob.nz, names, prob.ns, prob.k, prob.nobs,
+                describe_loc(cfg["localization"])),
             "columns_total": int(prob.ncol), "columns_active": nact, "ensemble": int(prob.k), "slabs": int(prob.ns),
             "observations": int(prob.nobs), "l2": "flushed (256 MB device write) before every timed step; "
-                                                  "state in+out 6.7 GB per step also exceeds L2",
+                                                  "state in+out %.1f GB per step" % state_gb,
             "parallelism": "replicas" if args.gpus > 1 else "single"}
 
 
