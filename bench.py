@@ -382,6 +382,137 @@ def gpu_arm(args, dist):
     return 0
 
 
+def learned_arm(args, dist):
+    """C5: the learned form in a cycling experiment.  Cycles 0-4 run the exact
+    analysis (AUTO form) and collect training rows; the network is trained on
+    the GPU; on the next cycle the exact (AUTO), plain and learned analyses
+    are timed on the same inputs and the learned analysis is compared with
+    the exact one (RMS of the analysis-mean difference over the background
+    spread; the interpolation without the network alongside)."""
+    from letkf_gb300 import PinnedArray, Solver, synth
+    from letkf_gb300.workloads import WORKLOADS
+    cfg = WORKLOADS[args.workload]
+    gen = dict(cfg["gen"])
+    w = gen.pop("workload")
+    cy = cfg["cycles"]
+    t_setup = time.perf_counter()
+    prob = synth.generate(w, **gen)
+    nobs = prob.nobs
+    prob = synth.observe(prob, seed=2000, n_obs=nobs)
+    dev = dist.local if dist.world > 1 else 0
+    s = Solver(dev)
+    s.solver_init(cfg["solver"])
+    s.loc_init(cfg["localization"], prob.vars, prob.lev_depth)
+    s.set_problem(prob)
+    s.learn_init(prob.nx, prob.ny, **cfg["learn"])
+
+    def next_cycle(p, ana, c):
+        x, m, sp = ana
+        p.state[...] = x - m[:, :, None]
+        p.mean[...] = m
+        p.sprd[...] = sp
+        synth.forecast(p, u=cy["u"], kappa=cy["kappa"], dt=cy["dt"])
+        return synth.observe(p, seed=2000 + c, n_obs=nobs)
+
+    for c in range(cy["train"]):
+        if c:
+            prob = next_cycle(prob, ana, c)
+            s.set_problem(prob)
+        s.set_variant("auto")
+        rows = s.learn_collect()
+        ana = s.get_state()
+    t_tr = time.perf_counter()
+    loss = s.learn_train(epochs=cy["epochs"], batch=cy["batch"], lr=cy["lr"])
+    t_tr = time.perf_counter() - t_tr
+    prob = next_cycle(prob, ana, cy["train"])
+    s.set_problem(prob)
+    t_setup = time.perf_counter() - t_setup
+    nact = int(np.sum(prob.mask == 0))
+
+    def timed(variant, steps, warm):
+        s.set_variant(variant)
+        for _ in range(max(warm, 3)):
+            s.run()
+        dist.barrier()
+        ts = []
+        for _ in range(steps):
+            s.flush_l2(256 << 20)
+            s.run()
+            ts.append(s.timings())
+        dist.barrier()
+        return ts
+
+    ex_t = timed("auto", args.steps, args.warmup)
+    ex = s.get_state()
+    exact_variant = {1: "plain", 2: "batched_tc"}.get(ex_t[-1]["variant"], "?")
+    pl_t = timed("plain", max(1, min(args.steps, 3)), 1)
+    clocks = Clocks(dev)
+    le_t = timed("learned", args.steps, args.warmup)
+    ck = clocks.stop()
+    le = s.get_state()
+    st = s.learn_stats()
+    s.learn_set_network(False)
+    s.run()
+    ip = s.get_state()
+    s.learn_set_network(True)
+    act = prob.mask == 0
+    spread = float(np.sqrt(np.mean(prob.sprd[act].astype(np.float64) ** 2)))
+    err = lambda a: float(np.sqrt(np.mean((a[1][act].astype(np.float64) - ex[1][act]) ** 2))) / spread
+    # end to end through the C ABI: state and observations from page-locked
+    # host buffers, analysis back into page-locked buffers, every step
+    names = ("olat", "olon", "oz", "otime", "oval", "oerr", "oobsid", "oplatid", "hx", "hx_mean")
+    pin = {n: PinnedArray(getattr(prob, n).shape, getattr(prob, n).dtype) for n in names + ("state", "mean", "sprd")}
+    for n, p_ in pin.items():
+        p_.array[...] = getattr(prob, n)
+    outp = [PinnedArray(prob.state.shape), PinnedArray(prob.mean.shape), PinnedArray(prob.sprd.shape)]
+    h2d = sum(p_.array.nbytes for p_ in pin.values())
+    d2h = sum(p_.array.nbytes for p_ in outp)
+
+    def e2e_step():
+        s.set_state(pin["state"].array, pin["mean"].array, pin["sprd"].array, prob.vars)
+        s.set_obs(*(pin[n].array for n in names))
+        s.run()
+        s.get_state(tuple(p_.array for p_ in outp))
+
+    s.set_variant("learned")
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    et = []
+    for _ in range(args.steps):
+        s.flush_l2(256 << 20)
+        t0 = time.perf_counter()
+        e2e_step()
+        et.append(time.perf_counter() - t0)
+    for p_ in list(pin.values()) + outp:
+        p_.free()
+    s.close()
+    ms = dist.max(statistics.mean(t["total_ms"] for t in le_t))
+    ms_ex = statistics.mean(t["total_ms"] for t in ex_t)
+    ms_pl = statistics.mean(t["total_ms"] for t in pl_t)
+    e2e_ms = dist.max(1000.0 * statistics.mean(et))
+    line = {"metric": METRIC, "value": dist.world * nact / (ms / 1000.0), "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (exact solves), bf16 x bf16 -> f32 (network)",
+            "data": "synthetic (seeded generator; cycling with a zonal jet, persistent clustered network)",
+            "config": dict(workload_config(args, prob, cfg), learn=cfg["learn"], cycles=cy),
+            "clocks": ck, "gpu_launches": le_t[-1]["launches"] * args.steps, "variant": "learned",
+            "e2e": {"value": dist.world * nact / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                    "step_ms": [round(1000.0 * t, 3) for t in et]},
+            "exact": {"variant": exact_variant, "ms_per_step": ms_ex, "value": nact / (ms_ex / 1000.0)},
+            "plain_variant": {"ms_per_step": ms_pl, "value": nact / (ms_pl / 1000.0),
+                              "speedup_of_headline": ms_pl / ms},
+            "analysis_error": {"learned_mean_rms_over_spread": err(le), "interpolation_only": err(ip),
+                               "bar": 0.01},
+            "learn": dict(st, train_loss=loss, train_s=t_tr, train_rows=rows, setup_s=t_setup),
+            "stages": {"learned_exact_ms": st["exact_ms"], "features_ms": st["feature_ms"],
+                       "network_ms": st["network_ms"], "apply_ms": st["apply_ms"],
+                       "update_ms": statistics.mean(t["update_ms"] for t in le_t)}}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def single_run(args):
     """One lgpu_solver_run of the workload, for kernel profiles; prints the
     library's stage timings."""
@@ -432,6 +563,9 @@ def main():
     try:
         if args.impl == "reference":
             return reference_arm(args, dist)
+        from letkf_gb300.workloads import WORKLOADS
+        if "learn" in WORKLOADS.get(args.workload, {}):
+            return learned_arm(args, dist)
         return gpu_arm(args, dist)
     finally:
         dist.close()

@@ -138,7 +138,7 @@ typedef struct lgpu_timings {
   int launches;      /* kernels launched by the run */
   int units;         /* (column, group) solve units */
   long long kept_pairs;   /* sum over units of kept local observations (only when counted) */
-  int variant;       /* Gram variant that ran (LGPU_VARIANT_PLAIN / _BATCHED_TC) */
+  int variant;       /* variant that ran (LGPU_VARIANT_PLAIN / _BATCHED_TC / _LEARNED) */
   float tiles_ms;    /* BATCHED_TC: part of gram_ms spent building the tile candidate streams */
   long long mma_chunks;  /* BATCHED_TC: (tile, group, pass, 16-observation chunk) steps that ran MMAs */
   int mma_n;         /* BATCHED_TC: features per pass (MMA N); executed TF32 flops =
@@ -156,6 +156,14 @@ typedef struct lgpu_timings {
 #define LGPU_VARIANT_AUTO 0
 #define LGPU_VARIANT_PLAIN 1
 #define LGPU_VARIANT_BATCHED_TC 2
+/* LEARNED (after lgpu_learn_init and lgpu_learn_train; loc_novrt only): exact
+ * solves (PLAIN Gram) on the columns of a coarse lattice, a random judge
+ * sample and the columns the confidence gate sends back; every other column
+ * gets the bilinear interpolation of the coarse (W, w-bar) corrected by the
+ * learned network.  The update and its epilogue are those of the exact
+ * forms.  No counterpart in the reference, which solves every column
+ * (src/letkf_solver.F90:203-384). */
+#define LGPU_VARIANT_LEARNED 3
 
 int lgpu_create(int device, lgpu_handle **out);
 void lgpu_destroy(lgpu_handle *h);
@@ -244,6 +252,74 @@ int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, i
 int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
                              int *n, int *ncand);
 
+
+/* ---- Learned form: interpolation of (W, w-bar) with a learned correction.
+ * No counterpart in the reference (it solves every column exactly).
+ *
+ * The grid must be a regular lattice, column ij = i + nx * j (i longitude,
+ * j latitude), with nx a multiple of `stride`.  Columns with i % stride == 0
+ * and j % stride == 0 are the coarse lattice.  The network maps, per column,
+ * the bilinear interpolation of the four coarse neighbours' (W, w-bar)
+ * (k*k + k values) and 16 observation-geometry features (local count, sums
+ * of localisation weights, nearest-observation distance, innovation
+ * moments, position in the coarse cell, neighbour spread) to a correction
+ * of (W, w-bar): layers din -> hidden -> hidden -> dout, GELU, BF16 weights
+ * and activations with FP32 accumulation; inference on the tensor cores
+ * (tcgen05 kind::f16), training on the CUDA cores (Adam). */
+typedef struct lgpu_learn_config {
+  int nx, ny;            /* lattice */
+  int stride;            /* coarse lattice stride (>= 2) */
+  int hidden;            /* hidden width, a multiple of 16 (512) */
+  float judge_frac;      /* fraction of the other columns solved exactly every analysis to judge the network (0.02) */
+  float gate_frac;       /* fraction of calibration columns whose network output is large enough to send them to the exact solve (0.05) */
+  float sample_frac;     /* fraction of the other columns of a collected analysis added to the training rows */
+  int train_cap;         /* training rows kept */
+  unsigned long long seed;
+} lgpu_learn_config;
+
+typedef struct lgpu_learn_stats {
+  int coarse;            /* exact: coarse lattice columns */
+  int judged;            /* exact: judge sample */
+  int fallback;          /* exact: columns without four coarse neighbours */
+  int gated;             /* exact: sent back by the gate */
+  int inferred;          /* columns whose transform came from the network */
+  float judge_rms;       /* RMS over judged, ungated columns of ||T_net - T_exact||_F / k */
+  float judge_ref_rms;   /* RMS of ||T_exact - I||_F / k over the same columns */
+  float tau;             /* gate threshold (RMS of the standardised network output) */
+  long long train_rows;  /* training rows stored */
+  float exact_ms, feature_ms, network_ms, apply_ms;   /* device time of the learned stages */
+} lgpu_learn_stats;
+
+int lgpu_learn_init(lgpu_handle *h, const lgpu_learn_config *cfg);
+/* Runs an exact analysis (the AUTO / PLAIN / BATCHED_TC form in force; the
+ * analysis result is the exact one) and adds training rows: network inputs
+ * and residual targets (exact - interpolated) of a sample of the
+ * non-lattice columns.  *rows receives the number of rows stored. */
+int lgpu_learn_collect(lgpu_handle *h, long long *rows);
+/* Standardises the stored rows (first call), runs `epochs` passes of Adam
+ * with mini-batches of `batch` rows, then calibrates the gate threshold.
+ * *loss receives the mean training loss of the last epoch (standardised
+ * units). */
+int lgpu_learn_train(lgpu_handle *h, int epochs, int batch, float lr, float *loss);
+int lgpu_learn_stats_get(lgpu_handle *h, lgpu_learn_stats *out);
+/* use_network = 0: the LEARNED variant applies the bare interpolation (no
+ * correction, the gate only for columns without four coarse neighbours): the
+ * method without the network, for comparison. */
+int lgpu_learn_set_network(lgpu_handle *h, int use_network);
+/* Network parameters (FP32 masters; W1, b1, W2, b2, W3, b3 row-major
+ * [out][in]); n must equal the count lgpu_learn_param_count returns. */
+long long lgpu_learn_param_count(lgpu_handle *h);
+int lgpu_learn_get_params(lgpu_handle *h, float *params, long long n);
+int lgpu_learn_set_params(lgpu_handle *h, const float *params, long long n);
+
+/* Verification of the network kernels (standalone, allocates): for rows x
+ * [rows][din] (rounded to BF16 inside) and targets t [rows][dout], with the
+ * parameters given (rounded to BF16 inside), returns the mean squared error
+ * *loss, its gradient (FP32, the parameter layout) from the training
+ * kernels, the output of the CUDA-core forward y_simt and of the tensor-core
+ * forward y_tc ([rows][dout] each; any may be null). */
+int lgpu_mlp_debug(int device, int din, int hidden, int dout, int rows, const float *params, const float *x,
+                   const float *t, float *loss, float *grad, float *y_simt, float *y_tc);
 
 /* Page-locked host memory for callers that stream state in and out every
  * analysis (host<->device copies run at full link speed from it). */

@@ -68,6 +68,8 @@ enum {
 
 constexpr int kOutChunks = 8;   // column chunks of eigensolve / update / analysis download of a bound state
 
+struct LearnState;   // learned form (below)
+
 struct lgpu_handle {
   int device = 0;
   cudaStream_t st = nullptr;
@@ -99,7 +101,11 @@ struct lgpu_handle {
   int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
   DevBuf buf[B_COUNT_ALL];
   lgpu_timings tim{};
+  LearnState *learn = nullptr;      // learned form, after lgpu_learn_init
+  float *learn_wbar = nullptr;      // mean weights of every unit while training rows are collected
 };
+
+static void learn_free(lgpu_handle *h);
 
 namespace {
 
@@ -251,6 +257,7 @@ void lgpu_destroy(lgpu_handle *h) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->cst) cudaStreamSynchronize(h->cst);
   for (auto &b : h->buf) b.release();
+  learn_free(h);
   for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_in) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_tune) if (ev) cudaEventDestroy(ev);
@@ -342,7 +349,7 @@ int lgpu_loc_maxgroups(const lgpu_handle *h) { return (h && h->loc_ok) ? h->loc.
 
 int lgpu_set_variant(lgpu_handle *h, int variant) {
   if (!h) return LGPU_ERR_ARG;
-  if (variant < LGPU_VARIANT_AUTO || variant > LGPU_VARIANT_BATCHED_TC)
+  if (variant < LGPU_VARIANT_AUTO || variant > LGPU_VARIANT_LEARNED)
     return fail(h, LGPU_ERR_ARG, "unknown variant " + std::to_string(variant));
   h->variant = variant;
   return LGPU_OK;
@@ -630,8 +637,10 @@ int lgpu_get_obs_prepared(lgpu_handle *h, float *hx, float *hx_mean, float *lat,
   return LGPU_OK;
 }
 
-// letkf_solver_run (src/letkf_solver.F90:150-389)
-int lgpu_solver_run(lgpu_handle *h) {
+// First part of a run: checks, buffers, the observation index and the
+// per-column parameters (events ev[0..2]); shared by the exact and the
+// learned forms.
+static int prepare_run(lgpu_handle *h, ObsSorted &os, int &launches) {
   if (!h) return LGPU_ERR_ARG;
   if (!h->solver_ok) return fail(h, LGPU_ERR_ORDER, "solver_run before solver_init");
   if (!h->loc_ok) return fail(h, LGPU_ERR_ORDER, "solver_run before loc_init");
@@ -684,13 +693,11 @@ int lgpu_solver_run(lgpu_handle *h) {
   CK(h->buf[B_DLGC].ensure(4 * (size_t)h->ncol * G), "alloc");
   CK(h->buf[B_DLGL].ensure(4 * (size_t)h->ncol * G), "alloc");
   CK(h->buf[B_STATUS].ensure(16), "alloc");
-  ObsSorted os;
   os.A = h->buf[B_SA].as<float4>();
   os.B = h->buf[B_SB].as<float4>();
   os.hx = h->buf[B_SHX].as<float>();
   os.idx = h->buf[B_SIDX].as<int>();
   os.cell_start = h->buf[B_CSTART].as<int>();
-  int launches = 0;
   cudaStream_t st = h->st;
   const bool bound = h->bound_state != nullptr;
   CK(cudaEventRecord(h->ev[0], st), "event");
@@ -727,6 +734,82 @@ int lgpu_solver_run(lgpu_handle *h) {
   CK(cudaMemsetAsync(h->buf[B_DLGL].p, 0, 4 * (size_t)h->ncol * G, st), "memset");
   CK(cudaMemsetAsync(h->buf[B_STATUS].p, 0, 16, st), "memset");
   CK(cudaEventRecord(h->ev[2], st), "event");
+  return LGPU_OK;
+}
+
+static int learned_run(lgpu_handle *h);
+static int eig_scratch(lgpu_handle *h, int units, EigSplit &sp, int &batch);
+static UpdateArgs update_args(lgpu_handle *h);
+
+// eigensolve scratch of the split pipeline for `units` units (at most 8 GB,
+// units in batches); batch = 0 when it cannot be had (the fused kernel runs)
+static int eig_scratch(lgpu_handle *h, int units, EigSplit &sp, int &batch) {
+  const int k = h->k;
+  const size_t per = eig_split_bytes_per_unit(k);
+  const size_t budget = (size_t)8 << 30;
+  batch = (int)std::min<size_t>((size_t)std::max(1, units), std::max<size_t>(1024, budget / per));
+  const size_t need = per * (size_t)batch + 5 * 256;
+  if (h->buf[B_EIGSCR].cap >= need || h->buf[B_EIGSCR].ensure(need) == cudaSuccess) {
+    unsigned char *base = h->buf[B_EIGSCR].as<unsigned char>();
+    size_t off = 0;
+    auto take = [&](size_t bytes) { unsigned char *p = base + off; off += (bytes + 255) & ~(size_t)255; return p; };
+    sp.Q = reinterpret_cast<float *>(take((size_t)batch * k * k * 4));
+    sp.DE = reinterpret_cast<float *>(take((size_t)batch * 2 * k * 4));
+    sp.log = reinterpret_cast<float2 *>(take((size_t)batch * eig_log_cap(k) * 8));
+    sp.logn = reinterpret_cast<int *>(take((size_t)batch * 4));
+    sp.lam = reinterpret_cast<float *>(take((size_t)batch * k * 4));
+    sp.cap = eig_log_cap(k);
+  } else {
+    cudaGetLastError();   // clear the failed allocation
+    batch = 0;
+  }
+  return LGPU_OK;
+}
+
+static UpdateArgs update_args(lgpu_handle *h) {
+  UpdateArgs ua;
+  ua.ncol = h->ncol;
+  ua.ns = h->ns;
+  ua.k = h->k;
+  ua.groups = h->loc.groups;
+  ua.col0 = 0;
+  ua.ncols = h->ncol;
+  ua.mask = h->buf[B_MASK].as<int>();
+  ua.col2act = h->buf[B_COL2ACT].as<int>();
+  ua.cp = h->buf[B_CP].as<ColPar>();
+  ua.loc_cls = h->loc.cls;
+  ua.vtloc_surf = h->loc.vtloc_surf;
+  ua.slab_var = h->buf[B_SLABVAR].as<int>();
+  ua.slab_lev = h->buf[B_SLABLEV].as<int>();
+  ua.var_inc_max = h->buf[B_VARINC].as<float>();
+  ua.var_lb = h->buf[B_VARLB].as<float>();
+  ua.var_ub = h->buf[B_VARUB].as<float>();
+  ua.bkg = h->buf[B_BKG].as<float>();
+  ua.mean_b = h->buf[B_MEANB].as<float>();
+  ua.sprd_b = h->buf[B_SPRDB].as<float>();
+  ua.T = h->buf[B_T].as<float>();
+  ua.nkept = h->buf[B_NKEPT].as<int>();
+  ua.ana = h->buf[B_ANA].as<float>();
+  ua.mean_a = h->buf[B_MEANA].as<float>();
+  ua.sprd_a = h->buf[B_SPRDA].as<float>();
+  ua.rtps = h->scfg.rtps;
+  ua.rtpp = h->scfg.rtpp;
+  ua.mul = h->scfg.mul;
+  ua.status = h->buf[B_STATUS].as<int>();
+  return ua;
+}
+
+// letkf_solver_run (src/letkf_solver.F90:150-389)
+int lgpu_solver_run(lgpu_handle *h) {
+  if (!h) return LGPU_ERR_ARG;
+  if (h->variant == LGPU_VARIANT_LEARNED) return learned_run(h);
+  ObsSorted os;
+  int launches = 0;
+  int rc0 = prepare_run(h, os, launches);
+  if (rc0 != LGPU_OK) return rc0;
+  const int k = h->k, kp = h->kp, ns = h->ns, G = h->loc.groups;
+  cudaStream_t st = h->st;
+  const bool bound = h->bound_state != nullptr;
   // ---- search + localize + Gram ----
   // ---- Gram: the batched tensor-core form or the plain per-column form ----
   auto run_batched = [&]() -> int {
@@ -841,6 +924,7 @@ int lgpu_solver_run(lgpu_handle *h) {
   // analysis is downloaded into the caller's arrays while the eigensolve and
   // update of the following chunks run.
   EigArgs ea;
+  ea.wbar = h->learn_wbar;   // mean weights of every unit while training data is collected
   ea.nunits = h->nunits;
   ea.k = k;
   ea.infl = 1.0f;   // letkf_core_solve is called with infl = 1.0 (src/letkf_solver.F90:279)
@@ -848,56 +932,14 @@ int lgpu_solver_run(lgpu_handle *h) {
   ea.nkept = h->buf[B_NKEPT].as<int>();
   ea.T = h->buf[B_T].as<float>();
   ea.status = h->buf[B_STATUS].as<int>();
-  UpdateArgs ua;
-  ua.ncol = h->ncol;
-  ua.ns = ns;
-  ua.k = k;
-  ua.groups = G;
-  ua.mask = h->buf[B_MASK].as<int>();
-  ua.col2act = h->buf[B_COL2ACT].as<int>();
-  ua.cp = h->buf[B_CP].as<ColPar>();
-  ua.loc_cls = h->loc.cls;
-  ua.vtloc_surf = h->loc.vtloc_surf;
-  ua.slab_var = h->buf[B_SLABVAR].as<int>();
-  ua.slab_lev = h->buf[B_SLABLEV].as<int>();
-  ua.var_inc_max = h->buf[B_VARINC].as<float>();
-  ua.var_lb = h->buf[B_VARLB].as<float>();
-  ua.var_ub = h->buf[B_VARUB].as<float>();
-  ua.bkg = h->buf[B_BKG].as<float>();
-  ua.mean_b = h->buf[B_MEANB].as<float>();
-  ua.sprd_b = h->buf[B_SPRDB].as<float>();
-  ua.T = h->buf[B_T].as<float>();
-  ua.nkept = h->buf[B_NKEPT].as<int>();
-  ua.ana = h->buf[B_ANA].as<float>();
-  ua.mean_a = h->buf[B_MEANA].as<float>();
-  ua.sprd_a = h->buf[B_SPRDA].as<float>();
-  ua.rtps = h->scfg.rtps;
-  ua.rtpp = h->scfg.rtpp;
-  ua.mul = h->scfg.mul;
-  ua.status = h->buf[B_STATUS].as<int>();
+  UpdateArgs ua = update_args(h);
   // eigensolve scratch: the split pipeline (at most 8 GB, units in batches);
   // the fused one-warp kernel over all units if the scratch cannot be had
   EigSplit sp;
   int batch = 0;
   {
-    const size_t per = eig_split_bytes_per_unit(k);
-    const size_t budget = (size_t)8 << 30;
-    batch = (int)std::min<size_t>((size_t)std::max(1, h->nunits), std::max<size_t>(1024, budget / per));
-    const size_t need = per * (size_t)batch + 5 * 256;
-    if (h->buf[B_EIGSCR].cap >= need || h->buf[B_EIGSCR].ensure(need) == cudaSuccess) {
-      unsigned char *base = h->buf[B_EIGSCR].as<unsigned char>();
-      size_t off = 0;
-      auto take = [&](size_t bytes) { unsigned char *p = base + off; off += (bytes + 255) & ~(size_t)255; return p; };
-      sp.Q = reinterpret_cast<float *>(take((size_t)batch * k * k * 4));
-      sp.DE = reinterpret_cast<float *>(take((size_t)batch * 2 * k * 4));
-      sp.log = reinterpret_cast<float2 *>(take((size_t)batch * eig_log_cap(k) * 8));
-      sp.logn = reinterpret_cast<int *>(take((size_t)batch * 4));
-      sp.lam = reinterpret_cast<float *>(take((size_t)batch * k * 4));
-      sp.cap = eig_log_cap(k);
-    } else {
-      cudaGetLastError();   // clear the failed allocation
-      batch = 0;
-    }
+    const int rc = eig_scratch(h, h->nunits, sp, batch);
+    if (rc != LGPU_OK) return rc;
   }
   if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
   if (bound) CK(cudaStreamWaitEvent(st, h->ev_in[1], 0), "stream wait");
@@ -1209,3 +1251,681 @@ int lgpu_debug_gc(lgpu_handle *h, int n, const float *z, const float *L, float *
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Learned form (no counterpart in the reference, which solves every column:
+// src/letkf_solver.F90:203-384)
+
+struct LearnState {
+  lgpu_learn_config cfg{};
+  MlpShape shape{};
+  size_t nparam = 0;
+  std::vector<int> coarse, fine_ok, fine_miss;   // active columns by role
+  std::vector<int> rank;                         // [ncol] row of a coarse column in the exact set, or -1
+  DevBuf d_fine, d_rank, d_cact, d_mark;
+  DevBuf P, Pq, Pm, Pv, Pg, Wt;                  // masters, BF16-rounded copy, Adam moments, gradient, tiled weights
+  DevBuf mu_in, sd_in, mu_out, sd_out;
+  DevBuf feat, nkf, X, Xt, H1, H2, Yn, flag, gate, gate_n, jacc;
+  DevBuf ecols, Gsub, nksub, Tsub, wsub;         // exact subsets
+  DevBuf store_X, store_Y, wbar_all;
+  DevBuf bidx, Xb, Yb, scr, lacc;
+  DevBuf wout;                                   // per-output loss weights: 1 for W, k for w-bar
+  long long nstore = 0;
+  bool stats_ok = false, trained = false;
+  unsigned long long runs = 0;
+  int adam_step = 0;
+  float tau = 3.0e38f;
+  int use_net = 1;
+  lgpu_learn_stats st{};
+  cudaEvent_t ev[6] = {};
+};
+
+static void learn_free(lgpu_handle *h) {
+  if (!h->learn) return;
+  LearnState *L = h->learn;
+  DevBuf *all[] = {&L->d_fine, &L->d_rank, &L->d_cact, &L->d_mark, &L->P, &L->Pq, &L->Pm, &L->Pv, &L->Pg, &L->Wt,
+                   &L->mu_in, &L->sd_in, &L->mu_out, &L->sd_out, &L->feat, &L->nkf, &L->X, &L->Xt, &L->H1, &L->H2,
+                   &L->Yn, &L->flag, &L->gate, &L->gate_n, &L->jacc, &L->ecols, &L->Gsub, &L->nksub, &L->Tsub,
+                   &L->wsub, &L->store_X, &L->store_Y, &L->wbar_all, &L->bidx, &L->Xb, &L->Yb, &L->scr, &L->lacc,
+                   &L->wout};
+  for (DevBuf *b : all) b->release();
+  for (auto &e : L->ev) if (e) cudaEventDestroy(e);
+  delete L;
+  h->learn = nullptr;
+}
+
+namespace {
+
+unsigned long long mix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+double unif01(unsigned long long &s) {
+  s = mix64(s);
+  return (double)(s >> 11) * (1.0 / 9007199254740992.0);
+}
+
+}  // namespace
+
+int lgpu_learn_init(lgpu_handle *h, const lgpu_learn_config *cfg) {
+  if (!h || !cfg) return LGPU_ERR_ARG;
+  if (!h->grid_ok || !h->loc_ok || !h->state_ok)
+    return fail(h, LGPU_ERR_ORDER, "learn_init before grid, localizer and state were set");
+  if (h->loc.cls != LOC_NOVRT || h->loc.groups != 1)
+    return fail(h, LGPU_ERR_UNSUPPORTED, "the learned form supports loc_novrt (one group per column) only");
+  if (cfg->nx <= 0 || cfg->ny <= 0 || (long long)cfg->nx * cfg->ny != h->ncol)
+    return fail(h, LGPU_ERR_ARG, "learn_init: nx * ny must equal the number of grid columns");
+  if (cfg->stride < 2 || cfg->nx % cfg->stride != 0)
+    return fail(h, LGPU_ERR_ARG, "learn_init: stride must be >= 2 and divide nx");
+  if (cfg->hidden < 16 || cfg->hidden % 16 != 0 || cfg->hidden > 2048)
+    return fail(h, LGPU_ERR_ARG, "learn_init: hidden must be a multiple of 16 in [16, 2048]");
+  if (!(cfg->judge_frac >= 0.0f && cfg->judge_frac <= 1.0f) || !(cfg->gate_frac >= 0.0f && cfg->gate_frac <= 1.0f) ||
+      !(cfg->sample_frac > 0.0f && cfg->sample_frac <= 1.0f) || cfg->train_cap <= 0)
+    return fail(h, LGPU_ERR_ARG, "learn_init: fractions must lie in [0, 1] and train_cap be positive");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  learn_free(h);
+  LearnState *L = new LearnState();
+  h->learn = L;
+  L->cfg = *cfg;
+  const int k = h->k, nx = cfg->nx, ny = cfg->ny, s = cfg->stride;
+  L->shape.din = k * k + k + 16;
+  L->shape.k1 = (L->shape.din + 15) & ~15;
+  L->shape.H = cfg->hidden;
+  L->shape.dout = k * k + k;
+  L->nparam = mlp_param_count(L->shape);
+  // roles of the active columns
+  L->rank.assign(h->ncol, -1);
+  for (int c = 0; c < h->ncol; c++) {
+    if (h->h_col2act[c] < 0) continue;
+    const int i = c % nx, j = c / nx;
+    if (i % s == 0 && j % s == 0) {
+      L->rank[c] = (int)L->coarse.size();
+      L->coarse.push_back(c);
+    }
+  }
+  for (int c = 0; c < h->ncol; c++) {
+    if (h->h_col2act[c] < 0 || L->rank[c] >= 0) continue;
+    const int i = c % nx, j = c / nx;
+    const int i0 = (i / s) * s, j0 = (j / s) * s, i1 = (i0 + s) % nx, j1 = j0 + s < ny ? j0 + s : j0;
+    const double fx = (double)(i - i0) / s, fy = j1 != j0 ? (double)(j - j0) / s : 0.0;
+    const int nb[4] = {i0 + nx * j0, i1 + nx * j0, i0 + nx * j1, i1 + nx * j1};
+    const double w[4] = {(1 - fx) * (1 - fy), fx * (1 - fy), (1 - fx) * fy, fx * fy};
+    bool ok = true;
+    for (int q = 0; q < 4; q++)
+      if (w[q] > 0.0 && L->rank[nb[q]] < 0) ok = false;
+    (ok ? L->fine_ok : L->fine_miss).push_back(c);
+  }
+  const int nf = std::max<int>(1, (int)L->fine_ok.size());
+  const int nexact = std::max<int>(1, h->nact);
+  std::vector<int> cact(h->ncol, -1);
+  for (int c : L->coarse) cact[c] = h->h_col2act[c];
+  const MlpShape &S = L->shape;
+  const size_t rows_pad = ((size_t)nf + 127) / 128 * 128;
+  const size_t cap = (size_t)cfg->train_cap;
+  struct { DevBuf *b; size_t bytes; } al[] = {
+      {&L->d_fine, 4 * (size_t)nf}, {&L->d_rank, 4 * (size_t)h->ncol}, {&L->d_cact, 4 * (size_t)h->ncol},
+      {&L->d_mark, 4 * (size_t)h->ncol},
+      {&L->P, 4 * L->nparam}, {&L->Pq, 4 * L->nparam}, {&L->Pm, 4 * L->nparam}, {&L->Pv, 4 * L->nparam},
+      {&L->Pg, 4 * L->nparam}, {&L->Wt, mlp_tiled_weight_bytes(S)},
+      {&L->mu_in, 4 * (size_t)S.din}, {&L->sd_in, 4 * (size_t)S.din}, {&L->mu_out, 4 * (size_t)S.dout},
+      {&L->sd_out, 4 * (size_t)S.dout},
+      {&L->feat, 64 * (size_t)nf}, {&L->nkf, 4 * (size_t)nf}, {&L->X, 4 * (size_t)nf * S.din},
+      {&L->Xt, rows_pad * (size_t)S.k1 * 2}, {&L->H1, mlp_act_bytes(S, nf)}, {&L->H2, mlp_act_bytes(S, nf)},
+      {&L->Yn, 4 * (size_t)nf * S.dout}, {&L->flag, 4 * (size_t)nf}, {&L->gate, 4 * (size_t)nf}, {&L->gate_n, 16},
+      {&L->jacc, 16},
+      {&L->ecols, 4 * (size_t)nexact}, {&L->Gsub, 4 * (size_t)nexact * packed_size(k)},
+      {&L->nksub, 4 * (size_t)nexact}, {&L->Tsub, 4 * (size_t)nexact * k * k}, {&L->wsub, 4 * (size_t)nexact * k},
+      {&L->store_X, 4 * cap * S.din}, {&L->store_Y, 4 * cap * S.dout}, {&L->wbar_all, 4 * (size_t)nexact * k},
+      {&L->lacc, 16}, {&L->wout, 4 * (size_t)S.dout}};
+  for (auto &a : al) CK(a.b->ensure(a.bytes), "alloc learned form");
+  {
+    // the analysis mean depends on w-bar alone (W 1 = 1): its k outputs
+    // weigh as much in the loss as the k*k outputs of W
+    std::vector<float> w(S.dout, 1.0f);
+    for (int i = 0; i < k; i++) w[(size_t)k * k + i] = (float)k;
+    CK(cudaMemcpy(L->wout.p, w.data(), 4 * w.size(), cudaMemcpyHostToDevice), "H2D loss weights");
+  }
+  for (auto &e : L->ev) CK(cudaEventCreate(&e), "event");
+  CK(cudaMemcpyAsync(L->d_fine.p, L->fine_ok.data(), 4 * L->fine_ok.size(), cudaMemcpyHostToDevice, h->st), "H2D");
+  CK(cudaMemcpyAsync(L->d_rank.p, L->rank.data(), 4 * (size_t)h->ncol, cudaMemcpyHostToDevice, h->st), "H2D");
+  CK(cudaMemcpyAsync(L->d_cact.p, cact.data(), 4 * (size_t)h->ncol, cudaMemcpyHostToDevice, h->st), "H2D");
+  CK(cudaMemsetAsync(L->d_mark.p, 0, 4 * (size_t)h->ncol, h->st), "memset");
+  // parameters: uniform(-a, a), a = sqrt(6 / (fan_in + fan_out)) (Glorot);
+  // the last layer scaled by 0.1 so the first corrections are small; zero biases
+  std::vector<float> p(L->nparam, 0.0f);
+  size_t off[6];
+  mlp_param_offsets(S, off);
+  unsigned long long rs = cfg->seed * 0x2545F4914F6CDD1Dull + 7;
+  auto fill = [&](size_t o, int nout, int nin, double scale) {
+    const double a = scale * std::sqrt(6.0 / (nin + nout));
+    for (size_t q = 0; q < (size_t)nout * nin; q++) p[o + q] = (float)((2.0 * unif01(rs) - 1.0) * a);
+  };
+  fill(off[0], S.H, S.din, 1.0);
+  fill(off[2], S.H, S.H, 1.0);
+  fill(off[4], S.dout, S.H, 0.1);
+  CK(cudaMemcpyAsync(L->P.p, p.data(), 4 * L->nparam, cudaMemcpyHostToDevice, h->st), "H2D params");
+  CK(mlp_round(h->st, (long long)L->nparam, L->P.as<float>(), L->Pq.as<float>()), "round params");
+  CK(cudaMemsetAsync(L->Pm.p, 0, 4 * L->nparam, h->st), "memset");
+  CK(cudaMemsetAsync(L->Pv.p, 0, 4 * L->nparam, h->st), "memset");
+  CK(mlp_tile_weights(h->st, S, L->Pq.as<float>(), L->Wt.as<unsigned char>()), "tile weights");
+  CK(cudaStreamSynchronize(h->st), "learn_init");
+  L->st.coarse = (int)L->coarse.size();
+  L->st.fallback = (int)L->fine_miss.size();
+  L->st.tau = L->tau;
+  return LGPU_OK;
+}
+
+int lgpu_learn_set_network(lgpu_handle *h, int use_network) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->learn) return fail(h, LGPU_ERR_ORDER, "learn_set_network before learn_init");
+  h->learn->use_net = use_network ? 1 : 0;
+  return LGPU_OK;
+}
+
+long long lgpu_learn_param_count(lgpu_handle *h) { return (h && h->learn) ? (long long)h->learn->nparam : -1; }
+
+int lgpu_learn_get_params(lgpu_handle *h, float *params, long long n) {
+  if (!h || !params) return LGPU_ERR_ARG;
+  if (!h->learn) return fail(h, LGPU_ERR_ORDER, "learn_get_params before learn_init");
+  if (n != (long long)h->learn->nparam) return fail(h, LGPU_ERR_ARG, "learn_get_params: wrong parameter count");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(cudaMemcpyAsync(params, h->learn->P.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, h->st), "D2H params");
+  CK(cudaStreamSynchronize(h->st), "get params");
+  return LGPU_OK;
+}
+
+int lgpu_learn_set_params(lgpu_handle *h, const float *params, long long n) {
+  if (!h || !params) return LGPU_ERR_ARG;
+  if (!h->learn) return fail(h, LGPU_ERR_ORDER, "learn_set_params before learn_init");
+  LearnState *L = h->learn;
+  if (n != (long long)L->nparam) return fail(h, LGPU_ERR_ARG, "learn_set_params: wrong parameter count");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(cudaMemcpyAsync(L->P.p, params, 4 * (size_t)n, cudaMemcpyHostToDevice, h->st), "H2D params");
+  CK(mlp_round(h->st, n, L->P.as<float>(), L->Pq.as<float>()), "round params");
+  CK(mlp_tile_weights(h->st, L->shape, L->Pq.as<float>(), L->Wt.as<unsigned char>()), "tile weights");
+  CK(cudaStreamSynchronize(h->st), "set params");
+  return LGPU_OK;
+}
+
+int lgpu_learn_stats_get(lgpu_handle *h, lgpu_learn_stats *out) {
+  if (!h || !out) return LGPU_ERR_ARG;
+  if (!h->learn) return fail(h, LGPU_ERR_ORDER, "learn_stats before learn_init");
+  *out = h->learn->st;
+  out->tau = h->learn->tau;
+  out->train_rows = h->learn->nstore;
+  return LGPU_OK;
+}
+
+int lgpu_learn_collect(lgpu_handle *h, long long *rows) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->learn) return fail(h, LGPU_ERR_ORDER, "learn_collect before learn_init");
+  LearnState *L = h->learn;
+  if (h->bound_state) return fail(h, LGPU_ERR_UNSUPPORTED, "learn_collect with a bound state");
+  const int k = h->k;
+  const MlpShape &S = L->shape;
+  // the exact analysis, with the mean weights of every unit
+  const int variant = h->variant;
+  if (variant == LGPU_VARIANT_LEARNED) h->variant = LGPU_VARIANT_AUTO;
+  CK(h->learn->wbar_all.ensure(4 * (size_t)std::max(1, h->nact) * k), "alloc");
+  h->learn_wbar = L->wbar_all.as<float>();
+  int rc = lgpu_solver_run(h);
+  h->learn_wbar = nullptr;
+  h->variant = variant;
+  if (rc != LGPU_OK) return rc;
+  // a sample of the columns with four coarse neighbours
+  std::vector<int> sample;
+  const double frac = L->cfg.sample_frac;
+  unsigned long long rs = mix64(L->cfg.seed ^ (0x51ull + L->runs++));
+  for (int c : L->fine_ok)
+    if (unif01(rs) < frac) sample.push_back(c);
+  const long long room = (long long)L->cfg.train_cap - L->nstore;
+  if ((long long)sample.size() > room) sample.resize((size_t)std::max(0LL, room));
+  const int n = (int)sample.size();
+  if (n > 0) {
+    cudaStream_t st = h->st;
+    int launches = 0;
+    CK(L->ecols.ensure(4 * (size_t)std::max(n, std::max(1, h->nact))), "alloc");
+    CK(cudaMemcpyAsync(L->ecols.p, sample.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, st), "H2D sample");
+    CK(L->feat.ensure(64 * (size_t)n), "alloc");
+    CK(L->nkf.ensure(4 * (size_t)n), "alloc");
+    CK(L->flag.ensure(4 * (size_t)n), "alloc");
+    ObsSorted os;
+    os.A = h->buf[B_SA].as<float4>();
+    os.B = h->buf[B_SB].as<float4>();
+    os.hx = h->buf[B_SHX].as<float>();
+    os.idx = h->buf[B_SIDX].as<int>();
+    os.cell_start = h->buf[B_CSTART].as<int>();
+    CK(lrn_obsfeat(st, n, L->ecols.as<int>(), h->buf[B_CP].as<ColPar>(), h->loc, os, h->buf[B_GEOM].as<IndexGeom>(),
+                   L->feat.as<float>(), L->nkf.as<int>(), &launches),
+       "learned features");
+    LrnInterpArgs ia;
+    ia.nfine = n;
+    ia.cols = L->ecols.as<int>();
+    ia.nx = L->cfg.nx;
+    ia.ny = L->cfg.ny;
+    ia.s = L->cfg.stride;
+    ia.k = k;
+    ia.din = S.din;
+    ia.dout = S.dout;
+    ia.Ts = h->buf[B_T].as<float>();
+    ia.ws = L->wbar_all.as<float>();
+    ia.src_of_col = L->d_cact.as<int>();   // coarse column -> its unit
+    ia.feat = L->feat.as<float>();
+    ia.lat = h->buf[B_LAT].as<float>();
+    ia.mu = nullptr;
+    ia.sd = nullptr;
+    ia.X = L->store_X.as<float>() + (size_t)L->nstore * S.din;
+    ia.ldx = S.din;
+    ia.flag = L->flag.as<int>();
+    ia.Tex = h->buf[B_T].as<float>();
+    ia.wex = L->wbar_all.as<float>();
+    ia.col2act = h->buf[B_COL2ACT].as<int>();
+    ia.Yt = L->store_Y.as<float>() + (size_t)L->nstore * S.dout;
+    ia.ldy = S.dout;
+    CK(lrn_interp(st, ia, &launches), "learned interpolation");
+    CK(cudaStreamSynchronize(st), "collect");
+    L->nstore += n;
+  }
+  if (rows) *rows = L->nstore;
+  return LGPU_OK;
+}
+
+namespace lgpu {
+cudaError_t mlp_loss_accumulate(cudaStream_t st, const float *parts, int n, float *acc);
+}
+
+int lgpu_learn_train(lgpu_handle *h, int epochs, int batch, float lr, float *loss) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->learn) return fail(h, LGPU_ERR_ORDER, "learn_train before learn_init");
+  LearnState *L = h->learn;
+  if (L->nstore <= 0) return fail(h, LGPU_ERR_ORDER, "learn_train before learn_collect stored rows");
+  if (epochs < 0 || batch <= 0 || !(lr > 0.0f)) return fail(h, LGPU_ERR_ARG, "learn_train: epochs >= 0, batch > 0, lr > 0");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = h->st;
+  const MlpShape &S = L->shape;
+  const long long n = L->nstore;
+  batch = (int)std::min<long long>(batch, n);
+  if (!L->stats_ok) {
+    CK(lrn_colstats(st, L->store_X.as<float>(), n, S.din, S.din, L->mu_in.as<float>(), L->sd_in.as<float>()),
+       "input statistics");
+    CK(lrn_colstats(st, L->store_Y.as<float>(), n, S.dout, S.dout, L->mu_out.as<float>(), L->sd_out.as<float>()),
+       "output statistics");
+    L->stats_ok = true;
+  }
+  CK(L->bidx.ensure(4 * (size_t)n), "alloc");
+  CK(L->Xb.ensure(4 * (size_t)batch * S.din), "alloc");
+  CK(L->Yb.ensure(4 * (size_t)batch * S.dout), "alloc");
+  CK(L->scr.ensure(4 * mlp_train_scratch_floats(S, batch)), "alloc");
+  std::vector<int> perm((size_t)n);
+  unsigned long long rs = mix64(L->cfg.seed ^ 0xA5A5ull ^ (unsigned long long)L->adam_step);
+  float last = 0.0f;
+  for (int ep = 0; ep < epochs; ep++) {
+    for (long long i = 0; i < n; i++) perm[(size_t)i] = (int)i;
+    for (long long i = n - 1; i > 0; i--) {
+      const long long j = (long long)(unif01(rs) * (double)(i + 1));
+      std::swap(perm[(size_t)i], perm[(size_t)std::min(j, i)]);
+    }
+    CK(cudaMemcpyAsync(L->bidx.p, perm.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, st), "H2D batch order");
+    CK(cudaMemsetAsync(L->lacc.p, 0, 16, st), "memset");
+    int steps = 0;
+    for (long long b0 = 0; b0 + batch <= n; b0 += batch) {
+      CK(lrn_batch(st, batch, L->bidx.as<int>() + b0, L->store_X.as<float>(), S.din, S.din, L->store_Y.as<float>(),
+                   S.dout, S.dout, L->mu_in.as<float>(), L->sd_in.as<float>(), L->mu_out.as<float>(),
+                   L->sd_out.as<float>(), L->Xb.as<float>(), L->Yb.as<float>()),
+         "training batch");
+      int np = 0;
+      CK(mlp_grad(st, S, L->Pq.as<float>(), L->Xb.as<float>(), L->Yb.as<float>(), batch, L->Pg.as<float>(),
+                  L->scr.as<float>(), &np, L->wout.as<float>()),
+         "network gradient");
+      CK(mlp_loss_accumulate(st, mlp_loss_parts(S, L->scr.as<float>(), batch), np, L->lacc.as<float>()), "loss");
+      L->adam_step++;
+      CK(mlp_adam(st, (long long)L->nparam, L->P.as<float>(), L->Pq.as<float>(), L->Pg.as<float>(), L->Pm.as<float>(),
+                  L->Pv.as<float>(), lr, L->adam_step),
+         "adam");
+      steps++;
+    }
+    float acc = 0.0f;
+    CK(cudaMemcpyAsync(&acc, L->lacc.p, 4, cudaMemcpyDeviceToHost, st), "D2H loss");
+    CK(cudaStreamSynchronize(st), "train epoch");
+    last = steps > 0 ? acc / ((float)steps * (float)batch * (float)S.dout) : 0.0f;
+  }
+  if (loss) *loss = last;
+  CK(mlp_tile_weights(st, S, L->Pq.as<float>(), L->Wt.as<unsigned char>()), "tile weights");
+  // gate threshold: the (1 - gate_frac) quantile of the RMS network output
+  // over (up to) 16,384 stored rows, through the tensor-core forward
+  const int ncal = (int)std::min<long long>(n, 16384);
+  {
+    std::vector<int> idx(ncal);
+    for (int i = 0; i < ncal; i++) idx[i] = (int)((long long)i * n / ncal);
+    CK(L->bidx.ensure(4 * (size_t)std::max<long long>(n, ncal)), "alloc");
+    CK(cudaMemcpyAsync(L->bidx.p, idx.data(), 4 * (size_t)ncal, cudaMemcpyHostToDevice, st), "H2D");
+    CK(L->X.ensure(4 * (size_t)ncal * S.din), "alloc");
+    CK(L->Yn.ensure(4 * (size_t)ncal * S.dout), "alloc");
+    CK(L->Xt.ensure(((size_t)ncal + 127) / 128 * 128 * (size_t)S.k1 * 2), "alloc");
+    CK(L->H1.ensure(mlp_act_bytes(S, ncal)), "alloc");
+    CK(L->H2.ensure(mlp_act_bytes(S, ncal)), "alloc");
+    float *Ycal = L->Yn.as<float>();
+    CK(L->Yb.ensure(4 * (size_t)std::max(ncal, batch) * S.dout), "alloc");
+    CK(lrn_batch(st, ncal, L->bidx.as<int>(), L->store_X.as<float>(), S.din, S.din, L->store_Y.as<float>(), S.dout,
+                 S.dout, L->mu_in.as<float>(), L->sd_in.as<float>(), L->mu_out.as<float>(), L->sd_out.as<float>(),
+                 L->X.as<float>(), L->Yb.as<float>()),
+       "calibration rows");
+    CK(mlp_tile_input(st, S, L->X.as<float>(), ncal, S.din, L->Xt.as<unsigned char>()), "tile input");
+    int launches = 0;
+    CK(cudaMemsetAsync(h->buf[B_STATUS].p, 0, 16, st), "memset");
+    CK(mlp_forward_tc(st, S, L->Wt.as<unsigned char>(), L->Pq.as<float>(), L->Xt.as<unsigned char>(), ncal,
+                      L->H1.as<unsigned char>(), L->H2.as<unsigned char>(), Ycal, S.dout, h->buf[B_STATUS].as<int>(),
+                      &launches),
+       "network forward");
+    std::vector<float> y((size_t)ncal * S.dout);
+    CK(cudaMemcpyAsync(y.data(), Ycal, 4 * y.size(), cudaMemcpyDeviceToHost, st), "D2H");
+    int stat = 0;
+    CK(cudaMemcpyAsync(&stat, h->buf[B_STATUS].p, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "calibration");
+    if (stat & 16) return fail(h, LGPU_ERR_CUDA, "network forward: tensor-core pipeline wait timed out");
+    std::vector<float> sc(ncal);
+    for (int r = 0; r < ncal; r++) {
+      double q = 0.0;
+      for (int e = 0; e < S.dout; e++) q += (double)y[(size_t)r * S.dout + e] * y[(size_t)r * S.dout + e];
+      sc[r] = (float)std::sqrt(q / S.dout);
+    }
+    std::sort(sc.begin(), sc.end());
+    const double qf = 1.0 - (double)L->cfg.gate_frac;
+    L->tau = L->cfg.gate_frac <= 0.0f ? 3.0e38f : sc[(size_t)std::min<double>(ncal - 1, std::floor(qf * (ncal - 1)))];
+  }
+  L->trained = true;
+  L->st.tau = L->tau;
+  return LGPU_OK;
+}
+
+// exact solves (PLAIN Gram + split eigensolve) of a column list into the
+// compact arrays of the learned state (rows 0..n)
+static int learned_exact(lgpu_handle *h, const ObsSorted &os, int n, int &launches) {
+  LearnState *L = h->learn;
+  if (n <= 0) return LGPU_OK;
+  cudaStream_t st = h->st;
+  const int k = h->k;
+  GramArgs ga;
+  ga.nunits = n;
+  ga.groups = 1;
+  ga.k = k;
+  ga.kp = h->kp;
+  ga.active = L->ecols.as<int>();
+  ga.cp = h->buf[B_CP].as<ColPar>();
+  ga.loc = h->loc;
+  ga.obs = os;
+  ga.geom = h->buf[B_GEOM].as<IndexGeom>();
+  ga.G = L->Gsub.as<float>();
+  ga.nkept = L->nksub.as<int>();
+  ga.diag_obscount = h->buf[B_DOBSC].as<float>();
+  ga.diag_lg_obscount = h->buf[B_DLGC].as<float>();
+  ga.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
+  ga.ncol = h->ncol;
+  CK(launch_gram(st, ga, &launches), "gram kernel");
+  EigArgs ea;
+  ea.nunits = n;
+  ea.k = k;
+  ea.infl = 1.0f;
+  ea.G = L->Gsub.as<float>();
+  ea.nkept = L->nksub.as<int>();
+  ea.T = L->Tsub.as<float>();
+  ea.wbar = L->wsub.as<float>();
+  ea.status = h->buf[B_STATUS].as<int>();
+  EigSplit sp;
+  int batch = 0;
+  int rc = eig_scratch(h, n, sp, batch);
+  if (rc != LGPU_OK) return rc;
+  if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
+  else CK(launch_eig_split(st, ea, sp, batch, 0, n, &launches), "eigen kernels");
+  return LGPU_OK;
+}
+
+static int learned_run(lgpu_handle *h) {
+  LearnState *L = h->learn;
+  if (!L) return fail(h, LGPU_ERR_ORDER, "LEARNED variant before learn_init");
+  if (!L->trained) return fail(h, LGPU_ERR_ORDER, "LEARNED variant before learn_train");
+  if (h->bound_state) return fail(h, LGPU_ERR_UNSUPPORTED, "the LEARNED variant with a bound state");
+  ObsSorted os;
+  int launches = 0;
+  int rc = prepare_run(h, os, launches);
+  if (rc != LGPU_OK) return rc;
+  cudaStream_t st = h->st;
+  const int k = h->k;
+  const MlpShape &S = L->shape;
+  // exact set: coarse lattice, judge sample, columns without four coarse neighbours
+  std::vector<int> ex(L->coarse);
+  const int ncoarse = (int)ex.size();
+  unsigned long long rs = mix64(L->cfg.seed ^ (0x1234567ull + L->runs++));
+  std::vector<int> judge;
+  for (int c : L->fine_ok)
+    if (unif01(rs) < (double)L->cfg.judge_frac) judge.push_back(c);
+  ex.insert(ex.end(), judge.begin(), judge.end());
+  ex.insert(ex.end(), L->fine_miss.begin(), L->fine_miss.end());
+  const int nex = (int)ex.size(), nj = (int)judge.size();
+  const int nf = (int)L->fine_ok.size();
+  CK(L->ecols.ensure(4 * (size_t)std::max(1, h->nact)), "alloc");
+  CK(cudaMemcpyAsync(L->ecols.p, ex.data(), 4 * (size_t)nex, cudaMemcpyHostToDevice, st), "H2D exact set");
+  CK(cudaEventRecord(L->ev[0], st), "event");
+  if ((rc = learned_exact(h, os, nex, launches)) != LGPU_OK) return rc;
+  CK(cudaEventRecord(L->ev[1], st), "event");
+  // network inputs of the columns with four coarse neighbours
+  CK(lrn_obsfeat(st, nf, L->d_fine.as<int>(), h->buf[B_CP].as<ColPar>(), h->loc, os, h->buf[B_GEOM].as<IndexGeom>(),
+                 L->feat.as<float>(), L->nkf.as<int>(), &launches),
+     "learned features");
+  LrnInterpArgs ia;
+  ia.nfine = nf;
+  ia.cols = L->d_fine.as<int>();
+  ia.nx = L->cfg.nx;
+  ia.ny = L->cfg.ny;
+  ia.s = L->cfg.stride;
+  ia.k = k;
+  ia.din = S.din;
+  ia.dout = S.dout;
+  ia.Ts = L->Tsub.as<float>();
+  ia.ws = L->wsub.as<float>();
+  ia.src_of_col = L->d_rank.as<int>();   // coarse rows come first in the exact set
+  ia.feat = L->feat.as<float>();
+  ia.lat = h->buf[B_LAT].as<float>();
+  ia.mu = L->mu_in.as<float>();
+  ia.sd = L->sd_in.as<float>();
+  ia.X = L->X.as<float>();
+  ia.ldx = S.din;
+  ia.flag = L->flag.as<int>();
+  ia.Tex = nullptr;
+  ia.wex = nullptr;
+  ia.col2act = h->buf[B_COL2ACT].as<int>();
+  ia.Yt = nullptr;
+  ia.ldy = 0;
+  CK(L->X.ensure(4 * (size_t)std::max(1, nf) * S.din), "alloc");
+  CK(L->Yn.ensure(4 * (size_t)std::max(1, nf) * S.dout), "alloc");
+  CK(L->Xt.ensure(((size_t)std::max(1, nf) + 127) / 128 * 128 * (size_t)S.k1 * 2), "alloc");
+  CK(L->H1.ensure(mlp_act_bytes(S, std::max(1, nf))), "alloc");
+  CK(L->H2.ensure(mlp_act_bytes(S, std::max(1, nf))), "alloc");
+  ia.X = L->X.as<float>();
+  CK(lrn_interp(st, ia, &launches), "learned interpolation");
+  CK(mlp_tile_input(st, S, L->X.as<float>(), nf, S.din, L->Xt.as<unsigned char>()), "tile input");
+  CK(cudaEventRecord(L->ev[2], st), "event");
+  CK(mlp_forward_tc(st, S, L->Wt.as<unsigned char>(), L->Pq.as<float>(), L->Xt.as<unsigned char>(), nf,
+                    L->H1.as<unsigned char>(), L->H2.as<unsigned char>(), L->Yn.as<float>(), S.dout,
+                    h->buf[B_STATUS].as<int>(), &launches),
+     "network forward");
+  CK(cudaEventRecord(L->ev[3], st), "event");
+  CK(cudaMemsetAsync(L->gate_n.p, 0, 16, st), "memset");
+  LrnApplyArgs aa;
+  aa.nfine = nf;
+  aa.cols = L->d_fine.as<int>();
+  aa.nx = L->cfg.nx;
+  aa.ny = L->cfg.ny;
+  aa.s = L->cfg.stride;
+  aa.k = k;
+  aa.dout = S.dout;
+  aa.Ts = L->Tsub.as<float>();
+  aa.ws = L->wsub.as<float>();
+  aa.src_of_col = L->d_rank.as<int>();
+  aa.Yn = L->Yn.as<float>();
+  aa.ldy = S.dout;
+  aa.mu_out = L->mu_out.as<float>();
+  aa.sd_out = L->sd_out.as<float>();
+  aa.tau = L->tau;
+  aa.net = L->use_net;
+  aa.flag = L->flag.as<int>();
+  aa.nk_fine = L->nkf.as<int>();
+  aa.col2act = h->buf[B_COL2ACT].as<int>();
+  aa.T = h->buf[B_T].as<float>();
+  aa.nkept = h->buf[B_NKEPT].as<int>();
+  aa.gate_cols = L->gate.as<int>();
+  aa.gate_n = L->gate_n.as<int>();
+  aa.score = nullptr;
+  CK(lrn_apply(st, aa, &launches), "learned apply");
+  // judge the network on the judged columns it did not send back, then put
+  // every exact transform in place
+  int ngate = 0;
+  CK(cudaMemcpyAsync(&ngate, L->gate_n.p, 4, cudaMemcpyDeviceToHost, st), "D2H gate count");
+  CK(cudaStreamSynchronize(st), "gate count");
+  CK(lrn_mark(st, ngate, L->gate.as<int>(), L->d_mark.as<int>(), 1), "mark");
+  CK(cudaMemsetAsync(L->jacc.p, 0, 16, st), "memset");
+  std::vector<int> jsub(nj);
+  for (int i = 0; i < nj; i++) jsub[i] = ncoarse + i;
+  DevBuf &jb = h->buf[B_LIST_IDX];
+  CK(jb.ensure(8 * (size_t)std::max(1, nj)), "alloc");
+  CK(cudaMemcpyAsync(jb.p, jsub.data(), 4 * (size_t)nj, cudaMemcpyHostToDevice, st), "H2D");
+  CK(lrn_judge(st, nj, L->ecols.as<int>() + ncoarse, jb.as<int>(), L->Tsub.as<float>(), h->buf[B_T].as<float>(),
+               h->buf[B_COL2ACT].as<int>(), L->d_mark.as<int>(), k, L->jacc.as<float>(), &launches),
+     "judge");
+  CK(lrn_mark(st, ngate, L->gate.as<int>(), L->d_mark.as<int>(), 0), "unmark");
+  CK(lrn_scatter(st, nex, L->ecols.as<int>(), h->buf[B_COL2ACT].as<int>(), L->Tsub.as<float>(), L->nksub.as<int>(), k,
+                 h->buf[B_T].as<float>(), h->buf[B_NKEPT].as<int>(), &launches),
+     "exact transforms");
+  CK(cudaEventRecord(L->ev[4], st), "event");
+  // the gate's columns, solved exactly
+  if (ngate > 0) {
+    CK(cudaMemcpyAsync(L->ecols.p, L->gate.p, 4 * (size_t)ngate, cudaMemcpyDeviceToDevice, st), "D2D");
+    if ((rc = learned_exact(h, os, ngate, launches)) != LGPU_OK) return rc;
+    CK(lrn_scatter(st, ngate, L->ecols.as<int>(), h->buf[B_COL2ACT].as<int>(), L->Tsub.as<float>(),
+                   L->nksub.as<int>(), k, h->buf[B_T].as<float>(), h->buf[B_NKEPT].as<int>(), &launches),
+       "exact transforms");
+  }
+  CK(cudaEventRecord(L->ev[5], st), "event");
+  CK(cudaEventRecord(h->ev[3], st), "event");
+  // update of every column
+  UpdateArgs ua = update_args(h);
+  CK(cudaEventRecord(h->ev_chunk[0][1], st), "event");
+  CK(launch_update(st, ua, &launches), "update kernel");
+  CK(cudaEventRecord(h->ev_chunk[0][2], st), "event");
+  CK(cudaEventRecord(h->ev[5], st), "event");
+  int stat4[4] = {0, 0, 0, 0};
+  float jacc[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(stat4, h->buf[B_STATUS].p, 16, cudaMemcpyDeviceToHost, st), "D2H status");
+  CK(cudaMemcpyAsync(jacc, L->jacc.p, 16, cudaMemcpyDeviceToHost, st), "D2H judge");
+  CK(cudaStreamSynchronize(st), "solver_run");
+  float ms[3];
+  for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
+  float le[5];
+  for (int i = 0; i < 5; i++) CK(cudaEventElapsedTime(&le[i], L->ev[i], L->ev[i + 1]), "timing");
+  h->tim.index_ms = ms[0];
+  h->tim.prep_ms = ms[1];
+  CK(cudaEventElapsedTime(&h->tim.gram_ms, h->ev[2], h->ev[3]), "timing");
+  h->tim.tiles_ms = 0.0f;
+  h->tim.eig_ms = 0.0f;
+  CK(cudaEventElapsedTime(&h->tim.update_ms, h->ev_chunk[0][1], h->ev_chunk[0][2]), "timing");
+  CK(cudaEventElapsedTime(&h->tim.total_ms, h->ev[0], h->ev[5]), "timing");
+  h->tim.launches = launches;
+  h->tim.variant = LGPU_VARIANT_LEARNED;
+  h->tim.units = h->nunits;
+  h->tim.kept_pairs = -1;
+  h->tim.mma_chunks = 0;
+  h->tim.mma_n = 0;
+  L->st.coarse = ncoarse;
+  L->st.judged = nj;
+  L->st.fallback = (int)L->fine_miss.size();
+  L->st.gated = ngate;
+  L->st.inferred = nf - ngate;
+  L->st.judge_rms = jacc[2] > 0.0f ? std::sqrt(jacc[0] / jacc[2]) / (float)k : 0.0f;
+  L->st.judge_ref_rms = jacc[2] > 0.0f ? std::sqrt(jacc[1] / jacc[2]) / (float)k : 0.0f;
+  L->st.exact_ms = le[0] + le[4];
+  L->st.feature_ms = le[1];
+  L->st.network_ms = le[2];
+  L->st.apply_ms = le[3];
+  h->ran = true;
+  const int status = stat4[0];
+  if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
+  if (status & 2) return fail(h, LGPU_ERR_EIG, "non-positive eigenvalue in at least one unit");
+  if (status & 4) return fail(h, LGPU_ERR_NONFINITE, "non-finite analysis mean or spread");
+  if (status & 16) return fail(h, LGPU_ERR_CUDA, "tensor-core pipeline wait timed out");
+  if (status & 32) return fail(h, LGPU_ERR_CUDA, "internal: malformed eigensolver rotation log");
+  if (status & 64) return fail(h, LGPU_ERR_CUDA, "update stage copy wait timed out");
+  return LGPU_OK;
+}
+
+// ---- network verification entry (standalone)
+int lgpu_mlp_debug(int device, int din, int hidden, int dout, int rows, const float *params, const float *x,
+                   const float *t, float *loss, float *grad, float *y_simt, float *y_tc) {
+  if (din <= 0 || hidden <= 0 || hidden % 16 || dout <= 0 || rows <= 0 || !params || !x) return LGPU_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return LGPU_ERR_CUDA;
+  MlpShape S;
+  S.din = din;
+  S.k1 = (din + 15) & ~15;
+  S.H = hidden;
+  S.dout = dout;
+  const size_t np = mlp_param_count(S);
+  std::vector<void *> bufs;
+  auto take = [&](size_t bytes) -> void * {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+    bufs.push_back(p);
+    return p;
+  };
+  auto release = [&]() { for (void *p : bufs) cudaFree(p); };
+  float *P = (float *)take(4 * np), *Pq = (float *)take(4 * np), *G = (float *)take(4 * np);
+  float *X = (float *)take(4 * (size_t)rows * din), *Xq = (float *)take(4 * (size_t)rows * din);
+  float *T = (float *)take(4 * (size_t)rows * dout), *Y = (float *)take(4 * (size_t)rows * dout);
+  float *scr = (float *)take(4 * mlp_train_scratch_floats(S, rows));
+  unsigned char *Wt = (unsigned char *)take(mlp_tiled_weight_bytes(S));
+  unsigned char *Xt = (unsigned char *)take(((size_t)rows + 127) / 128 * 128 * (size_t)S.k1 * 2);
+  unsigned char *H1 = (unsigned char *)take(mlp_act_bytes(S, rows)), *H2 = (unsigned char *)take(mlp_act_bytes(S, rows));
+  float *acc = (float *)take(16);
+  int *status = (int *)take(16);
+  for (void *p : bufs)
+    if (!p) { release(); return LGPU_ERR_NOMEM; }
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaSuccess;
+  int rc = LGPU_OK;
+  auto ck = [&](cudaError_t x2) { if (e == cudaSuccess && x2 != cudaSuccess) e = x2; };
+  ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  ck(cudaMemcpyAsync(P, params, 4 * np, cudaMemcpyHostToDevice, st));
+  ck(cudaMemcpyAsync(X, x, 4 * (size_t)rows * din, cudaMemcpyHostToDevice, st));
+  if (t) ck(cudaMemcpyAsync(T, t, 4 * (size_t)rows * dout, cudaMemcpyHostToDevice, st));
+  else ck(cudaMemsetAsync(T, 0, 4 * (size_t)rows * dout, st));
+  ck(mlp_round(st, (long long)np, P, Pq));
+  ck(mlp_round(st, (long long)rows * din, X, Xq));
+  ck(cudaMemsetAsync(acc, 0, 16, st));
+  ck(cudaMemsetAsync(status, 0, 16, st));
+  int nparts = 0;
+  ck(mlp_grad(st, S, Pq, Xq, T, rows, G, scr, &nparts, nullptr));
+  ck(mlp_loss_accumulate(st, mlp_loss_parts(S, scr, rows), nparts, acc));
+  // the forward output of the gradient pass is the CUDA-core forward
+  const size_t yoff = (size_t)rows * 4 * S.H;
+  if (y_simt) ck(cudaMemcpyAsync(y_simt, scr + yoff, 4 * (size_t)rows * dout, cudaMemcpyDeviceToHost, st));
+  if (grad) ck(cudaMemcpyAsync(grad, G, 4 * np, cudaMemcpyDeviceToHost, st));
+  float a = 0.0f;
+  ck(cudaMemcpyAsync(&a, acc, 4, cudaMemcpyDeviceToHost, st));
+  if (y_tc) {
+    int launches = 0;
+    ck(mlp_tile_weights(st, S, Pq, Wt));
+    ck(mlp_tile_input(st, S, Xq, rows, din, Xt));
+    ck(mlp_forward_tc(st, S, Wt, Pq, Xt, rows, H1, H2, Y, dout, status, &launches));
+    ck(cudaMemcpyAsync(y_tc, Y, 4 * (size_t)rows * dout, cudaMemcpyDeviceToHost, st));
+  }
+  int stat = 0;
+  ck(cudaMemcpyAsync(&stat, status, 4, cudaMemcpyDeviceToHost, st));
+  ck(cudaStreamSynchronize(st));
+  if (st) cudaStreamDestroy(st);
+  release();
+  if (e != cudaSuccess) { (void)cudaGetLastError(); return LGPU_ERR_CUDA; }
+  if (stat & 16) rc = LGPU_ERR_CUDA;
+  if (loss) *loss = a / ((float)rows * (float)dout);
+  return rc;
+}

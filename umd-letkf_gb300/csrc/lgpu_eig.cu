@@ -236,6 +236,7 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
     float acc = 0.0f;
     for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], p[l], acc);
     w[i] = acc;
+    if (a.wbar) a.wbar[(size_t)unit * k + i] = acc;
   }
   TM.sync();
   // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
@@ -660,6 +661,7 @@ cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
                              int *status) {
   EigArgs a;
+  a.wbar = nullptr;
   a.nunits = nunits;
   a.k = k;
   a.infl = 1.0f;

@@ -428,6 +428,7 @@ struct EigArgs {
   const float *G;
   const int *nkept;
   float *T;               // [unit][k][k]
+  float *wbar;            // [unit][k] mean weights, or null
   int *status;            // [1] accumulated error bits
 };
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
@@ -464,6 +465,83 @@ struct UpdateArgs {
   int *status;
 };
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches);
+
+// ---- weight-correction network of the learned form (lgpu_mlp.cu) ----
+struct MlpShape {
+  int din, k1, H, dout;   // k1 = din rounded up to 16
+};
+size_t mlp_param_count(const MlpShape &s);
+void mlp_param_offsets(const MlpShape &s, size_t off[6]);   // W1 b1 W2 b2 W3 b3
+size_t mlp_tiled_weight_bytes(const MlpShape &s);
+size_t mlp_act_bytes(const MlpShape &s, int rows);
+size_t mlp_train_scratch_floats(const MlpShape &s, int rows);
+float *mlp_loss_parts(const MlpShape &s, float *scr, int rows);
+__host__ __device__ size_t mlp_tile_off(int r, int kk, int K, int rb);
+cudaError_t mlp_tile_weights(cudaStream_t st, const MlpShape &s, const float *wq, unsigned char *tiled);
+cudaError_t mlp_tile_input(cudaStream_t st, const MlpShape &s, const float *x, int rows, int ld, unsigned char *tiled);
+cudaError_t mlp_forward_tc(cudaStream_t st, const MlpShape &s, const unsigned char *wtiled, const float *bias_base,
+                           const unsigned char *x, int rows, unsigned char *h1, unsigned char *h2, float *y, int ldy,
+                           int *status, int *launches);
+cudaError_t mlp_forward_simt(cudaStream_t st, const MlpShape &s, const float *wq, const float *x, int rows, float *y,
+                             float *scr);
+cudaError_t mlp_grad(cudaStream_t st, const MlpShape &s, const float *wq, const float *x, const float *t, int rows,
+                     float *grad, float *scr, int *nparts, const float *wout);
+cudaError_t mlp_adam(cudaStream_t st, long long n, float *w, float *wq, const float *g, float *m, float *v, float lr,
+                     int step);
+cudaError_t mlp_round(cudaStream_t st, long long n, const float *w, float *wq);
+
+// ---- learned analysis form (lgpu_learn.cu) ----
+struct LrnInterpArgs {
+  int nfine;
+  const int *cols;
+  int nx, ny, s, k, din, dout;
+  const float *Ts, *ws;       // coarse solutions: T = W + w-bar 1^T [src][k][k], w-bar [src][k]
+  const int *src_of_col;      // [ncol] row of the coarse solution or -1
+  const float *feat;          // [nfine][16] (0..9 from k_lrn_obsfeat)
+  const float *lat;
+  const float *mu, *sd;       // input standardisation [din], or null (raw rows)
+  float *X;                   // [nfine][din] network input rows (row f at X + f * ldx)
+  long long ldx;
+  int *flag;                  // [nfine] 1 = a coarse neighbour has no solution
+  const float *Tex, *wex;     // collecting: exact T / w-bar of every unit
+  const int *col2act;
+  float *Yt;                  // collecting: residual targets [nfine][dout] (row f at Yt + f * ldy), or null
+  long long ldy;
+};
+
+struct LrnApplyArgs {
+  int nfine;
+  const int *cols;
+  int nx, ny, s, k, dout;
+  const float *Ts, *ws;
+  const int *src_of_col;
+  const float *Yn;            // network outputs [nfine][ldy] (standardised residuals)
+  long long ldy;
+  const float *mu_out, *sd_out;
+  float tau;                  // gate: RMS of the standardised output above tau -> exact
+  int net;                    // 0: interpolation only (zero correction, no score gate)
+  const int *flag;
+  const int *nk_fine;         // [nfine] kept count
+  const int *col2act;
+  float *T;                   // [unit][k][k]
+  int *nkept;                 // [unit]
+  int *gate_cols, *gate_n;    // exact fallback list
+  float *score;               // [nfine] or null
+};
+
+cudaError_t lrn_obsfeat(cudaStream_t st, int nfine, const int *cols, const ColPar *cp, const DevLoc &loc,
+                        const ObsSorted &obs, const IndexGeom *geom, float *feat, int *nkept, int *launches);
+cudaError_t lrn_interp(cudaStream_t st, const LrnInterpArgs &a, int *launches);
+cudaError_t lrn_apply(cudaStream_t st, const LrnApplyArgs &a, int *launches);
+cudaError_t lrn_judge(cudaStream_t st, int nj, const int *jcols, const int *jsub, const float *Tsub, const float *T,
+                      const int *col2act, const int *gate_mark, int k, float *acc, int *launches);
+cudaError_t lrn_mark(cudaStream_t st, int n, const int *cols, int *mark, int v);
+cudaError_t lrn_scatter(cudaStream_t st, int n, const int *cols, const int *col2act, const float *Tsub,
+                        const int *nk_sub, int k, float *T, int *nkept, int *launches);
+cudaError_t lrn_colstats(cudaStream_t st, const float *M, long long rows, int n, long long ld, float *mu, float *sd);
+cudaError_t lrn_batch(cudaStream_t st, int b, const int *idx, const float *X, long long ldx, int din, const float *Y,
+                      long long ldy, int dout, const float *mu, const float *sd, const float *muo, const float *sdo,
+                      float *Xb, float *Yb);
 
 // list emission for verification
 cudaError_t launch_obslist(cudaStream_t st, int col, int gid, int group_slot, const ColPar *cp_col, const DevLoc &loc,

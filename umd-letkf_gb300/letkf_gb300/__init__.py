@@ -83,8 +83,25 @@ class Timings(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
-VARIANT_AUTO, VARIANT_PLAIN, VARIANT_BATCHED_TC = 0, 1, 2
-VARIANTS = {"auto": 0, "plain": 1, "batched": 2}
+VARIANT_AUTO, VARIANT_PLAIN, VARIANT_BATCHED_TC, VARIANT_LEARNED = 0, 1, 2, 3
+VARIANTS = {"auto": 0, "plain": 1, "batched": 2, "learned": 3}
+
+
+class _LearnCfg(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("stride", ctypes.c_int), ("hidden", ctypes.c_int),
+                ("judge_frac", ctypes.c_float), ("gate_frac", ctypes.c_float), ("sample_frac", ctypes.c_float),
+                ("train_cap", ctypes.c_int), ("seed", ctypes.c_uint64)]
+
+
+class LearnStats(ctypes.Structure):
+    _fields_ = [("coarse", ctypes.c_int), ("judged", ctypes.c_int), ("fallback", ctypes.c_int),
+                ("gated", ctypes.c_int), ("inferred", ctypes.c_int), ("judge_rms", ctypes.c_float),
+                ("judge_ref_rms", ctypes.c_float), ("tau", ctypes.c_float), ("train_rows", ctypes.c_longlong),
+                ("exact_ms", ctypes.c_float), ("feature_ms", ctypes.c_float), ("network_ms", ctypes.c_float),
+                ("apply_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_solver_init", "lgpu_loc_init",
            "lgpu_loc_maxgroups", "lgpu_set_grid", "lgpu_set_state", "lgpu_set_obs", "lgpu_solver_run",
@@ -92,7 +109,9 @@ EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error",
            "lgpu_debug_metric", "lgpu_debug_gc", "lgpu_host_alloc", "lgpu_host_free", "lgpu_flush_l2",
            "lgpu_get_obslist_noalloc", "lgpu_set_obs_raw", "lgpu_set_state_members", "lgpu_get_background",
            "lgpu_get_obs_prepared", "lgpu_debug_transform", "lgpu_bind_state",
-           "lgpu_debug_weight"]
+           "lgpu_debug_weight", "lgpu_learn_init", "lgpu_learn_collect", "lgpu_learn_train", "lgpu_learn_stats_get",
+           "lgpu_learn_param_count", "lgpu_learn_get_params", "lgpu_learn_set_params", "lgpu_mlp_debug",
+           "lgpu_learn_set_network"]
 
 _lib = None
 
@@ -138,6 +157,17 @@ def lib(path=None):
     L.lgpu_debug_transform.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP]
     L.lgpu_get_obs_prepared.argtypes = [H, FP, FP, FP, FP, FP, FP]
     L.lgpu_bind_state.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP, FP, ctypes.c_int, ctypes.POINTER(_Var)]
+    L.lgpu_learn_init.argtypes = [H, ctypes.POINTER(_LearnCfg)]
+    L.lgpu_learn_collect.argtypes = [H, ctypes.POINTER(ctypes.c_longlong)]
+    L.lgpu_learn_train.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_float, FP]
+    L.lgpu_learn_stats_get.argtypes = [H, ctypes.POINTER(LearnStats)]
+    L.lgpu_learn_set_network.argtypes = [H, ctypes.c_int]
+    L.lgpu_learn_param_count.argtypes = [H]
+    L.lgpu_learn_param_count.restype = ctypes.c_longlong
+    L.lgpu_learn_get_params.argtypes = [H, FP, ctypes.c_longlong]
+    L.lgpu_learn_set_params.argtypes = [H, FP, ctypes.c_longlong]
+    L.lgpu_mlp_debug.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, FP, FP, FP, FP,
+                                 FP, FP, FP]
     if path is None:
         _lib = L
     return L
@@ -432,6 +462,43 @@ class Solver:
                                       _fp(d["lg_obsloc"])))
         return d
 
+    # -- learned form (no counterpart in the reference)
+    def learn_init(self, nx, ny, stride=4, hidden=512, judge_frac=0.02, gate_frac=0.05, sample_frac=0.25,
+                   train_cap=200000, seed=0):
+        c = _LearnCfg(int(nx), int(ny), int(stride), int(hidden), float(judge_frac), float(gate_frac),
+                      float(sample_frac), int(train_cap), int(seed))
+        return self._ck(self.L.lgpu_learn_init(self.h, ctypes.byref(c)))
+
+    def learn_collect(self):
+        n = ctypes.c_longlong(0)
+        self._ck(self.L.lgpu_learn_collect(self.h, ctypes.byref(n)))
+        return n.value
+
+    def learn_train(self, epochs=4, batch=1024, lr=1e-3):
+        loss = np.zeros(1, np.float32)
+        self._ck(self.L.lgpu_learn_train(self.h, int(epochs), int(batch), float(lr), _fp(loss)))
+        return float(loss[0])
+
+    def learn_stats(self):
+        st = LearnStats()
+        self._ck(self.L.lgpu_learn_stats_get(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def learn_set_network(self, on=True):
+        self._ck(self.L.lgpu_learn_set_network(self.h, 1 if on else 0))
+
+    def learn_params(self):
+        n = self.L.lgpu_learn_param_count(self.h)
+        if n < 0:
+            raise LgpuError(6, "learn_params before learn_init")
+        p = np.empty(n, np.float32)
+        self._ck(self.L.lgpu_learn_get_params(self.h, _fp(p), n))
+        return p
+
+    def learn_set_params(self, p):
+        p = _f32(p)
+        self._ck(self.L.lgpu_learn_set_params(self.h, _fp(p), p.size))
+
     def timings(self):
         t = Timings()
         self._ck(self.L.lgpu_get_timings(self.h, ctypes.byref(t)))
@@ -498,6 +565,37 @@ class Solver:
         out = np.zeros(2 * n, np.float32)
         self._ck(self.L.lgpu_debug_gc(self.h, n, _fp(z), _fp(L), _fp(out)))
         return out[:n], out[n:]
+
+
+def mlp_param_shapes(din, hidden, dout):
+    """Shapes of the network parameters in their flat order (W1, b1, W2, b2,
+    W3, b3; weights row-major [out][in])."""
+    return [(hidden, din), (hidden,), (hidden, hidden), (hidden,), (dout, hidden), (dout,)]
+
+
+def mlp_debug(params, x, t=None, hidden=512, device=0):
+    """The network kernels on one batch (verification): returns loss, the
+    gradient from the training kernels, the CUDA-core forward output and the
+    tensor-core forward output."""
+    L = lib()
+    x = _f32(x)
+    rows, din = x.shape
+    params = _f32(params)
+    # dout from the parameter count: H*din + H + H*H + H + dout*H + dout
+    rest = params.size - (hidden * din + hidden + hidden * hidden + hidden)
+    dout = rest // (hidden + 1)
+    if rest != dout * (hidden + 1):
+        raise ValueError("parameter count does not match din=%d hidden=%d" % (din, hidden))
+    t = np.zeros((rows, dout), np.float32) if t is None else _f32(t)
+    loss = np.zeros(1, np.float32)
+    grad = np.empty(params.size, np.float32)
+    ys = np.empty((rows, dout), np.float32)
+    yt = np.empty((rows, dout), np.float32)
+    rc = L.lgpu_mlp_debug(int(device), din, int(hidden), int(dout), rows, _fp(params), _fp(x), _fp(t), _fp(loss),
+                          _fp(grad), _fp(ys), _fp(yt))
+    if rc != LGPU_OK:
+        raise LgpuError(rc, "lgpu_mlp_debug failed")
+    return {"loss": float(loss[0]), "grad": grad, "y_simt": ys, "y_tc": yt}
 
 
 class PinnedArray:

@@ -94,7 +94,74 @@ def _L():
         _lib = ctypes.CDLL(synth_lib_path())
         _lib.lgs_generate.argtypes = [ctypes.POINTER(_Opt), ctypes.POINTER(_Prob)]
         _lib.lgs_free.argtypes = [ctypes.POINTER(_Prob)]
+        _lib.lgs_forecast.argtypes = [ctypes.POINTER(_Prob), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int]
+        _lib.lgs_observe.argtypes = [ctypes.POINTER(_Opt), ctypes.POINTER(_Prob), ctypes.c_uint64]
+        _lib.lgs_free_obs.argtypes = [ctypes.POINTER(_Prob)]
     return _lib
+
+
+def _view(prob):
+    """A _Prob over the Problem's own grid / state arrays (no copies)."""
+    p = _Prob()
+    p.nx, p.ny, p.nz, p.ncol, p.k, p.ns = prob.nx, prob.ny, prob.nz, prob.ncol, prob.k, prob.ns
+    p.nvars = len(prob.vars)
+    for i, v in enumerate(prob.vars):
+        p.vars[i].name = v["name"].encode()[:15]
+        p.vars[i].grid_s_idx = v["grid_s_idx"]
+        p.vars[i].levels = v["levels"]
+        p.vars[i].ana_inc_max = v["ana_inc_max"]
+        p.vars[i].ana_bounds[0], p.vars[i].ana_bounds[1] = v["ana_bounds"]
+    for name in ("lev_depth", "lat", "lon", "state", "mean", "sprd", "truth"):
+        a = getattr(prob, name)
+        assert a.dtype == np.float32 and a.flags.c_contiguous
+        setattr(p, name, a.ctypes.data_as(FP))
+    assert prob.mask.dtype == np.int32 and prob.mask.flags.c_contiguous
+    p.mask = prob.mask.ctypes.data_as(IP)
+    return p
+
+
+def forecast(prob, u=0.5, kappa=1.0e3, dt=21600.0, nthreads=0):
+    """One forecast step of a cycling experiment, in place: members and truth
+    advected by a zonal jet u (m/s) over dt (s) and diffused with kappa
+    (m^2/s); background mean / perturbations / spread recomputed."""
+    p = _view(prob)
+    rc = _L().lgs_forecast(ctypes.byref(p), float(u), float(kappa), float(dt), int(nthreads))
+    if rc != 0:
+        raise RuntimeError("lgs_forecast failed (%d)" % rc)
+    return prob
+
+
+def observe(prob, seed, n_obs=0, n_clusters=0, cluster_sigma_m=0.0, centre_seed=1003):
+    """A copy of prob with new clustered observations of its current
+    background and truth: the C3/C4 network with cluster centres from
+    `centre_seed` (persistent from cycle to cycle), positions and errors
+    drawn with `seed`."""
+    from dataclasses import replace
+    p = _view(prob)
+    o = _Opt()
+    o.seed = int(seed)
+    o.n_obs = int(n_obs)
+    o.n_clusters = int(n_clusters)
+    o.cluster_sigma_m = float(cluster_sigma_m)
+    rc = _L().lgs_observe(ctypes.byref(o), ctypes.byref(p), int(centre_seed))
+    try:
+        if rc != 0:
+            raise RuntimeError("lgs_observe failed (%d)" % rc)
+        n, k = p.nobs, prob.k
+
+        def arr(ptr, shape, dt=np.float32):
+            m = int(np.prod(shape))
+            if m == 0:
+                return np.zeros(shape, dt)
+            return np.ctypeslib.as_array(ptr, (m,)).astype(dt, copy=True).reshape(shape)
+
+        return replace(prob, olat=arr(p.olat, (n,)), olon=arr(p.olon, (n,)), oz=arr(p.oz, (n,)),
+                       otime=arr(p.otime, (n,)), oval=arr(p.oval, (n,)), oerr=arr(p.oerr, (n,)),
+                       oobsid=arr(p.oobsid, (n,), np.int32), oplatid=arr(p.oplatid, (n,), np.int32),
+                       hx=arr(p.hx, (n, k)), hx_mean=arr(p.hx_mean, (n,)))
+    finally:
+        _L().lgs_free_obs(ctypes.byref(p))
 
 
 def generate(workload, seed=0, nthreads=0, **overrides):

@@ -10,6 +10,9 @@ sections a reference YAML configuration would carry for them.
             with a constant 60 km length scale (support ~219 km)
   c4        1440x720x50 (T, S; 100 slabs), k=100, 1,000,000 clustered obs,
             loc_novrt 60 km as c3
+  c5        learned form: 720x360x40, k=32, c3's clustered network (persistent
+            clusters), loc_novrt 400 km, stride-4 coarse lattice, 5 exact
+            training cycles
   c2mid     c2 observations on a 360x180x10 grid (profiling-sized: the same
             local observation counts per column, a fifth of the columns)
   simple3d  test/simple3d-style (k=50, three 3-D variables, two synthetic
@@ -46,6 +49,18 @@ WORKLOADS = {
                localization={"class": "loc_novrt",
                              "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
                solver={}),
+    # learned form: the clustered network of c3 with k = 32 and a 400 km
+    # localisation scale (the transform then varies on scales the stride-4
+    # coarse lattice, 2 degrees, resolves); 5 exact training cycles, truth and
+    # members advanced by a zonal jet of 0.5 m/s with diffusion 1e3 m^2/s
+    # over 6 h between cycles
+    "c5": dict(gen=dict(workload="c3", k=32),
+               localization={"class": "loc_novrt",
+                             "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 400.0e3}]}},
+               solver={},
+               learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.05, sample_frac=0.3, train_cap=300000,
+                          seed=5),
+               cycles=dict(train=5, u=0.5, kappa=1.0e3, dt=21600.0, epochs=12, batch=1024, lr=1e-3)),
     "c4small": dict(gen=dict(workload="c4", nx=180, ny=90, nz=5, n_obs=40000),
                     localization={"class": "loc_novrt",
                                   "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},

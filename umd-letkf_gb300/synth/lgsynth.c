@@ -433,13 +433,14 @@ static int make_obs_c2(const lgs_options *o, lgs_problem *p) {
 
 /* C3/C4: clustered point obs (Gaussian clusters of given sigma + 10% uniform),
  * T/S at a random level, or SSH when the state has it */
-static int make_obs_clustered(const lgs_options *o, lgs_problem *p) {
+static int make_obs_clustered_c(const lgs_options *o, lgs_problem *p, uint64_t centre_seed) {
   if (alloc_obs(p, o->n_obs)) return 2;
-  rng_t r; rng_init(&r, o->seed, 3, 0);
+  rng_t r; rng_init(&r, centre_seed, 3, 0);
   rng_t re; rng_init(&re, o->seed, 4, 0);
   int nc = o->n_clusters > 0 ? o->n_clusters : 1;
   double cen[64][3];
   for (int c = 0; c < nc && c < 64; c++) { double la, lo; random_ocean_point(p, &r, &la, &lo); lonlat_to_xyz(la, lo, cen[c]); }
+  if (centre_seed != o->seed) rng_init(&r, o->seed, 3, 0);   /* positions drawn with the observation seed */
   int has_ssh = p->nvars >= 3;
   for (int i = 0; i < p->nobs; i++) {
     double la, lo;
@@ -503,6 +504,8 @@ static int make_obs_listed(lgs_problem *p, const synth_ob *list, int n) {
   return 0;
 }
 
+static int make_obs_clustered(const lgs_options *o, lgs_problem *p) { return make_obs_clustered_c(o, p, o->seed); }
+
 int lgs_generate(const lgs_options *opt, lgs_problem *out) {
   memset(out, 0, sizeof(*out));
   lgs_options o; lgs_default_options(opt->workload, &o);
@@ -548,4 +551,110 @@ int lgs_generate(const lgs_options *opt, lgs_problem *out) {
   }
   if (rc) lgs_free(out);
   return rc;
+}
+
+/* ---- cycling experiments (the learned analysis form) ----
+ * One forecast step on the regular lattice: every member (mean +
+ * perturbation) and the truth are advected by a zonal wind u (m/s) over dt
+ * seconds (semi-Lagrangian, linear interpolation, periodic in longitude) and
+ * diffused with kappa (m^2/s, one explicit 5-point step, the coefficients
+ * capped at 0.2 for stability near the poles); the background mean,
+ * perturbations and spread are then recomputed (src/letkf_state.F90:326-334).
+ * p holds caller arrays (grid, state, mean, sprd, truth). */
+static void advect_field(const lgs_problem *p, double u, double kappa, double dt, float *f, float *g) {
+  const int nx = p->nx, ny = p->ny;
+  const double dl = 2.0 * PI_D / nx, dphi = PI_D / ny;
+  for (int j = 0; j < ny; j++) {
+    const double phi = (-90.0 + (j + 0.5) * 180.0 / ny) * D2R;
+    const double cphi = fmax(cos(phi), 1e-3);
+    const double sh = u * dt / (EARTH_R * cphi * dl);   /* cells moved eastwards */
+    const double fl = floor(sh);
+    const int is = (int)fl;
+    const double a = sh - fl;
+    for (int i = 0; i < nx; i++) {
+      int i0 = ((i - is) % nx + nx) % nx, i1 = ((i - is - 1) % nx + nx) % nx;
+      g[i + nx * j] = (float)((1.0 - a) * f[i0 + nx * j] + a * f[i1 + nx * j]);
+    }
+  }
+  for (int j = 0; j < ny; j++) {
+    const double phi = (-90.0 + (j + 0.5) * 180.0 / ny) * D2R;
+    const double dx = EARTH_R * fmax(cos(phi), 1e-3) * dl, dy = EARTH_R * dphi;
+    const double cx = fmin(0.2, kappa * dt / (dx * dx)), cy = fmin(0.2, kappa * dt / (dy * dy));
+    const int jm = j > 0 ? j - 1 : j, jp = j < ny - 1 ? j + 1 : j;
+    for (int i = 0; i < nx; i++) {
+      const int im = (i + nx - 1) % nx, ip = (i + 1) % nx;
+      const double c = g[i + nx * j];
+      f[i + nx * j] = (float)(c + cx * (g[ip + nx * j] - 2.0 * c + g[im + nx * j]) +
+                              cy * (g[i + nx * jp] - 2.0 * c + g[i + nx * jm]));
+    }
+  }
+}
+
+int lgs_forecast(lgs_problem *p, double u, double kappa, double dt, int nthreads) {
+  const size_t ncol = (size_t)p->ncol, ns = (size_t)p->ns, k = (size_t)p->k;
+  if (ncol != (size_t)p->nx * p->ny) return 1;
+  const int nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+  const long long ntask = (long long)ns * (long long)(k + 1);
+  int bad = 0;
+#pragma omp parallel num_threads(nth)
+  {
+    float *f = malloc(ncol * sizeof(float)), *g = malloc(ncol * sizeof(float));
+    if (!f || !g) {
+#pragma omp atomic write
+      bad = 1;
+    } else {
+#pragma omp for schedule(dynamic, 1)
+      for (long long t = 0; t < ntask; t++) {
+        const size_t s = (size_t)(t / (long long)(k + 1)), m = (size_t)(t % (long long)(k + 1));
+        if (m < k) {
+          for (size_t c = 0; c < ncol; c++) f[c] = p->state[(c * ns + s) * k + m] + p->mean[c * ns + s];
+        } else {
+          for (size_t c = 0; c < ncol; c++) f[c] = p->truth[c * ns + s];
+        }
+        advect_field(p, u, kappa, dt, f, g);
+        if (m < k) {
+          for (size_t c = 0; c < ncol; c++) p->state[(c * ns + s) * k + m] = f[c];   /* full values for now */
+        } else {
+          for (size_t c = 0; c < ncol; c++) p->truth[c * ns + s] = f[c];
+        }
+      }
+    }
+    free(f);
+    free(g);
+  }
+  if (bad) return 2;
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (size_t cs = 0; cs < ncol * ns; cs++) {
+    float *x = p->state + cs * k;
+    float sum = 0.0f;
+    for (size_t m = 0; m < k; m++) sum += x[m];
+    float mean = sum / (float)k;
+    float dot = 0.0f;
+    for (size_t m = 0; m < k; m++) { x[m] = x[m] - mean; dot += x[m] * x[m]; }
+    p->mean[cs] = mean;
+    p->sprd[cs] = sqrtf(dot / (float)(k - 1));
+  }
+  return 0;
+}
+
+/* New clustered observations of p's current background and truth: the
+ * C3/C4 network with its cluster centres drawn from centre_seed (a persistent
+ * observing network), positions and errors from opt->seed; the observation
+ * arrays are allocated here and freed by lgs_free_obs. */
+int lgs_observe(const lgs_options *opt, lgs_problem *p, uint64_t centre_seed) {
+  lgs_options o;
+  lgs_default_options(LGS_W_C3, &o);
+  o.seed = opt->seed;
+  if (opt->n_obs > 0) o.n_obs = opt->n_obs;
+  if (opt->n_clusters > 0) o.n_clusters = opt->n_clusters;
+  if (opt->cluster_sigma_m > 0) o.cluster_sigma_m = opt->cluster_sigma_m;
+  return make_obs_clustered_c(&o, p, centre_seed);
+}
+
+void lgs_free_obs(lgs_problem *p) {
+  free(p->olat); free(p->olon); free(p->oz); free(p->otime); free(p->oval); free(p->oerr);
+  free(p->oobsid); free(p->oplatid); free(p->oqc); free(p->hx); free(p->hx_mean);
+  p->olat = p->olon = p->oz = p->otime = p->oval = p->oerr = p->hx = p->hx_mean = NULL;
+  p->oobsid = p->oplatid = p->oqc = NULL;
+  p->nobs = 0;
 }

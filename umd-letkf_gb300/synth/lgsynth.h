@@ -87,6 +87,14 @@ void lgs_default_options(int workload, lgs_options *opt);
 int lgs_generate(const lgs_options *opt, lgs_problem *out);
 void lgs_free(lgs_problem *p);
 
+/* Cycling experiments: one forecast step of members and truth (zonal
+ * advection u m/s over dt s, diffusion kappa m^2/s) with the background
+ * statistics recomputed; new clustered observations of the current state
+ * (allocated here, freed by lgs_free_obs).  p may hold caller arrays. */
+int lgs_forecast(lgs_problem *p, double u, double kappa, double dt, int nthreads);
+int lgs_observe(const lgs_options *opt, lgs_problem *p, uint64_t centre_seed);
+void lgs_free_obs(lgs_problem *p);
+
 #ifdef __cplusplus
 }
 #endif
