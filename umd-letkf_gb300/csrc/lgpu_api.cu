@@ -1270,6 +1270,7 @@ struct LearnState {
   DevBuf store_X, store_Y, wbar_all;
   DevBuf bidx, Xb, Yb, scr, lacc;
   DevBuf wout;                                   // per-output loss weights: 1 for W, k for w-bar
+  DevBuf cells;                                  // per-cell observation aggregates (two float4 per cell)
   long long nstore = 0;
   bool stats_ok = false, trained = false;
   unsigned long long runs = 0;
@@ -1287,7 +1288,7 @@ static void learn_free(lgpu_handle *h) {
                    &L->mu_in, &L->sd_in, &L->mu_out, &L->sd_out, &L->feat, &L->nkf, &L->X, &L->Xt, &L->H1, &L->H2,
                    &L->Yn, &L->flag, &L->gate, &L->gate_n, &L->jacc, &L->ecols, &L->Gsub, &L->nksub, &L->Tsub,
                    &L->wsub, &L->store_X, &L->store_Y, &L->wbar_all, &L->bidx, &L->Xb, &L->Yb, &L->scr, &L->lacc,
-                   &L->wout};
+                   &L->wout, &L->cells};
   for (DevBuf *b : all) b->release();
   for (auto &e : L->ev) if (e) cudaEventDestroy(e);
   delete L;
@@ -1498,8 +1499,11 @@ int lgpu_learn_collect(lgpu_handle *h, long long *rows) {
     os.hx = h->buf[B_SHX].as<float>();
     os.idx = h->buf[B_SIDX].as<int>();
     os.cell_start = h->buf[B_CSTART].as<int>();
-    CK(lrn_obsfeat(st, n, L->ecols.as<int>(), h->buf[B_CP].as<ColPar>(), h->loc, os, h->buf[B_GEOM].as<IndexGeom>(),
-                   L->feat.as<float>(), L->nkf.as<int>(), &launches),
+    CK(L->cells.ensure(32 * ((size_t)h->ncell + 1)), "alloc");
+    float4 *c0 = L->cells.as<float4>(), *c1 = c0 + h->ncell;
+    CK(lrn_cellstats(st, h->ncell, os, c0, c1, &launches), "cell aggregates");
+    CK(lrn_obsfeat(st, n, L->ecols.as<int>(), h->buf[B_CP].as<ColPar>(), h->loc, os.cell_start, c0, c1,
+                   h->buf[B_GEOM].as<IndexGeom>(), L->feat.as<float>(), L->nkf.as<int>(), &launches),
        "learned features");
     LrnInterpArgs ia;
     ia.nfine = n;
@@ -1712,8 +1716,11 @@ static int learned_run(lgpu_handle *h) {
   if ((rc = learned_exact(h, os, nex, launches)) != LGPU_OK) return rc;
   CK(cudaEventRecord(L->ev[1], st), "event");
   // network inputs of the columns with four coarse neighbours
-  CK(lrn_obsfeat(st, nf, L->d_fine.as<int>(), h->buf[B_CP].as<ColPar>(), h->loc, os, h->buf[B_GEOM].as<IndexGeom>(),
-                 L->feat.as<float>(), L->nkf.as<int>(), &launches),
+  CK(L->cells.ensure(32 * ((size_t)h->ncell + 1)), "alloc");
+  float4 *c0 = L->cells.as<float4>(), *c1 = c0 + h->ncell;
+  CK(lrn_cellstats(st, h->ncell, os, c0, c1, &launches), "cell aggregates");
+  CK(lrn_obsfeat(st, nf, L->d_fine.as<int>(), h->buf[B_CP].as<ColPar>(), h->loc, os.cell_start, c0, c1,
+                 h->buf[B_GEOM].as<IndexGeom>(), L->feat.as<float>(), L->nkf.as<int>(), &launches),
      "learned features");
   LrnInterpArgs ia;
   ia.nfine = nf;

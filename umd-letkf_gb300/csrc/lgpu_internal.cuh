@@ -529,8 +529,10 @@ struct LrnApplyArgs {
   float *score;               // [nfine] or null
 };
 
+cudaError_t lrn_cellstats(cudaStream_t st, int ncell, const ObsSorted &obs, float4 *c0, float4 *c1, int *launches);
 cudaError_t lrn_obsfeat(cudaStream_t st, int nfine, const int *cols, const ColPar *cp, const DevLoc &loc,
-                        const ObsSorted &obs, const IndexGeom *geom, float *feat, int *nkept, int *launches);
+                        const int *cell_start, const float4 *c0, const float4 *c1, const IndexGeom *geom,
+                        float *feat, int *nkept, int *launches);
 cudaError_t lrn_interp(cudaStream_t st, const LrnInterpArgs &a, int *launches);
 cudaError_t lrn_apply(cudaStream_t st, const LrnApplyArgs &a, int *launches);
 cudaError_t lrn_judge(cudaStream_t st, int nj, const int *jcols, const int *jsub, const float *Tsub, const float *T,

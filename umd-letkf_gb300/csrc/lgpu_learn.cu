@@ -8,10 +8,11 @@
 // interpolation of the coarse solutions (W, w-bar) plus a correction from
 // the network of lgpu_mlp.cu.  The analysis update itself is unchanged.
 //
-//   k_lrn_obsfeat  per column: the observation-geometry features (local count,
-//                  sums of localisation weights, nearest distance, innovation
-//                  moments) from the same search and localizer as the exact
-//                  path
+//   k_lrn_cellstats, k_lrn_obsfeat  per column: the observation-geometry
+//                  features (local count, sums of localisation weights,
+//                  nearest distance, innovation moments) from per-cell
+//                  aggregates of the observation index and the same
+//                  localizer as the exact path
 //   k_lrn_interp   per column: the bilinear (W, w-bar) of the four coarse
 //                  neighbours, the network input row and, while collecting
 //                  training data, the residual target exact - interpolated
@@ -55,82 +56,82 @@ __device__ __forceinline__ float bmin128(float v, float *red) {
   return fminf(fminf(red[0], red[1]), fminf(red[2], red[3]));
 }
 
-// Observation-geometry features of column cols[f] (one CTA per column):
-//   0 kept count / 100        1 sum rho / 100         2 sum rho/err / 1000
-//   3 nearest kept distance / search radius (1 if none)
+// Per-cell aggregates of the cell-sorted observation table: centroid
+// direction (sum of unit vectors) and count; sums of dep, dep^2, 1/err,
+// dep/err.  One thread per cell.
+__global__ void k_lrn_cellstats(int ncell, ObsSorted obs, float4 *c0, float4 *c1) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = obs.cell_start[c], e = obs.cell_start[c + 1];
+  float sx = 0.f, sy = 0.f, sz = 0.f, sd = 0.f, sd2 = 0.f, si = 0.f, sdi = 0.f;
+  for (int p = b; p < e; p++) {
+    const float4 A = obs.A[p];
+    const float dep = obs.B[p].x, ie = 1.0f / A.w;
+    sx += A.x; sy += A.y; sz += A.z;
+    sd += dep; sd2 += dep * dep; si += ie; sdi += dep * ie;
+  }
+  c0[c] = make_float4(sx, sy, sz, (float)(e - b));
+  c1[c] = make_float4(sd, sd2, si, sdi);
+}
+
+// Observation-geometry features of column cols[f] from the cell aggregates
+// of its search window (one warp per column; a cell's observations are
+// taken at the cell's centroid):
+//   0 count within the search radius / 100   1 sum rho / 100
+//   2 sum rho/err / 1000   3 nearest centroid distance / search radius (1 if none)
 //   4 mean dep   5 variance of dep   6 rho-weighted mean dep
-//   7 (rho/err)-weighted mean dep    8 max rho   9 mean rho
+//   7 (rho/err)-weighted mean dep   8 max rho   9 mean rho
 // (features 10-15 are filled by k_lrn_interp)
 __global__ void __launch_bounds__(FT) k_lrn_obsfeat(int nfine, const int *cols, const ColPar *cps, DevLoc loc,
-                                                    ObsSorted obs, const IndexGeom *geom, float *feat, int *nkept) {
-  __shared__ float red[4];
-  const int f = blockIdx.x;
-  if (f >= nfine) return;
+                                                    const int *cell_start, const float4 *c0, const float4 *c1,
+                                                    const IndexGeom *geom, float *feat, int *nkept) {
+  const int lane = threadIdx.x & 31;
+  const int f = blockIdx.x * (FT / 32) + (threadIdx.x >> 5);
+  if (f >= nfine) return;   // whole warps
   const int col = cols[f];
   const ColPar cp = cps[col];
-  const float hq = fminf(cp.rmax / 12742000.0f, 1.5707963f);
-  const float sh = sinf(hq);
-  const float c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
   float n = 0.f, sr = 0.f, sre = 0.f, dmin = 3.0e38f, sd = 0.f, sd2 = 0.f, srd = 0.f, sred = 0.f, rmx = 0.f;
   for (int b = cp.b0; b <= cp.b1; b++) {
     const int nl = geom->nlon[b], off = geom->off[b];
-    int s0 = 0, l0 = 0, s1 = 0, l1 = 0;
-    bool whole = cp.dlon >= 180.0f;
-    int clo = 0, chi = nl - 1;
-    if (!whole) {
-      clo = (int)floorf((cp.lonn - cp.dlon) * (float)nl / 360.0f);
-      chi = (int)floorf((cp.lonn + cp.dlon) * (float)nl / 360.0f);
-      if (chi - clo + 1 >= nl) whole = true;
+    int lo = 0, cnt = nl;
+    if (cp.dlon < 180.0f) {
+      const int clo = (int)floorf((cp.lonn - cp.dlon) * (float)nl / 360.0f);
+      const int chi = (int)floorf((cp.lonn + cp.dlon) * (float)nl / 360.0f);
+      if (chi - clo + 1 < nl) { lo = clo; cnt = chi - clo + 1; }
     }
-    if (whole) {
-      s0 = obs.cell_start[off];
-      l0 = obs.cell_start[off + nl] - s0;
-    } else if (clo < 0) {
-      s0 = obs.cell_start[off + clo + nl];
-      l0 = obs.cell_start[off + nl] - s0;
-      s1 = obs.cell_start[off];
-      l1 = obs.cell_start[off + chi + 1] - s1;
-    } else if (chi >= nl) {
-      s0 = obs.cell_start[off + clo];
-      l0 = obs.cell_start[off + nl] - s0;
-      s1 = obs.cell_start[off];
-      l1 = obs.cell_start[off + (chi - nl) + 1] - s1;
-    } else {
-      s0 = obs.cell_start[off + clo];
-      l0 = obs.cell_start[off + chi + 1] - s0;
-    }
-    for (int j = threadIdx.x; j < l0 + l1; j += FT) {
-      const int p = j < l0 ? s0 + j : s1 + (j - l0);
-      const float4 A = obs.A[p];
-      const float c2 = chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
-      if (c2 > c2max) continue;
-      const float d = dist_from_chord2(c2);
+    for (int q = lane; q < cnt; q += 32) {
+      const int cell = off + (((lo + q) % nl) + nl) % nl;
+      const float4 A = c0[cell];
+      if (A.w <= 0.0f) continue;
+      const float inv = rsqrtf(A.x * A.x + A.y * A.y + A.z * A.z);
+      const float d = dist_from_chord2(chord2_exact(cp.ux, cp.uy, cp.uz, A.x * inv, A.y * inv, A.z * inv));
       if (d > cp.rmax) continue;
-      const float4 B = obs.B[p];
-      const float r = localize(loc, cp, 0, d, B.y, B.z, B.w);
+      const float r = localize(loc, cp, 0, d, 0.0f, 0.0f, 0.0f);
       if (!(r > kKeep)) continue;
-      const float re = r / A.w, dep = B.x;
-      n += 1.0f;
-      sr += r;
-      sre += re;
+      const float4 B = c1[cell];
+      n += A.w;
+      sr += r * A.w;
+      sre += r * B.z;
       dmin = fminf(dmin, d);
-      sd += dep;
-      sd2 += dep * dep;
-      srd += r * dep;
-      sred += re * dep;
+      sd += B.x;
+      sd2 += B.y;
+      srd += r * B.x;
+      sred += r * B.w;
       rmx = fmaxf(rmx, r);
     }
   }
-  n = bsum128(n, red);
-  sr = bsum128(sr, red);
-  sre = bsum128(sre, red);
-  sd = bsum128(sd, red);
-  sd2 = bsum128(sd2, red);
-  srd = bsum128(srd, red);
-  sred = bsum128(sred, red);
-  dmin = bmin128(dmin, red);
-  rmx = bmax128(rmx, red);
-  if (threadIdx.x == 0) {
+  for (int o = 16; o > 0; o >>= 1) {
+    n += __shfl_xor_sync(0xffffffffu, n, o);
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    sre += __shfl_xor_sync(0xffffffffu, sre, o);
+    sd += __shfl_xor_sync(0xffffffffu, sd, o);
+    sd2 += __shfl_xor_sync(0xffffffffu, sd2, o);
+    srd += __shfl_xor_sync(0xffffffffu, srd, o);
+    sred += __shfl_xor_sync(0xffffffffu, sred, o);
+    dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+    rmx = fmaxf(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
+  }
+  if (lane == 0) {
     float *o = feat + (size_t)f * 16;
     const float nn = fmaxf(n, 1.0f);
     const float m = sd / nn;
@@ -391,10 +392,19 @@ __global__ void k_lrn_batch(int b, const int *idx, const float *X, long long ldx
 // ---------------------------------------------------------------------------
 // launchers
 
+cudaError_t lrn_cellstats(cudaStream_t st, int ncell, const ObsSorted &obs, float4 *c0, float4 *c1, int *launches) {
+  if (ncell <= 0) return cudaSuccess;
+  k_lrn_cellstats<<<(ncell + 255) / 256, 256, 0, st>>>(ncell, obs, c0, c1);
+  (*launches)++;
+  return cudaGetLastError();
+}
+
 cudaError_t lrn_obsfeat(cudaStream_t st, int nfine, const int *cols, const ColPar *cp, const DevLoc &loc,
-                        const ObsSorted &obs, const IndexGeom *geom, float *feat, int *nkept, int *launches) {
+                        const int *cell_start, const float4 *c0, const float4 *c1, const IndexGeom *geom,
+                        float *feat, int *nkept, int *launches) {
   if (nfine <= 0) return cudaSuccess;
-  k_lrn_obsfeat<<<nfine, FT, 0, st>>>(nfine, cols, cp, loc, obs, geom, feat, nkept);
+  const int per = FT / 32;
+  k_lrn_obsfeat<<<(nfine + per - 1) / per, FT, 0, st>>>(nfine, cols, cp, loc, cell_start, c0, c1, geom, feat, nkept);
   (*launches)++;
   return cudaGetLastError();
 }

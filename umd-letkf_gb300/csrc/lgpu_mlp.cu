@@ -188,9 +188,21 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(MlpTcArgs a) {
         reinterpret_cast<uint4 *>(dst)[0] = reinterpret_cast<const uint4 *>(hb)[0];
         *reinterpret_cast<uint4 *>(dst + 128) = reinterpret_cast<const uint4 *>(hb)[1];
       } else if (row < a.rows) {
+        float *dst = a.out + (size_t)row * a.ldo + n;
+        const float *bn = a.bias + n;
+        if (n + 16 <= a.N && ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(bn)) & 15) == 0) {
+          // 16-byte stores of the row's 16 outputs
 #pragma unroll
-        for (int j = 0; j < 16; j++)
-          if (n + j < a.N) a.out[(size_t)row * a.ldo + n + j] = v[j] + a.bias[n + j];
+          for (int q = 0; q < 4; q++) {
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(bn) + q);
+            reinterpret_cast<float4 *>(dst)[q] =
+                make_float4(v[4 * q] + b.x, v[4 * q + 1] + b.y, v[4 * q + 2] + b.z, v[4 * q + 3] + b.w);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            if (n + j < a.N) dst[j] = v[j] + bn[j];
+        }
       }
     }
   }

@@ -13,6 +13,8 @@ sections a reference YAML configuration would carry for them.
   c5        learned form: 720x360x40, k=32, c3's clustered network (persistent
             clusters), loc_novrt 400 km, stride-4 coarse lattice, 5 exact
             training cycles
+  c5mid     c5 with 10 levels and 2 training cycles (profiling-sized: the same
+            network rows per analysis)
   c2mid     c2 observations on a 360x180x10 grid (profiling-sized: the same
             local observation counts per column, a fifth of the columns)
   simple3d  test/simple3d-style (k=50, three 3-D variables, two synthetic
@@ -58,9 +60,16 @@ WORKLOADS = {
                localization={"class": "loc_novrt",
                              "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 400.0e3}]}},
                solver={},
-               learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.05, sample_frac=0.3, train_cap=300000,
+               learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.1, sample_frac=0.6, train_cap=600000,
                           seed=5),
-               cycles=dict(train=5, u=0.5, kappa=1.0e3, dt=21600.0, epochs=12, batch=1024, lr=1e-3)),
+               cycles=dict(train=5, u=0.5, kappa=1.0e3, dt=21600.0, epochs=15, batch=1024, lr=1e-3)),
+    "c5mid": dict(gen=dict(workload="c3", k=32, nz=10),
+                  localization={"class": "loc_novrt",
+                                "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 400.0e3}]}},
+                  solver={},
+                  learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.05, sample_frac=0.3,
+                             train_cap=300000, seed=5),
+                  cycles=dict(train=2, u=0.5, kappa=1.0e3, dt=21600.0, epochs=2, batch=1024, lr=1e-3)),
     "c4small": dict(gen=dict(workload="c4", nx=180, ny=90, nz=5, n_obs=40000),
                     localization={"class": "loc_novrt",
                                   "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
