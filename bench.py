@@ -345,7 +345,7 @@ def gpu_arm(args, dist):
                   pin["hx_mean"].array)
         s.run()
 
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(6, args.warmup)):
         refill()
         e2e_step()
     dist.barrier()

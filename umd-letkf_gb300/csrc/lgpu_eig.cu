@@ -101,6 +101,7 @@ template <int NQ, int NW>
 __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> &T) {
   const int ld = k + 1, tt = T.tt, TS = T.TS;
   float *A = W.A, *d = W.d, *e = W.e, *tau = W.tau, *p = W.p, *w = W.w;
+  float *vv = W.fl;   // the current reflector, contiguous (fl is free until the transform)
   // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j];
   // its vector v_j = A[j+1:, j] stays in column j
   for (int j = 0; j < k - 2; j++) {
@@ -120,28 +121,28 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
     const float t = 2.0f / (v0 * v0 + s1);
     T.sync();
     if (tt == 0) { A[(j + 1) * ld + j] = v0; tau[j] = t; e[j] = alpha; d[j] = A[j * ld + j]; }
+    for (int r = tt; r < m; r += TS) vv[r] = r == 0 ? v0 : A[(j + 1 + r) * ld + j];
     T.sync();
     // p = t * A22 v
     for (int r = tt; r < m; r += TS) {
       const float *row = A + (j + 1 + r) * ld + (j + 1);
       float acc = 0.0f;
-      for (int c = 0; c < m; c++) acc = __fmaf_rn(row[c], A[(j + 1 + c) * ld + j], acc);
+#pragma unroll 4
+      for (int c = 0; c < m; c++) acc = __fmaf_rn(row[c], vv[c], acc);
       p[r] = t * acc;
     }
     T.sync();
     float pv = 0.0f;
-    for (int r = tt; r < m; r += TS) pv = __fmaf_rn(p[r], A[(j + 1 + r) * ld + j], pv);
+    for (int r = tt; r < m; r += TS) pv = __fmaf_rn(p[r], vv[r], pv);
     const float beta = 0.5f * t * T.sum(pv);
-    for (int r = tt; r < m; r += TS) w[r] = p[r] - beta * A[(j + 1 + r) * ld + j];
+    for (int r = tt; r < m; r += TS) w[r] = p[r] - beta * vv[r];
     T.sync();
     // A22 -= v w^T + w v^T
     for (int r = tt; r < m; r += TS) {
       float *row = A + (j + 1 + r) * ld + (j + 1);
-      const float vr = A[(j + 1 + r) * ld + j], wr = w[r];
-      for (int c = 0; c < m; c++) {
-        const float vc = A[(j + 1 + c) * ld + j], wc = w[c];
-        row[c] = row[c] - __fmaf_rn(vr, wc, wr * vc);
-      }
+      const float vr = vv[r], wr = w[r];
+#pragma unroll 4
+      for (int c = 0; c < m; c++) row[c] = row[c] - __fmaf_rn(vr, w[c], wr * vv[c]);
     }
     T.sync();
   }
@@ -173,6 +174,8 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
       const float t = tau[j];
       if (t == 0.0f) continue;
       const int m = k - j - 1;
+      for (int r = tt; r < m; r += TS) vv[r] = A[(j + 1 + r) * ld + j];
+      T.sync();
       // w_c = t * sum_r v_r Q[r][c]; Q[r][c] -= v_r w_c  (rows, columns j+1..k-1)
       float wc[NQ];
       bool in[NQ];
@@ -183,7 +186,7 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
         in[q] = c > j && c < k;
       }
       for (int r = 0; r < m; r++) {
-        const float v = A[(j + 1 + r) * ld + j];
+        const float v = vv[r];
 #pragma unroll
         for (int q = 0; q < NQ; q++)
           if (in[q]) wc[q] = __fmaf_rn(v, A[(j + 1 + r) * ld + tt + TS * q], wc[q]);
@@ -191,7 +194,7 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
 #pragma unroll
       for (int q = 0; q < NQ; q++) wc[q] *= t;
       for (int r = 0; r < m; r++) {
-        const float v = A[(j + 1 + r) * ld + j];
+        const float v = vv[r];
 #pragma unroll
         for (int q = 0; q < NQ; q++)
           if (in[q]) A[(j + 1 + r) * ld + tt + TS * q] -= v * wc[q];
