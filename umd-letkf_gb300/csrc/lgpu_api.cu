@@ -799,6 +799,78 @@ static UpdateArgs update_args(lgpu_handle *h) {
   return ua;
 }
 
+// The batched tensor-core Gram over a tile set (tiles of 128 columns; the
+// records and the weight cache are the handle's scratch): G, nkept and the
+// diagnostics of the tiles' units.  Events ev[6] after the tile streams.
+struct TileSet {
+  int ntiles;
+  DevBuf *cols, *par, *n, *off;
+};
+
+static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet &ts, int &launches) {
+  cudaStream_t st = h->st;
+  const int k = h->k, kp = h->kp, G = h->loc.groups;
+  CK(launch_tile_prep(st, ts.ntiles, (*ts.cols).as<int>(), h->buf[B_CP].as<ColPar>(),
+                      (*ts.par).as<TilePar>(), &launches), "tile prep");
+  // tile candidate streams: count, size the record buffer, fill
+  CK(launch_tile_count(st, ts.ntiles, (*ts.par).as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os,
+                       (*ts.n).as<int>(), (*ts.off).as<int>(), &launches),
+     "tile count");
+  int nchunk_total = 0;
+  CK(cudaMemcpyAsync(&nchunk_total, (*ts.off).as<int>() + ts.ntiles, sizeof(int), cudaMemcpyDeviceToHost, st),
+     "D2H stream size");
+  CK(cudaStreamSynchronize(st), "stream size sync");
+  CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
+  CK(launch_tile_fill(st, ts.ntiles, (*ts.par).as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
+                      (*ts.off).as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
+                      h->buf[B_STATUS].as<int>(), &launches),
+     "tile fill");
+  CK(cudaEventRecord(h->ev[6], st), "event");
+  TcArgs ta;
+  ta.ntiles = ts.ntiles;
+  ta.groups = G;
+  ta.k = k;
+  ta.kp = kp;
+  gram_tc_passes(k, &ta.npass, &ta.np);
+  h->mma_n = ta.np;
+  ta.nf = packed_size(k);
+  ta.ncol = h->ncol;
+  ta.tile_cols = (*ts.cols).as<int>();
+  ta.col2act = h->buf[B_COL2ACT].as<int>();
+  ta.cp = h->buf[B_CP].as<ColPar>();
+  ta.loc = h->loc;
+  ta.tp = (*ts.par).as<TilePar>();
+  ta.rec = h->buf[B_TILEREC].as<unsigned char>();
+  ta.tile_off = (*ts.off).as<int>();
+  ta.tile_n = (*ts.n).as<int>();
+  ta.G = h->buf[B_G].as<float>();
+  ta.nkept = h->buf[B_NKEPT].as<int>();
+  ta.diag_obscount = h->buf[B_DOBSC].as<float>();
+  ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
+  ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
+  ta.status = h->buf[B_STATUS].as<int>();
+  // weight cache for multi-pass tiles (at most 48 GB; without it every pass
+  // recomputes the weights)
+  ta.wcache = nullptr;
+  ta.nchunk_total = nchunk_total;
+  ta.wflag = nullptr;
+  if (ta.npass >= 2) {
+    const size_t wb = gram_tc_wcache_bytes(G, nchunk_total);
+    if (wb <= ((size_t)48 << 30)) {
+      if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess) {
+        ta.wcache = h->buf[B_WCACHE].as<float>();
+        ta.wflag = reinterpret_cast<int *>(h->buf[B_WCACHE].as<unsigned char>() +
+                                           (wb - (size_t)G * nchunk_total * sizeof(int)));
+      } else {
+        cudaGetLastError();   // clear the failed allocation
+      }
+    }
+  }
+  CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+  
+    return LGPU_OK;
+}
+
 // letkf_solver_run (src/letkf_solver.F90:150-389)
 int lgpu_solver_run(lgpu_handle *h) {
   if (!h) return LGPU_ERR_ARG;
@@ -812,67 +884,8 @@ int lgpu_solver_run(lgpu_handle *h) {
   const bool bound = h->bound_state != nullptr;
   // ---- search + localize + Gram ----
   // ---- Gram: the batched tensor-core form or the plain per-column form ----
-  auto run_batched = [&]() -> int {
-      CK(launch_tile_prep(st, h->ntiles, h->buf[B_TILECOLS].as<int>(), h->buf[B_CP].as<ColPar>(),
-                          h->buf[B_TILEPAR].as<TilePar>(), &launches), "tile prep");
-      // tile candidate streams: count, size the record buffer, fill
-      CK(launch_tile_count(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os,
-                           h->buf[B_TILEN].as<int>(), h->buf[B_TILEOFF].as<int>(), &launches),
-         "tile count");
-      int nchunk_total = 0;
-      CK(cudaMemcpyAsync(&nchunk_total, h->buf[B_TILEOFF].as<int>() + h->ntiles, sizeof(int), cudaMemcpyDeviceToHost, st),
-         "D2H stream size");
-      CK(cudaStreamSynchronize(st), "stream size sync");
-      CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
-      CK(launch_tile_fill(st, h->ntiles, h->buf[B_TILEPAR].as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
-                          h->buf[B_TILEOFF].as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
-                          h->buf[B_STATUS].as<int>(), &launches),
-         "tile fill");
-      CK(cudaEventRecord(h->ev[6], st), "event");
-      TcArgs ta;
-      ta.ntiles = h->ntiles;
-      ta.groups = G;
-      ta.k = k;
-      ta.kp = kp;
-      gram_tc_passes(k, &ta.npass, &ta.np);
-      h->mma_n = ta.np;
-      ta.nf = packed_size(k);
-      ta.ncol = h->ncol;
-      ta.tile_cols = h->buf[B_TILECOLS].as<int>();
-      ta.col2act = h->buf[B_COL2ACT].as<int>();
-      ta.cp = h->buf[B_CP].as<ColPar>();
-      ta.loc = h->loc;
-      ta.tp = h->buf[B_TILEPAR].as<TilePar>();
-      ta.rec = h->buf[B_TILEREC].as<unsigned char>();
-      ta.tile_off = h->buf[B_TILEOFF].as<int>();
-      ta.tile_n = h->buf[B_TILEN].as<int>();
-      ta.G = h->buf[B_G].as<float>();
-      ta.nkept = h->buf[B_NKEPT].as<int>();
-      ta.diag_obscount = h->buf[B_DOBSC].as<float>();
-      ta.diag_lg_obscount = h->buf[B_DLGC].as<float>();
-      ta.diag_lg_obsloc = h->buf[B_DLGL].as<float>();
-      ta.status = h->buf[B_STATUS].as<int>();
-      // weight cache for multi-pass tiles (at most 48 GB; without it every pass
-      // recomputes the weights)
-      ta.wcache = nullptr;
-      ta.nchunk_total = nchunk_total;
-      ta.wflag = nullptr;
-      if (ta.npass >= 2) {
-        const size_t wb = gram_tc_wcache_bytes(G, nchunk_total);
-        if (wb <= ((size_t)48 << 30)) {
-          if (h->buf[B_WCACHE].cap >= wb || h->buf[B_WCACHE].ensure(std::max<size_t>(wb, 256)) == cudaSuccess) {
-            ta.wcache = h->buf[B_WCACHE].as<float>();
-            ta.wflag = reinterpret_cast<int *>(h->buf[B_WCACHE].as<unsigned char>() +
-                                               (wb - (size_t)G * nchunk_total * sizeof(int)));
-          } else {
-            cudaGetLastError();   // clear the failed allocation
-          }
-        }
-      }
-      CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
-  
-    return LGPU_OK;
-  };
+  const TileSet grid_tiles{h->ntiles, &h->buf[B_TILECOLS], &h->buf[B_TILEPAR], &h->buf[B_TILEN], &h->buf[B_TILEOFF]};
+  auto run_batched = [&]() -> int { return run_batched_tiles(h, os, grid_tiles, launches); };
   auto run_plain = [&]() -> int {
     GramArgs ga;
     ga.nunits = h->nunits;
@@ -925,6 +938,7 @@ int lgpu_solver_run(lgpu_handle *h) {
   // update of the following chunks run.
   EigArgs ea;
   ea.wbar = h->learn_wbar;   // mean weights of every unit while training data is collected
+  ea.ulist = nullptr;
   ea.nunits = h->nunits;
   ea.k = k;
   ea.infl = 1.0f;   // letkf_core_solve is called with infl = 1.0 (src/letkf_solver.F90:279)
@@ -1677,6 +1691,7 @@ static int learned_exact(lgpu_handle *h, const ObsSorted &os, int n, int &launch
   ea.nkept = L->nksub.as<int>();
   ea.T = L->Tsub.as<float>();
   ea.wbar = L->wsub.as<float>();
+  ea.ulist = nullptr;
   ea.status = h->buf[B_STATUS].as<int>();
   EigSplit sp;
   int batch = 0;

@@ -386,8 +386,9 @@ __global__ void k_eig(EigArgs a, int wpb) {
   extern __shared__ __align__(16) float sm[];
   const int k = a.k;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int unit = blockIdx.x * wpb + warp;
-  if (unit >= a.nunits) return;           // whole warps exit; no block-level barriers below
+  const int un = blockIdx.x * wpb + warp;
+  if (un >= a.nunits) return;             // whole warps exit; no block-level barriers below
+  const int unit = a.ulist ? a.ulist[un] : un;
   if (a.nkept[unit] <= 0) return;         // no local observations: the update keeps the background
   EigWork W(sm + (size_t)warp * eig_floats_per_warp(k), k);
   const Team<1> T{lane, lane, warp, nullptr};
@@ -421,7 +422,7 @@ __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   const int slot = NW == 1 ? warp : 0;
   const int ub = blockIdx.x * wpb + slot;
   if (ub >= nb) return;
-  const int unit = u0 + ub;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
   if (a.nkept[unit] <= 0) return;
   EigWork W(sm + (size_t)slot * eig_floats_per_warp(k), k);
   const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
@@ -444,7 +445,7 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
 #define D(i) d[(size_t)(i) * QLT]
 #define E(i) e[(size_t)(i) * QLT]
   if (ub >= nb) return;
-  const int unit = u0 + ub;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
   if (a.nkept[unit] <= 0) return;
   const float *de = sp.DE + (size_t)ub * 2 * k;
   for (int i = 0; i < k; i++) { D(i) = de[i]; E(i) = de[k + i]; }
@@ -514,7 +515,7 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   const int slot = NW == 1 ? warp : 0;
   const int ub = blockIdx.x * wpb + slot;
   if (ub >= nb) return;
-  const int unit = u0 + ub;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
   if (a.nkept[unit] <= 0) return;
   const int total = sp.logn[ub];
   if (total == -1) return;                // no convergence: status set by k_eig_ql
@@ -665,6 +666,7 @@ cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G,
                              int *status) {
   EigArgs a;
   a.wbar = nullptr;
+  a.ulist = nullptr;
   a.nunits = nunits;
   a.k = k;
   a.infl = 1.0f;

@@ -429,6 +429,7 @@ struct EigArgs {
   const int *nkept;
   float *T;               // [unit][k][k]
   float *wbar;            // [unit][k] mean weights, or null
+  const int *ulist;       // units to solve (the i-th is ulist[i]), or null: units 0..nunits-1
   int *status;            // [1] accumulated error bits
 };
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
