@@ -298,8 +298,9 @@ int lgpu_learn_init(lgpu_handle *h, const lgpu_learn_config *cfg);
 int lgpu_learn_collect(lgpu_handle *h, long long *rows);
 /* Standardises the stored rows (first call), runs `epochs` passes of Adam
  * with mini-batches of `batch` rows, then calibrates the gate threshold.
- * *loss receives the mean training loss of the last epoch (standardised
- * units). */
+ * Once two or more analyses were collected, the rows of the last one are
+ * held out of training and calibrate the gate.  *loss receives the mean
+ * training loss of the last epoch (standardised units). */
 int lgpu_learn_train(lgpu_handle *h, int epochs, int batch, float lr, float *loss);
 int lgpu_learn_stats_get(lgpu_handle *h, lgpu_learn_stats *out);
 /* use_network = 0: the LEARNED variant applies the bare interpolation (no

@@ -1286,6 +1286,8 @@ struct LearnState {
   DevBuf wout;                                   // per-output loss weights: 1 for W, k for w-bar
   DevBuf cells;                                  // per-cell observation aggregates (two float4 per cell)
   long long nstore = 0;
+  long long hold0 = 0;     // first row of the last collected analysis (held out from training when ncollect >= 2)
+  int ncollect = 0;
   bool stats_ok = false, trained = false;
   unsigned long long runs = 0;
   int adam_step = 0;
@@ -1545,6 +1547,8 @@ int lgpu_learn_collect(lgpu_handle *h, long long *rows) {
     ia.ldy = S.dout;
     CK(lrn_interp(st, ia, &launches), "learned interpolation");
     CK(cudaStreamSynchronize(st), "collect");
+    L->hold0 = L->nstore;
+    L->ncollect++;
     L->nstore += n;
   }
   if (rows) *rows = L->nstore;
@@ -1564,7 +1568,11 @@ int lgpu_learn_train(lgpu_handle *h, int epochs, int batch, float lr, float *los
   CK(cudaSetDevice(h->device), "cudaSetDevice");
   cudaStream_t st = h->st;
   const MlpShape &S = L->shape;
-  const long long n = L->nstore;
+  // the rows of the last collected analysis are held out (for the gate's
+  // calibration) once two or more analyses were collected
+  const bool holdout = L->ncollect >= 2 && L->hold0 > 0 && L->hold0 < L->nstore;
+  const long long n = holdout ? L->hold0 : L->nstore;
+  const long long cal0 = holdout ? L->hold0 : 0, cal1 = L->nstore;
   batch = (int)std::min<long long>(batch, n);
   if (!L->stats_ok) {
     CK(lrn_colstats(st, L->store_X.as<float>(), n, S.din, S.din, L->mu_in.as<float>(), L->sd_in.as<float>()),
@@ -1613,11 +1621,12 @@ int lgpu_learn_train(lgpu_handle *h, int epochs, int batch, float lr, float *los
   if (loss) *loss = last;
   CK(mlp_tile_weights(st, S, L->Pq.as<float>(), L->Wt.as<unsigned char>()), "tile weights");
   // gate threshold: the (1 - gate_frac) quantile of the RMS network output
-  // over (up to) 16,384 stored rows, through the tensor-core forward
-  const int ncal = (int)std::min<long long>(n, 16384);
+  // over (up to) 16,384 held-out rows (training rows when none are held
+  // out), through the tensor-core forward
+  const int ncal = (int)std::min<long long>(cal1 - cal0, 16384);
   {
     std::vector<int> idx(ncal);
-    for (int i = 0; i < ncal; i++) idx[i] = (int)((long long)i * n / ncal);
+    for (int i = 0; i < ncal; i++) idx[i] = (int)(cal0 + (long long)i * (cal1 - cal0) / ncal);
     CK(L->bidx.ensure(4 * (size_t)std::max<long long>(n, ncal)), "alloc");
     CK(cudaMemcpyAsync(L->bidx.p, idx.data(), 4 * (size_t)ncal, cudaMemcpyHostToDevice, st), "H2D");
     CK(L->X.ensure(4 * (size_t)ncal * S.din), "alloc");
