@@ -60,7 +60,7 @@ enum {
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
   B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC, B_EIGSCR, B_WCACHE,
   B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7, B_RAWQC, B_RAWHX, B_RAWHXM, B_FLAG, B_POS,
-  B_PTRS, B_TOTAL,
+  B_PTRS, B_TOTAL, B_GPART, B_GCNT,
   B_COUNT_ALL
 };
 
@@ -99,6 +99,7 @@ struct lgpu_handle {
   bool used_tc = false;
   int mma_n = 0;
   int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
+  int gram_nseg = 1;     // accumulation segments of the last batched Gram
   DevBuf buf[B_COUNT_ALL];
   lgpu_timings tim{};
   LearnState *learn = nullptr;      // learned form, after lgpu_learn_init
@@ -866,7 +867,35 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
       }
     }
   }
+  // accumulation segments: long tile streams are split into up to 4 ranges
+  // accumulated by separate CTAs (the tensor core's FP32 accumulation error
+  // grows with the stream length), partial Grams summed in order afterwards;
+  // the partials take at most 24 GB
+  ta.units = (long long)h->nact * G;
+  ta.nseg = 1;
+  ta.Gpart = nullptr;
+  ta.cnt = nullptr;
+  {
+    const double avg = (double)nchunk_total / std::max(1, ts.ntiles);
+    int nseg = avg >= 512.0 ? 4 : (avg >= 256.0 ? 2 : 1);
+    const double per = (double)ta.units * ta.nf * 4.0;
+    while (nseg > 1 && (nseg - 1) * per > 24.0 * (1ull << 30)) nseg--;
+    if (nseg > 1) {
+      const size_t gp = (size_t)(nseg - 1) * (size_t)ta.units * ta.nf * 4;
+      const size_t cn = (size_t)nseg * (size_t)ta.units * 3 * 4;
+      if ((h->buf[B_GPART].cap >= gp || h->buf[B_GPART].ensure(gp) == cudaSuccess) &&
+          (h->buf[B_GCNT].cap >= cn || h->buf[B_GCNT].ensure(cn) == cudaSuccess)) {
+        ta.nseg = nseg;
+        ta.Gpart = h->buf[B_GPART].as<float>();
+        ta.cnt = h->buf[B_GCNT].as<float>();
+      } else {
+        cudaGetLastError();   // clear the failed allocation: one segment
+      }
+    }
+  }
+  h->gram_nseg = ta.nseg;
   CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+  CK(launch_gram_segsum(st, ta, h->buf[B_ACTIVE].as<int>(), &launches), "gram segment sum");
   
     return LGPU_OK;
 }

@@ -339,20 +339,26 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(16) TcSmem S;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int pass = a.pass0 + blockIdx.x % a.npl;
-  const int g = (blockIdx.x / a.npl) % a.groups;
-  const int tile = blockIdx.x / (a.npl * a.groups);
+  const int seg = blockIdx.x % a.nseg;
+  const int rest = blockIdx.x / a.nseg;
+  const int pass = a.pass0 + rest % a.npl;
+  const int g = (rest / a.npl) % a.groups;
+  const int tile = rest / (a.npl * a.groups);
   const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
   const int slotb = cb;   // ring slot: one chunk record
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
   const uint32_t stage_bytes = 2 * WB + 2 * PB;
   auto stage_ptr = [&](int s) { return dsm + (size_t)s * stage_bytes; };
   unsigned char *ring = dsm + (size_t)NS * stage_bytes;
-  const int c0 = a.tile_off[tile];
+  // this CTA's segment of the tile's chunk stream
+  const int t0 = a.tile_off[tile], tn = a.tile_off[tile + 1] - t0;
+  const int seglen = (tn + a.nseg - 1) / a.nseg;
+  const int cs = min(tn, seg * seglen), ce = min(tn, cs + seglen);
+  const int c0 = t0 + cs;
   float *wcache = WMODE != 0 ? a.wcache + (size_t)g * a.nchunk_total * (WCB / 4) : nullptr;
   int *wflag = WMODE != 0 ? a.wflag + (size_t)g * a.nchunk_total : nullptr;
-  const int nchunks = a.tile_off[tile + 1] - c0;
-  const int ntile = a.tile_n[tile];
+  const int nchunks = ce - cs;
+  const int ntile = a.tile_n[tile] - cs * KC;   // candidates from the segment's first chunk on
   const uint32_t tmem_cols = a.tmem_cols;
 
   // ---- setup: TMEM, barriers, feature table
@@ -606,12 +612,20 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     size_t unit = 0;
     if (colv) unit = (size_t)a.col2act[col] * G + g;
     if (colv && pass == 0) {
-      a.nkept[unit] = nkeep;
-      if (a.diag_lg_obscount) a.diag_lg_obscount[(size_t)g * a.ncol + col] = (float)nkeep;
-      if (a.diag_lg_obsloc) a.diag_lg_obsloc[(size_t)g * a.ncol + col] = rsum;
-      if (g == 0 && a.diag_obscount) a.diag_obscount[col] = (float)ncand;
+      if (a.nseg == 1) {
+        a.nkept[unit] = nkeep;
+        if (a.diag_lg_obscount) a.diag_lg_obscount[(size_t)g * a.ncol + col] = (float)nkeep;
+        if (a.diag_lg_obsloc) a.diag_lg_obsloc[(size_t)g * a.ncol + col] = rsum;
+        if (g == 0 && a.diag_obscount) a.diag_obscount[col] = (float)ncand;
+      } else {
+        float *cc = a.cnt + ((size_t)seg * a.units + unit) * 3;
+        cc[0] = (float)nkeep;
+        cc[1] = (float)ncand;
+        cc[2] = rsum;
+      }
     }
-    float *Gp = a.G + unit * (size_t)nf + (size_t)pass * NP;
+    float *Gbase = seg == 0 ? a.G : a.Gpart + (size_t)(seg - 1) * (size_t)a.units * nf;
+    float *Gp = Gbase + unit * (size_t)nf + (size_t)pass * NP;
     const int nvalid = nf - pass * NP < NP ? nf - pass * NP : NP;
     for (int f0 = 0; f0 < NP; f0 += 16) {
       float v[16];
@@ -768,7 +782,7 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
   int ns, nr;
   size_t smem;
   gram_tc_config(a.k, a.np, &ns, &nr, &smem);
-  const long long per_pass = (long long)a.ntiles * a.groups;
+  const long long per_pass = (long long)a.ntiles * a.groups * a.nseg;
   if (per_pass * a.npass > 0x7fffffffLL) return cudaErrorInvalidValue;
   cudaError_t e;
   if (a.npass >= 2 && a.wcache) {
@@ -804,6 +818,46 @@ cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
   case LOC_VTGC: return launch_gram_tc_loc<LOC_VTGC>(st, a, launches);
   default: return launch_gram_tc_loc<LOC_NOVRT>(st, a, launches);
   }
+}
+
+namespace {
+// G += partial Grams of segments 1..nseg-1, in segment order; counts summed
+// in segment order (the sums of rho in FP32, as a single CTA would)
+__global__ void k_gram_segsum(long long units, int nf, int nseg, int groups, int ncol, const int *active, float *G,
+                              const float *Gpart, const float *cnt, int *nkept, float *diag_obscount,
+                              float *diag_lg_obscount, float *diag_lg_obsloc) {
+  const long long total = units * nf;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    float v = G[t];
+    for (int s = 1; s < nseg; s++) v += Gpart[(size_t)(s - 1) * total + t];
+    G[t] = v;
+    if (t % nf == 0) {
+      const long long u = t / nf;
+      float kept = 0.0f, cand = 0.0f, rs = 0.0f;
+      for (int s = 0; s < nseg; s++) {
+        const float *cc = cnt + ((size_t)s * units + u) * 3;
+        kept += cc[0];
+        cand += cc[1];
+        rs += cc[2];
+      }
+      const int act = (int)(u / groups), g = (int)(u % groups), col = active[act];
+      nkept[u] = (int)kept;
+      if (diag_lg_obscount) diag_lg_obscount[(size_t)g * ncol + col] = kept;
+      if (diag_lg_obsloc) diag_lg_obsloc[(size_t)g * ncol + col] = rs;
+      if (g == 0 && diag_obscount) diag_obscount[col] = cand;
+    }
+  }
+}
+}  // namespace
+
+cudaError_t launch_gram_segsum(cudaStream_t st, const TcArgs &a, const int *active, int *launches) {
+  if (a.nseg <= 1 || a.units <= 0) return cudaSuccess;
+  const long long total = a.units * a.nf;
+  const int grid = (int)std::min<long long>(152 * 16, (total + 255) / 256);
+  k_gram_segsum<<<grid, 256, 0, st>>>(a.units, a.nf, a.nseg, a.groups, a.ncol, active, a.G, a.Gpart, a.cnt, a.nkept,
+                                       a.diag_obscount, a.diag_lg_obscount, a.diag_lg_obsloc);
+  (*launches)++;
+  return cudaGetLastError();
 }
 
 size_t gram_tc_wcache_bytes(int groups, int nchunk_total) {

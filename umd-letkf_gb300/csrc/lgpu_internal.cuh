@@ -403,11 +403,23 @@ struct TcArgs {
   int *wflag;                // [groups][chunks]: the chunk has a kept pair (MMA issued)
   int nchunk_total;          // chunks over all tiles (weight cache indexing)
   int pass0, npl;            // feature passes of one launch: [pass0, pass0 + npl) (set by the launcher)
+  // accumulation segments: each tile's chunk stream is split into nseg
+  // consecutive ranges, each accumulated by its own CTA; segment 0 writes G,
+  // segment s > 0 its partial Gram at Gpart + (s - 1) * units * nf and its
+  // counts at cnt + s * units * 3 (segment 0 too when nseg > 1), summed in
+  // segment order by launch_gram_segsum
+  int nseg;
+  long long units;
+  float *Gpart;
+  float *cnt;                // [nseg][units][3]: kept, candidates, sum rho (when nseg > 1)
   float *G;
   int *nkept;
   float *diag_obscount, *diag_lg_obscount, *diag_lg_obsloc;
   int *status;
 };
+// G += the partial Grams of segments 1..nseg-1; kept counts and diagnostics
+// from the per-segment counts
+cudaError_t launch_gram_segsum(cudaStream_t st, const TcArgs &a, const int *active, int *launches);
 cudaError_t launch_tile_prep(cudaStream_t st, int ntiles, const int *tile_cols, const ColPar *cp, TilePar *tp,
                              int *launches);
 // tile candidate streams: counts + chunk offsets (tile_off[ntiles] = total
