@@ -282,7 +282,7 @@ def gpu_arm(args, dist):
     times = {"gram": gram_kernel_ms, "eig": stage["eig_ms"], "update": stage["update_ms"]}
     dom = max(times, key=times.get)
     kname = {"gram": "k_gram_tc" if tims[-1]["variant"] == 2 else "k_gram", "eig": "k_eig", "update": "k_update"}[dom]
-    traffic = read_traffic(kname)
+    traffic = read_traffic(kname) if args.workload == "c2" else None   # the committed captures are of C2
     if dom == "update":
         ach = upd_bytes / (stage["update_ms"] * 1e-3) / 1e9
         roof = {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
