@@ -143,6 +143,9 @@ typedef struct lgpu_timings {
   long long mma_chunks;  /* BATCHED_TC: (tile, group, pass, 16-observation chunk) steps that ran MMAs */
   int mma_n;         /* BATCHED_TC: features per pass (MMA N); executed TF32 flops =
                         mma_chunks * 3 products * 2 * 128 * mma_n * 16 */
+  int precision;     /* eigensolve precision mode of the run (LGPU_PREC_*) */
+  int fp64_units;    /* units whose eigensolve ran in FP64 (re-solved, or all under LGPU_PREC_FP64) */
+  float fp64_ms;     /* part of eig_ms spent in the FP64 eigensolve */
 } lgpu_timings;
 
 /* Gram variants.  PLAIN: one CTA per (column, group), FP32 on the CUDA
@@ -173,6 +176,25 @@ int lgpu_solver_init(lgpu_handle *h, const lgpu_solver_config *cfg);
 int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *cfg);
 int lgpu_loc_maxgroups(const lgpu_handle *h);
 int lgpu_set_variant(lgpu_handle *h, int variant);   /* no reference counterpart: selects the Gram kernel */
+
+/* Precision of the eigensolve and transform (src/letkf_core.F90:100-141,
+ * FP32 ssyev in the reference); no reference counterpart.  The Gram stays
+ * FP32 in every mode.
+ * FP32 (default): FP32 throughout, the reference's precision.
+ * FP32_RESOLVE: FP32, and a unit is solved again in FP64 when its FP32
+ *   solve failed (no convergence, a non-positive or non-finite eigenvalue)
+ *   or when two of its relevant eigenvalues lie within gap_threshold *
+ *   lambda_max of each other.  Relevant eigenvalues are those above the
+ *   (k-1) floor of Yb^T R^-1 Yb + (k-1) I by more than the FP32 rounding
+ *   level (4 k eps lambda_max): the floor is exactly degenerate whenever the
+ *   unit has fewer observations than members and does not make T
+ *   ill-conditioned.  gap_threshold <= 0 takes 1e-6.
+ * FP64: every unit's eigensolve and transform in FP64 (results stored FP32).
+ * Under LGPU_VARIANT_LEARNED the mode applies to the exact solves. */
+#define LGPU_PREC_FP32 0
+#define LGPU_PREC_FP32_RESOLVE 1
+#define LGPU_PREC_FP64 2
+int lgpu_set_precision(lgpu_handle *h, int mode, float gap_threshold);
 
 int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, const int *mask);
 int lgpu_set_state(lgpu_handle *h, int k, int ns, const float *state, const float *mean,
@@ -351,7 +373,9 @@ int lgpu_debug_weight(lgpu_handle *h, int n, const float *lat1, const float *lon
 /* Verification of the eigensolve stage alone (src/letkf_core.F90:100-141
  * with infl = 1): gram holds nunits packed blocks (upper triangle of
  * Yb^T R^-1 rho Yb row-major, then the right-hand side b; k(k+3)/2 floats);
- * trans receives T = W + wbar 1^T, [unit][i][j] row-major. */
+ * trans receives T = W + wbar 1^T, [unit][i][j] row-major.  The precision
+ * mode of lgpu_set_precision applies; lgpu_get_timings then reports the
+ * FP64-solved unit count in fp64_units (the other fields are not set). */
 int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, float *trans);
 
 #ifdef __cplusplus

@@ -6,9 +6,10 @@ from letkf_gb300 import Solver, normalize_loc, normalize_solver
 from letkf_gb300.workloads import WORKLOADS
 
 
-def gpu_run(prob, localization, solver=None, variables=None, keep_open=False, variant="auto"):
+def gpu_run(prob, localization, solver=None, variables=None, keep_open=False, variant="auto", precision="fp32"):
     s = Solver(0)
     s.set_variant(variant)
+    s.set_precision(precision)
     s.solver_init(solver)
     s.loc_init(localization, variables if variables is not None else prob.vars, prob.lev_depth)
     s.set_problem(prob, variables)

@@ -27,7 +27,7 @@ cudaError_t launch_compact(cudaStream_t st, int nobs, int k, const int *flag, co
                            const float *hx, float *hx_out, const float *hxm, float *hxm_out);
 cudaError_t launch_state_stats(cudaStream_t st, long long ncs, int k, float *x, float *mean, float *sprd);
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
-                             int *status);
+                             int *status, int prec, float gap_thresh, int *nfp64);
 }
 
 namespace {
@@ -60,7 +60,7 @@ enum {
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
   B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC, B_EIGSCR, B_WCACHE,
   B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7, B_RAWQC, B_RAWHX, B_RAWHXM, B_FLAG, B_POS,
-  B_PTRS, B_TOTAL, B_GPART, B_GCNT,
+  B_PTRS, B_TOTAL, B_GPART, B_GCNT, B_FLAGLIST,
   B_COUNT_ALL
 };
 
@@ -77,7 +77,8 @@ struct lgpu_handle {
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev_in[2] = {};       // bound state: mean/spread, members uploaded
   cudaEvent_t ev_tune[3] = {};     // AUTO: timing of the two Gram forms
-  cudaEvent_t ev_chunk[kOutChunks][3] = {};   // per column chunk: eigensolve start, update start, update end
+  // per column chunk: eigensolve start, update start, update end, FP64 eigensolve start
+  cudaEvent_t ev_chunk[kOutChunks][4] = {};
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
   std::string err;
   bool solver_ok = false, loc_ok = false, grid_ok = false, state_ok = false, obs_ok = false, ran = false;
@@ -100,6 +101,8 @@ struct lgpu_handle {
   int mma_n = 0;
   int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
   int gram_nseg = 1;     // accumulation segments of the last batched Gram
+  int prec = LGPU_PREC_FP32;   // eigensolve precision mode
+  float gap_thresh = 1e-6f;    // FP32_RESOLVE: relative eigenvalue gap that sends a unit to FP64
   DevBuf buf[B_COUNT_ALL];
   lgpu_timings tim{};
   LearnState *learn = nullptr;      // learned form, after lgpu_learn_init
@@ -347,6 +350,16 @@ int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *c) {
 }
 
 int lgpu_loc_maxgroups(const lgpu_handle *h) { return (h && h->loc_ok) ? h->loc.groups : -1; }
+
+int lgpu_set_precision(lgpu_handle *h, int mode, float gap_threshold) {
+  if (!h) return LGPU_ERR_ARG;
+  if (mode < LGPU_PREC_FP32 || mode > LGPU_PREC_FP64)
+    return fail(h, LGPU_ERR_ARG, "unknown precision mode " + std::to_string(mode));
+  if (!(gap_threshold < 1.0f)) return fail(h, LGPU_ERR_ARG, "gap_threshold must be below 1");
+  h->prec = mode;
+  h->gap_thresh = gap_threshold > 0.0f ? gap_threshold : 1e-6f;
+  return LGPU_OK;
+}
 
 int lgpu_set_variant(lgpu_handle *h, int variant) {
   if (!h) return LGPU_ERR_ARG;
@@ -742,6 +755,27 @@ static int learned_run(lgpu_handle *h);
 static int eig_scratch(lgpu_handle *h, int units, EigSplit &sp, int &batch);
 static UpdateArgs update_args(lgpu_handle *h);
 
+// FP32_RESOLVE: the run's list of units for the FP64 re-solve, counters
+// reset; room for every unit of the run twice (an exact run flags a unit at
+// most once; the learned form may solve a column in two exact passes)
+static int flag_prepare(lgpu_handle *h) {
+  if (h->prec != LGPU_PREC_FP32_RESOLVE) return LGPU_OK;
+  CK(h->buf[B_FLAGLIST].ensure(16 + 8 * (size_t)std::max(1, h->nunits)), "alloc");
+  CK(cudaMemsetAsync(h->buf[B_FLAGLIST].p, 0, 16, h->st), "memset");
+  return LGPU_OK;
+}
+
+static void flag_args(lgpu_handle *h, EigArgs &ea) {
+  ea.gap_thresh = h->gap_thresh;
+  ea.flag_list = nullptr;
+  ea.flag_n = nullptr;
+  ea.flag_cap = 0;
+  if (h->prec != LGPU_PREC_FP32_RESOLVE) return;
+  ea.flag_n = h->buf[B_FLAGLIST].as<int>();
+  ea.flag_list = ea.flag_n + 4;
+  ea.flag_cap = 2 * std::max(1, h->nunits);
+}
+
 // eigensolve scratch of the split pipeline for `units` units (at most 8 GB,
 // units in batches); batch = 0 when it cannot be had (the fused kernel runs)
 static int eig_scratch(lgpu_handle *h, int units, EigSplit &sp, int &batch) {
@@ -976,19 +1010,22 @@ int lgpu_solver_run(lgpu_handle *h) {
   ea.T = h->buf[B_T].as<float>();
   ea.status = h->buf[B_STATUS].as<int>();
   UpdateArgs ua = update_args(h);
+  if ((rc = flag_prepare(h)) != LGPU_OK) return rc;
+  flag_args(h, ea);
+  const bool fp64 = h->prec == LGPU_PREC_FP64;
   // eigensolve scratch: the split pipeline (at most 8 GB, units in batches);
   // the fused one-warp kernel over all units if the scratch cannot be had
+  // (no FP64 re-solve then)
   EigSplit sp;
   int batch = 0;
-  {
-    const int rc = eig_scratch(h, h->nunits, sp, batch);
-    if (rc != LGPU_OK) return rc;
+  if (!fp64) {
+    if ((rc = eig_scratch(h, h->nunits, sp, batch)) != LGPU_OK) return rc;
+    if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
   }
-  if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
   if (bound) CK(cudaStreamWaitEvent(st, h->ev_in[1], 0), "stream wait");
   const int nch = bound ? kOutChunks : 1;
   const int per = (h->ncol + nch - 1) / nch;
-  float eig_ms = 0.0f, upd_ms = 0.0f;
+  float eig_ms = 0.0f, upd_ms = 0.0f, fp64_ms = 0.0f;
   int nrec = 0;
   for (int c = 0; c < nch; c++) {
     const int c0 = c * per, c1 = std::min(h->ncol, (c + 1) * per);
@@ -998,7 +1035,16 @@ int lgpu_solver_run(lgpu_handle *h) {
     for (int j = c0; j < c1 && a0 < 0; j++) if (h->h_col2act[j] >= 0) a0 = h->h_col2act[j];
     for (int j = c1 - 1; j >= c0 && a1 < 0; j--) if (h->h_col2act[j] >= 0) a1 = h->h_col2act[j] + 1;
     CK(cudaEventRecord(h->ev_chunk[c][0], st), "event");
-    if (batch > 0 && a0 >= 0) CK(launch_eig_split(st, ea, sp, batch, a0 * G, (a1 - a0) * G, &launches), "eigen kernels");
+    if (!fp64 && batch > 0 && a0 >= 0)
+      CK(launch_eig_split(st, ea, sp, batch, a0 * G, (a1 - a0) * G, &launches), "eigen kernels");
+    CK(cudaEventRecord(h->ev_chunk[c][3], st), "event");
+    if (fp64 && a0 >= 0) {
+      EigArgs e64 = ea;
+      e64.nunits = (a1 - a0) * G;
+      CK(launch_eig64(st, e64, a0 * G, &launches), "FP64 eigen kernel");
+    } else if (batch > 0 && a0 >= 0 && ea.flag_list) {
+      CK(launch_eig64_flagged(st, ea, &launches), "FP64 re-solve");
+    }
     CK(cudaEventRecord(h->ev_chunk[c][1], st), "event");
     ua.col0 = c0;
     ua.ncols = c1 - c0;
@@ -1019,17 +1065,22 @@ int lgpu_solver_run(lgpu_handle *h) {
   }
   CK(cudaEventRecord(h->ev[5], st), "event");
   int stat4[4] = {0, 0, 0, 0};
+  int nflag = 0;
   CK(cudaMemcpyAsync(stat4, h->buf[B_STATUS].p, 16, cudaMemcpyDeviceToHost, st), "D2H status");
+  if (ea.flag_n) CK(cudaMemcpyAsync(&nflag, ea.flag_n, 4, cudaMemcpyDeviceToHost, st), "D2H flag count");
   CK(cudaStreamSynchronize(st), "solver_run");
   if (bound) CK(cudaStreamSynchronize(h->cst), "solver_run copies");
   float ms[3];
   for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
   for (int c = 0; c < nrec; c++) {
     float te = 0.0f, tu = 0.0f;
+    float tf = 0.0f;
     CK(cudaEventElapsedTime(&te, h->ev_chunk[c][0], h->ev_chunk[c][1]), "timing");
     CK(cudaEventElapsedTime(&tu, h->ev_chunk[c][1], h->ev_chunk[c][2]), "timing");
+    CK(cudaEventElapsedTime(&tf, h->ev_chunk[c][3], h->ev_chunk[c][1]), "timing");
     eig_ms += te;
     upd_ms += tu;
+    fp64_ms += tf;
   }
   h->tim.index_ms = ms[0];
   h->tim.prep_ms = ms[1];
@@ -1045,6 +1096,9 @@ int lgpu_solver_run(lgpu_handle *h) {
   h->tim.kept_pairs = -1;
   h->tim.mma_chunks = h->used_tc ? stat4[2] : 0;
   h->tim.mma_n = h->used_tc ? h->mma_n : 0;
+  h->tim.precision = h->prec;
+  h->tim.fp64_units = fp64 ? h->nunits : std::min(nflag, ea.flag_cap);   // with a fused-kernel fallback: 0
+  h->tim.fp64_ms = fp64_ms;
   const int status = stat4[0];
   h->ran = true;
   if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
@@ -1200,7 +1254,10 @@ int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, f
   std::vector<int> ones(nunits + 1, 1);
   ones[nunits] = 0;   // status word
   if (e == cudaSuccess) e = cudaMemcpyAsync(dn, ones.data(), 4 * ((size_t)nunits + 1), cudaMemcpyHostToDevice, h->st);
-  if (e == cudaSuccess) e = launch_eig_debug(h->st, nunits, k, dG, dn, dT, dn + nunits);
+  int nfp64 = 0;
+  if (e == cudaSuccess) e = launch_eig_debug(h->st, nunits, k, dG, dn, dT, dn + nunits, h->prec, h->gap_thresh, &nfp64);
+  h->tim.precision = h->prec;
+  h->tim.fp64_units = nfp64;
   int status = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(trans, dT, 4 * nt * nunits, cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status, dn + nunits, 4, cudaMemcpyDeviceToHost, h->st);
@@ -1731,12 +1788,21 @@ static int learned_exact(lgpu_handle *h, const ObsSorted &os, int n, int &launch
   ea.wbar = L->wsub.as<float>();
   ea.ulist = nullptr;
   ea.status = h->buf[B_STATUS].as<int>();
+  flag_args(h, ea);
+  if (h->prec == LGPU_PREC_FP64) {
+    CK(launch_eig64(st, ea, 0, &launches), "FP64 eigen kernel");
+    return LGPU_OK;
+  }
   EigSplit sp;
   int batch = 0;
   int rc = eig_scratch(h, n, sp, batch);
   if (rc != LGPU_OK) return rc;
-  if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
-  else CK(launch_eig_split(st, ea, sp, batch, 0, n, &launches), "eigen kernels");
+  if (batch == 0) {
+    CK(launch_eig(st, ea, &launches), "eigen kernel");
+  } else {
+    CK(launch_eig_split(st, ea, sp, batch, 0, n, &launches), "eigen kernels");
+    if (ea.flag_list) CK(launch_eig64_flagged(st, ea, &launches), "FP64 re-solve");
+  }
   return LGPU_OK;
 }
 
@@ -1749,6 +1815,7 @@ static int learned_run(lgpu_handle *h) {
   int launches = 0;
   int rc = prepare_run(h, os, launches);
   if (rc != LGPU_OK) return rc;
+  if ((rc = flag_prepare(h)) != LGPU_OK) return rc;
   cudaStream_t st = h->st;
   const int k = h->k;
   const MlpShape &S = L->shape;
@@ -1878,7 +1945,10 @@ static int learned_run(lgpu_handle *h) {
   CK(cudaEventRecord(h->ev[5], st), "event");
   int stat4[4] = {0, 0, 0, 0};
   float jacc[4] = {0, 0, 0, 0};
+  int nflag = 0;
   CK(cudaMemcpyAsync(stat4, h->buf[B_STATUS].p, 16, cudaMemcpyDeviceToHost, st), "D2H status");
+  if (h->prec == LGPU_PREC_FP32_RESOLVE)
+    CK(cudaMemcpyAsync(&nflag, h->buf[B_FLAGLIST].p, 4, cudaMemcpyDeviceToHost, st), "D2H flag count");
   CK(cudaMemcpyAsync(jacc, L->jacc.p, 16, cudaMemcpyDeviceToHost, st), "D2H judge");
   CK(cudaStreamSynchronize(st), "solver_run");
   float ms[3];
@@ -1898,6 +1968,9 @@ static int learned_run(lgpu_handle *h) {
   h->tim.kept_pairs = -1;
   h->tim.mma_chunks = 0;
   h->tim.mma_n = 0;
+  h->tim.precision = h->prec;
+  h->tim.fp64_units = h->prec == LGPU_PREC_FP64 ? nex + ngate : std::min(nflag, 2 * std::max(1, h->nunits));
+  h->tim.fp64_ms = 0.0f;   // inside exact_ms of the learned statistics
   L->st.coarse = ncoarse;
   L->st.judged = nj;
   L->st.fallback = (int)L->fine_miss.size();

@@ -19,12 +19,27 @@
 // warp (shared memory broadcasts) with lane 0 as the only writer; the split
 // pipeline runs it once per unit and replays the logged rotations.
 #include "lgpu_internal.cuh"
+#include <algorithm>
 
 namespace lgpu {
 
 namespace {
 
-__device__ __forceinline__ float wsum(float v) {
+__device__ __forceinline__ float fmar(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmar(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float rcpr(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcpr(double x) { return __drcp_rn(x); }
+// unit roundoff and the smallest scale treated as zero, per precision
+template <class R> struct Lim;
+template <> struct Lim<float> {
+  static constexpr float eps = 1.1920929e-7f, tiny = 1e-30f;
+};
+template <> struct Lim<double> {
+  static constexpr double eps = 2.220446049250313e-16, tiny = 1e-300;
+};
+
+template <class R>
+__device__ __forceinline__ R wsum(R v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
@@ -39,23 +54,23 @@ __host__ __device__ __forceinline__ int eig_floats_per_warp(int k) {
 // (several units per CTA); NW > 1 is one unit per CTA, so the CTA barrier is
 // the team barrier.  Sums run over the warp's butterfly, then over the warps
 // in warp order (deterministic).
-template <int NW>
+template <int NW, class R = float>
 struct Team {
   static constexpr int TS = 32 * NW;
   int tt, lane, warp;
-  float *red;   // NW floats in shared memory (NW > 1)
+  R *red;       // NW values in shared memory (NW > 1)
   __device__ __forceinline__ void sync() const {
     if constexpr (NW == 1) __syncwarp();
     else __syncthreads();
   }
-  __device__ __forceinline__ float sum(float v) const {
-    v = wsum(v);
+  __device__ __forceinline__ R sum(R v) const {
+    v = wsum<R>(v);
     if constexpr (NW == 1) {
       return v;
     } else {
       if (lane == 0) red[warp] = v;
       __syncthreads();
-      float t = red[0];
+      R t = red[0];
 #pragma unroll
       for (int q = 1; q < NW; q++) t += red[q];
       __syncthreads();
@@ -66,9 +81,10 @@ struct Team {
 
 // Work arrays of one unit in shared memory: A (k x ld, ld = k + 1) holds A,
 // then Q, then V; then d, e, tau, bv, p, w, fl, gl (k each).
+template <class R = float>
 struct EigWork {
-  float *A, *d, *e, *tau, *bv, *p, *w, *fl, *gl;
-  __device__ EigWork(float *base, int k) {
+  R *A, *d, *e, *tau, *bv, *p, *w, *fl, *gl;
+  __device__ EigWork(R *base, int k) {
     A = base;
     d = A + k * (k + 1);
     e = d + k; tau = e + k; bv = tau + k; p = bv + k; w = p + k; fl = w + k; gl = fl + k;
@@ -76,20 +92,20 @@ struct EigWork {
 };
 
 // A = G + (k-1)/infl I from the packed Gram block, b from its tail
-template <int NW>
-__device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork &W, const Team<NW> &T) {
+template <int NW, class R>
+__device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork<R> &W, const Team<NW, R> &T) {
   const int k = a.k, ld = k + 1, tt = T.tt, TS = T.TS;
-  float *A = W.A, *bv = W.bv;
-  const float *G = a.G + (size_t)unit * packed_size(k);
+  R *A = W.A, *bv = W.bv;
+  const float *Gin = a.G + (size_t)unit * packed_size(k);
   // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
-  const float shift = (float)(k - 1) * 1.0f / a.infl;
+  const R shift = (R)(k - 1) * R(1) / (R)a.infl;
   for (int t = tt; t < k * k; t += TS) {
     const int i = t / k, j = t % k;
-    float v = (i <= j) ? G[tri_idx(i, j, k)] : G[tri_idx(j, i, k)];
+    R v = (i <= j) ? (R)Gin[tri_idx(i, j, k)] : (R)Gin[tri_idx(j, i, k)];
     if (i == j) v += shift;
     A[i * ld + j] = v;
   }
-  for (int i = tt; i < k; i += TS) bv[i] = G[k * (k + 1) / 2 + i];
+  for (int i = tt; i < k; i += TS) bv[i] = (R)Gin[k * (k + 1) / 2 + i];
   T.sync();
 
 }
@@ -97,52 +113,52 @@ __device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork &W,
 // Householder tridiagonalisation (d, e, tau; reflector vectors in the
 // columns of A) and Q formed in place.  NQ: rows / columns per lane
 // (tt + TS q, q < NQ).
-template <int NQ, int NW>
-__device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> &T) {
+template <int NQ, int NW, class R>
+__device__ __forceinline__ void eig_tridiag_q(int k, EigWork<R> &W, const Team<NW, R> &T) {
   const int ld = k + 1, tt = T.tt, TS = T.TS;
-  float *A = W.A, *d = W.d, *e = W.e, *tau = W.tau, *p = W.p, *w = W.w;
-  float *vv = W.fl;   // the current reflector, contiguous (fl is free until the transform)
+  R *A = W.A, *d = W.d, *e = W.e, *tau = W.tau, *p = W.p, *w = W.w;
+  R *vv = W.fl;   // the current reflector, contiguous (fl is free until the transform)
   // ---- Householder tridiagonalisation: column j's reflector zeroes A[j+2:, j];
   // its vector v_j = A[j+1:, j] stays in column j
   for (int j = 0; j < k - 2; j++) {
     const int m = k - j - 1;                 // length of x = A[j+1:, j]
-    float s = 0.0f;
-    for (int r = tt; r < m; r += TS) { float x = A[(j + 1 + r) * ld + j]; s += x * x; }
-    const float sig = T.sum(s);
-    const float x0 = A[(j + 1) * ld + j];
-    const float s1 = sig - x0 * x0;
-    if (!(s1 > 1e-30f * sig) || sig == 0.0f) {
-      if (tt == 0) { tau[j] = 0.0f; e[j] = x0; d[j] = A[j * ld + j]; }
+    R s = R(0);
+    for (int r = tt; r < m; r += TS) { R x = A[(j + 1 + r) * ld + j]; s += x * x; }
+    const R sig = T.sum(s);
+    const R x0 = A[(j + 1) * ld + j];
+    const R s1 = sig - x0 * x0;
+    if (!(s1 > Lim<R>::tiny * sig) || sig == R(0)) {
+      if (tt == 0) { tau[j] = R(0); e[j] = x0; d[j] = A[j * ld + j]; }
       T.sync();
       continue;
     }
-    const float alpha = -copysignf(sqrtf(sig), x0);
-    const float v0 = x0 - alpha;
-    const float t = 2.0f / (v0 * v0 + s1);
+    const R alpha = -copysign(sqrt(sig), x0);
+    const R v0 = x0 - alpha;
+    const R t = R(2) / (v0 * v0 + s1);
     T.sync();
     if (tt == 0) { A[(j + 1) * ld + j] = v0; tau[j] = t; e[j] = alpha; d[j] = A[j * ld + j]; }
     for (int r = tt; r < m; r += TS) vv[r] = r == 0 ? v0 : A[(j + 1 + r) * ld + j];
     T.sync();
     // p = t * A22 v
     for (int r = tt; r < m; r += TS) {
-      const float *row = A + (j + 1 + r) * ld + (j + 1);
-      float acc = 0.0f;
+      const R *row = A + (j + 1 + r) * ld + (j + 1);
+      R acc = R(0);
 #pragma unroll 4
-      for (int c = 0; c < m; c++) acc = __fmaf_rn(row[c], vv[c], acc);
+      for (int c = 0; c < m; c++) acc = fmar(row[c], vv[c], acc);
       p[r] = t * acc;
     }
     T.sync();
-    float pv = 0.0f;
-    for (int r = tt; r < m; r += TS) pv = __fmaf_rn(p[r], vv[r], pv);
-    const float beta = 0.5f * t * T.sum(pv);
+    R pv = R(0);
+    for (int r = tt; r < m; r += TS) pv = fmar(p[r], vv[r], pv);
+    const R beta = R(0.5) * t * T.sum(pv);
     for (int r = tt; r < m; r += TS) w[r] = p[r] - beta * vv[r];
     T.sync();
     // A22 -= v w^T + w v^T
     for (int r = tt; r < m; r += TS) {
-      float *row = A + (j + 1 + r) * ld + (j + 1);
-      const float vr = vv[r], wr = w[r];
+      R *row = A + (j + 1 + r) * ld + (j + 1);
+      const R vr = vv[r], wr = w[r];
 #pragma unroll 4
-      for (int c = 0; c < m; c++) row[c] = row[c] - __fmaf_rn(vr, w[c], wr * vv[c]);
+      for (int c = 0; c < m; c++) row[c] = row[c] - fmar(vr, w[c], wr * vv[c]);
     }
     T.sync();
   }
@@ -152,7 +168,7 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
       e[k - 2] = A[(k - 1) * ld + (k - 2)];
     }
     d[k - 1] = A[(k - 1) * ld + (k - 1)];
-    e[k - 1] = 0.0f;
+    e[k - 1] = R(0);
   }
   T.sync();
 
@@ -166,35 +182,35 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
         const int c = tt + TS * q;
-        if (c > j + 1 && c < k) { A[(j + 1) * ld + c] = 0.0f; A[c * ld + (j + 1)] = 0.0f; }
+        if (c > j + 1 && c < k) { A[(j + 1) * ld + c] = R(0); A[c * ld + (j + 1)] = R(0); }
       }
-      if (tt == 0) A[(j + 1) * ld + (j + 1)] = 1.0f;
+      if (tt == 0) A[(j + 1) * ld + (j + 1)] = R(1);
       T.sync();
       if (j > k - 3) continue;                 // the last block (2 x 2) has no reflector
-      const float t = tau[j];
-      if (t == 0.0f) continue;
+      const R t = tau[j];
+      if (t == R(0)) continue;
       const int m = k - j - 1;
       for (int r = tt; r < m; r += TS) vv[r] = A[(j + 1 + r) * ld + j];
       T.sync();
       // w_c = t * sum_r v_r Q[r][c]; Q[r][c] -= v_r w_c  (rows, columns j+1..k-1)
-      float wc[NQ];
+      R wc[NQ];
       bool in[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
         const int c = tt + TS * q;
-        wc[q] = 0.0f;
+        wc[q] = R(0);
         in[q] = c > j && c < k;
       }
       for (int r = 0; r < m; r++) {
-        const float v = vv[r];
+        const R v = vv[r];
 #pragma unroll
         for (int q = 0; q < NQ; q++)
-          if (in[q]) wc[q] = __fmaf_rn(v, A[(j + 1 + r) * ld + tt + TS * q], wc[q]);
+          if (in[q]) wc[q] = fmar(v, A[(j + 1 + r) * ld + tt + TS * q], wc[q]);
       }
 #pragma unroll
       for (int q = 0; q < NQ; q++) wc[q] *= t;
       for (int r = 0; r < m; r++) {
-        const float v = vv[r];
+        const R v = vv[r];
 #pragma unroll
         for (int q = 0; q < NQ; q++)
           if (in[q]) A[(j + 1 + r) * ld + tt + TS * q] -= v * wc[q];
@@ -205,41 +221,42 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork &W, const Team<NW> 
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
       const int c = tt + TS * q;
-      if (c > 0 && c < k) { A[c] = 0.0f; A[c * ld] = 0.0f; }
+      if (c > 0 && c < k) { A[c] = R(0); A[c * ld] = R(0); }
     }
-    if (tt == 0) A[0] = 1.0f;
+    if (tt == 0) A[0] = R(1);
     T.sync();
   }
 
 }
 
 // spectral functions and T = U U^T + wbar 1^T (A holds V, d the eigenvalues)
-template <int NQ, int NW>
-__device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWork &W, const Team<NW> &TM, int &bad) {
+template <int NQ, int NW, class R>
+__device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWork<R> &W, const Team<NW, R> &TM,
+                                              int &bad) {
   const int k = a.k, ld = k + 1, tt = TM.tt, TS = TM.TS;
-  float *A = W.A, *d = W.d, *bv = W.bv, *p = W.p, *w = W.w, *fl = W.fl, *gl = W.gl;
+  R *A = W.A, *d = W.d, *bv = W.bv, *p = W.p, *w = W.w, *fl = W.fl, *gl = W.gl;
   // ---- spectral functions: f = sqrt((k-1)/lambda), g = 1/lambda
   //      (src/letkf_core.F90:111-113, :128-131); fl holds sqrt(f)
   for (int l = tt; l < k; l += TS) {
-    const float lam = d[l];
-    if (!(lam > 0.0f)) bad |= 2;
-    fl[l] = sqrtf(sqrtf((float)(k - 1) / lam));
-    gl[l] = 1.0f / lam;
+    const R lam = d[l];
+    if (!(lam > R(0))) bad |= 2;
+    fl[l] = sqrt(sqrt((R)(k - 1) / lam));
+    gl[l] = R(1) / lam;
   }
   TM.sync();
   // s_l = g_l * (V^T b)_l
   for (int l = tt; l < k; l += TS) {
-    float acc = 0.0f;
-    for (int q = 0; q < k; q++) acc = __fmaf_rn(A[q * ld + l], bv[q], acc);
+    R acc = R(0);
+    for (int q = 0; q < k; q++) acc = fmar(A[q * ld + l], bv[q], acc);
     p[l] = gl[l] * acc;
   }
   TM.sync();
   // wbar_i = sum_l V[i][l] s_l
   for (int i = tt; i < k; i += TS) {
-    float acc = 0.0f;
-    for (int l = 0; l < k; l++) acc = __fmaf_rn(A[i * ld + l], p[l], acc);
+    R acc = R(0);
+    for (int l = 0; l < k; l++) acc = fmar(A[i * ld + l], p[l], acc);
     w[i] = acc;
-    if (a.wbar) a.wbar[(size_t)unit * k + i] = acc;
+    if (a.wbar) a.wbar[(size_t)unit * k + i] = (float)acc;
   }
   TM.sync();
   // U = V diag(sqrt f) in place: T = U U^T + wbar 1^T
@@ -247,24 +264,24 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
   TM.sync();
   // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; thread owns columns tt + TS q
   // (a column past k repeats the thread's first column and is not stored)
-  float *T = a.T + (size_t)unit * k * k;
+  float *Tout = a.T + (size_t)unit * k * k;
   if (tt < k) {
-    const float *u[NQ];
+    const R *u[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; q++) u[q] = A + (tt + TS * q < k ? tt + TS * q : tt) * ld;
     for (int i = 0; i < k; i++) {
-      const float *ur = A + i * ld;
-      float acc[NQ];
+      const R *ur = A + i * ld;
+      R acc[NQ];
 #pragma unroll
-      for (int q = 0; q < NQ; q++) acc[q] = 0.0f;
+      for (int q = 0; q < NQ; q++) acc[q] = R(0);
       for (int l = 0; l < k; l++) {
-        const float y = ur[l];
+        const R y = ur[l];
 #pragma unroll
-        for (int q = 0; q < NQ; q++) acc[q] = __fmaf_rn(y, u[q][l], acc[q]);
+        for (int q = 0; q < NQ; q++) acc[q] = fmar(y, u[q][l], acc[q]);
       }
 #pragma unroll
       for (int q = 0; q < NQ; q++)
-        if (tt + TS * q < k) T[i * k + tt + TS * q] = acc[q] + w[i];
+        if (tt + TS * q < k) Tout[i * k + tt + TS * q] = (R)(acc[q] + w[i]);
     }
   }
 }
@@ -277,24 +294,26 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
 // from the Householder reduction) keeps a strongly graded block from
 // meeting the local test; it leaves the eigenvalues within the backward
 // error the reduction has already made.
-__device__ __forceinline__ bool ql_negligible(float em, float dm, float dm1, float tabs) {
-  const float ae = fabsf(em);
-  return ae <= 1.1920929e-7f * (fabsf(dm) + fabsf(dm1)) || ae <= tabs;
+template <class R>
+__device__ __forceinline__ bool ql_negligible(R em, R dm, R dm1, R tabs) {
+  const R ae = fabs(em);
+  return ae <= Lim<R>::eps * (fabs(dm) + fabs(dm1)) || ae <= tabs;
 }
 
 // eps32 * max_i (|d_i| + |e_i|), elements at stride `st`
-__device__ __forceinline__ float ql_abs_tol(int k, const float *d, const float *e, int st) {
-  float an = 0.0f;
-  for (int i = 0; i < k; i++) an = fmaxf(an, fabsf(d[(size_t)i * st]) + fabsf(e[(size_t)i * st]));
-  return 1.1920929e-7f * an;
+template <class R>
+__device__ __forceinline__ R ql_abs_tol(int k, const R *d, const R *e, int st) {
+  R an = R(0);
+  for (int i = 0; i < k; i++) an = fmax(an, fabs(d[(size_t)i * st]) + fabs(e[(size_t)i * st]));
+  return Lim<R>::eps * an;
 }
 
 // implicit-shift QL on (d, e) with the rotations applied to the columns of
 // A (Q -> V), one warp
-template <int NQ>
-__device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &bad) {
+template <int NQ, class R>
+__device__ __forceinline__ void eig_ql_warp(int k, EigWork<R> &W, int lane, int &bad) {
   const int ld = k + 1;
-  float *A = W.A, *d = W.d, *e = W.e;
+  R *A = W.A, *d = W.d, *e = W.e;
   // ---- implicit-shift QL on (d, e), rotations applied at once to the
   // columns (i, i+1) of Q (V = Q Z).  The scalar recurrence is evaluated
   // redundantly by every lane: d[i+1] is carried in a register and only e[i],
@@ -303,13 +322,13 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
   // lane + 32 q of Q and carries the pending column i+1 of its rows.
   {
     bool own[NQ];
-    float *qr[NQ];
+    R *qr[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
       own[q] = lane + 32 * q < k;
       qr[q] = A + (own[q] ? lane + 32 * q : 0) * ld;
     }
-    const float tabs = ql_abs_tol(k, d, e, 1);
+    const R tabs = ql_abs_tol(k, d, e, 1);
     for (int l = 0; l < k; l++) {
       int iter = 0;
       for (;;) {
@@ -325,37 +344,37 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
         }
         if (m == l) break;
         if (++iter > 60) { bad = 1; break; }
-        const float dl = d[l], el = e[l];
-        float g = (d[l + 1] - dl) / (2.0f * el);
-        float r = sqrtf(g * g + 1.0f);
-        g = d[m] - dl + el / (g + copysignf(r, g));
-        float s = 1.0f, c = 1.0f, pp = 0.0f;
-        float di1 = d[m];
-        float z[NQ];   // pending column i+1
+        const R dl = d[l], el = e[l];
+        R g = (d[l + 1] - dl) / (R(2) * el);
+        R r = sqrt(g * g + R(1));
+        g = d[m] - dl + el / (g + copysign(r, g));
+        R s = R(1), c = R(1), pp = R(0);
+        R di1 = d[m];
+        R z[NQ];   // pending column i+1
 #pragma unroll
-        for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : 0.0f;
-        float ei = e[m - 1], di = d[m - 1];
+        for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : R(0);
+        R ei = e[m - 1], di = d[m - 1];
         int i = m - 1;
         bool deflate = false;
         for (; i >= l; i--) {
           const int in = i > 0 ? i - 1 : 0;
-          const float ei_n = e[in], di_n = d[in];           // next step's operands
-          float av[NQ];
+          const R ei_n = e[in], di_n = d[in];           // next step's operands
+          R av[NQ];
 #pragma unroll
-          for (int q = 0; q < NQ; q++) av[q] = own[q] ? qr[q][i] : 0.0f;
-          const float f = s * ei, b = c * ei;
-          r = sqrtf(f * f + g * g);
+          for (int q = 0; q < NQ; q++) av[q] = own[q] ? qr[q][i] : R(0);
+          const R f = s * ei, b = c * ei;
+          r = sqrt(f * f + g * g);
           if (lane == 0) e[i + 1] = r;
-          if (r == 0.0f) {
-            if (lane == 0) { d[i + 1] = di1 - pp; e[m] = 0.0f; }
+          if (r == R(0)) {
+            if (lane == 0) { d[i + 1] = di1 - pp; e[m] = R(0); }
             deflate = true;
             break;
           }
-          const float ir = __frcp_rn(r);
+          const R ir = rcpr(r);
           s = f * ir;
           c = g * ir;
           g = di1 - pp;
-          const float rr = (di - g) * s + 2.0f * c * b;
+          const R rr = (di - g) * s + R(2) * c * b;
           pp = s * rr;
           if (lane == 0) d[i + 1] = g + pp;
           g = c * rr - b;
@@ -371,7 +390,7 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork &W, int lane, int &ba
 #pragma unroll
         for (int q = 0; q < NQ; q++)
           if (own[q]) qr[q][ilo] = z[q];
-        if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = 0.0f; }
+        if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = R(0); }
         __syncwarp();
       }
       if (bad) break;
@@ -503,7 +522,7 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
   sp.logn[ub] = bad ? -1 : (pos > sp.cap ? -2 : pos);
   float *lam = sp.lam + (size_t)ub * k;
   for (int i = 0; i < k; i++) lam[i] = d[(size_t)i * QLT];
-  if (bad) atomicOr(a.status, bad);
+  if (bad && !a.flag_list) atomicOr(a.status, bad);   // with flagging, the FP64 re-solve takes the unit
 }
 
 template <int NQ, int NW>
@@ -591,10 +610,118 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   T.sync();
   eig_transform<NQ>(a, unit, W, T, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);
-  if (bad && lane == 0) atomicOr(a.status, bad);
+  if (bad && a.flag_list) {
+    if (lane == 0) sp.logn[ub] = -1;   // k_eig_flag hands the unit to the FP64 re-solve
+  } else if (bad && lane == 0) {
+    atomicOr(a.status, bad);
+  }
+}
+
+// FP64 re-solve candidates of a batch (warp per unit, after k_eig_vec):
+// the FP32 solve failed, or two relevant eigenvalues lie within
+// gap_thresh * max l of each other.  The eigenvalues at the (k-1)/infl floor
+// (the null space of the Gram, k - n of them when n < k) are exactly
+// degenerate and harmless, since T is a function of the matrix and not of
+// the basis chosen in an eigenspace; they are left out of the test.
+__global__ void k_eig_flag(EigArgs a, EigSplit sp, int u0, int nb) {
+  const int lane = threadIdx.x & 31;
+  const int ub = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (ub >= nb) return;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  const int k = a.k;
+  bool flag = sp.logn[ub] == -1;
+  if (!flag) {
+    const float *lam = sp.lam + (size_t)ub * k;
+    float lmax = 0.0f;
+    for (int i = lane; i < k; i += 32) lmax = fmaxf(lmax, lam[i]);
+    for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    // rounding level of the FP32 eigenvalues: a few k eps of the largest
+    const float floor_v = (float)(k - 1) / a.infl;
+    const float tol = 4.0f * (float)k * 1.1920929e-7f * lmax;
+    float gap = 3.0e38f;
+    for (int i = lane; i < k; i += 32) {
+      const float li = lam[i];
+      if (li - floor_v <= tol) continue;
+      for (int j = 0; j < k; j++) {
+        const float lj = lam[j];
+        if (j != i && lj - floor_v > tol) gap = fminf(gap, fabsf(li - lj));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) gap = fminf(gap, __shfl_xor_sync(0xffffffffu, gap, o));
+    flag = gap <= a.gap_thresh * lmax;
+  }
+  if (flag && lane == 0) {
+    const int pos = atomicAdd(a.flag_n, 1);
+    if (pos < a.flag_cap) a.flag_list[pos] = unit;
+    else atomicOr(a.status, 128);   // list full: the unit keeps its FP32 solve
+  }
+}
+
+// FP64 eigensolve + transform, one warp per unit, grid-stride over the
+// units: ulist / ubase + 0..nunits, or (range != null) the flagged entries
+// flag_list[range[1] .. min(range[0], flag_cap))
+template <int NQ>
+__global__ void k_eig64(EigArgs a, int wpb, int ubase, const int *range) {
+  extern __shared__ __align__(16) double smd[];
+  const int k = a.k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int beg = 0, end = a.nunits;
+  const int *list = a.ulist;
+  if (range) {
+    beg = range[1];
+    end = min(range[0], a.flag_cap);
+    list = a.flag_list;
+  }
+  EigWork<double> W(smd + (size_t)warp * eig_floats_per_warp(k), k);
+  const Team<1, double> T{lane, lane, warp, nullptr};
+  for (int un = beg + blockIdx.x * wpb + warp; un < end; un += gridDim.x * wpb) {
+    const int unit = list ? list[un] : ubase + un;
+    if (a.nkept[unit] <= 0) continue;
+    __syncwarp();   // the previous unit's transform has read the work arrays
+    eig_load(a, unit, W, T);
+    eig_tridiag_q<NQ>(k, W, T);
+    int bad = 0;
+    eig_ql_warp<NQ>(k, W, lane, bad);
+    eig_transform<NQ>(a, unit, W, T, bad);
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && lane == 0) atomicOr(a.status, bad);
+  }
 }
 
 }  // namespace
+
+namespace {
+int eig64_wpb(int k) {
+  const size_t per = (size_t)eig_floats_per_warp(k) * sizeof(double);
+  return (int)std::max<size_t>(1, std::min<size_t>(8, (160 * 1024) / per));
+}
+cudaError_t eig64_go(cudaStream_t st, const EigArgs &a, int ubase, const int *range, int blocks, int *launches) {
+  const int wpb = eig64_wpb(a.k);
+  const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(double);
+  auto kern = a.k > 64 ? k_eig64<4> : k_eig64<2>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kern<<<blocks, 32 * wpb, smem, st>>>(a, wpb, ubase, range);
+  (*launches)++;
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_eig64(cudaStream_t st, const EigArgs &a, int ubase, int *launches) {
+  if (a.nunits <= 0) return cudaSuccess;
+  const int wpb = eig64_wpb(a.k);
+  return eig64_go(st, a, ubase, nullptr, std::min((a.nunits + wpb - 1) / wpb, 152 * 16), launches);
+}
+
+cudaError_t launch_eig64_flagged(cudaStream_t st, const EigArgs &a, int *launches) {
+  if (!a.flag_list || a.flag_cap <= 0) return cudaSuccess;
+  const int wpb = eig64_wpb(a.k);
+  // flagged units are few; a small grid strides over however many there are
+  cudaError_t e = eig64_go(st, a, 0, a.flag_n, std::min((a.flag_cap + wpb - 1) / wpb, 152 * 2), launches);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(a.flag_n + 1, a.flag_n, sizeof(int), cudaMemcpyDeviceToDevice, st);
+}
 
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
 
@@ -643,6 +770,10 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
     k_eig_vec<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
     (*launches) += 3;
+    if (a.flag_list) {
+      k_eig_flag<<<(nb + 7) / 8, 256, 0, st>>>(a, sp, u0, nb);
+      (*launches)++;
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -663,10 +794,14 @@ cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &
 }
 
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
-                             int *status) {
+                             int *status, int prec, float gap_thresh, int *nfp64) {
   EigArgs a;
   a.wbar = nullptr;
   a.ulist = nullptr;
+  a.flag_list = nullptr;
+  a.flag_n = nullptr;
+  a.flag_cap = 0;
+  a.gap_thresh = gap_thresh;
   a.nunits = nunits;
   a.k = k;
   a.infl = 1.0f;
@@ -674,25 +809,41 @@ cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G,
   a.nkept = nkept;
   a.T = T;
   a.status = status;
+  *nfp64 = 0;
+  int l = 0;
+  if (prec == LGPU_PREC_FP64) {
+    cudaError_t e = launch_eig64(st, a, 0, &l);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    *nfp64 = nunits;
+    return e != cudaSuccess ? e : e2;
+  }
   // the split pipeline, as lgpu_solver_run uses it
   const size_t per = eig_split_bytes_per_unit(k);
+  const size_t n = nunits > 0 ? nunits : 1;
   unsigned char *buf = nullptr;
-  cudaError_t e = cudaMalloc(&buf, per * (size_t)(nunits > 0 ? nunits : 1) + 256);
+  cudaError_t e = cudaMalloc(&buf, per * n + 256 + 16 + 4 * n + 256);
   if (e != cudaSuccess) return e;
   EigSplit sp;
   size_t off = 0;
   auto take = [&](size_t bytes) { unsigned char *p = buf + off; off += (bytes + 255) & ~(size_t)255; return p; };
-  const size_t n = nunits > 0 ? nunits : 1;
   sp.Q = reinterpret_cast<float *>(take(n * k * k * 4));
   sp.DE = reinterpret_cast<float *>(take(n * 2 * k * 4));
   sp.log = reinterpret_cast<float2 *>(take(n * (size_t)eig_log_cap(k) * 8));
   sp.logn = reinterpret_cast<int *>(take(n * 4));
   sp.lam = reinterpret_cast<float *>(take(n * k * 4));
   sp.cap = eig_log_cap(k);
-  int l = 0;
-  e = launch_eig_split(st, a, sp, nunits, 0, nunits, &l);
+  if (prec == LGPU_PREC_FP32_RESOLVE) {
+    a.flag_n = reinterpret_cast<int *>(take(16 + 4 * n));
+    a.flag_list = a.flag_n + 4;
+    a.flag_cap = (int)n;
+    e = cudaMemsetAsync(a.flag_n, 0, 16, st);
+  }
+  if (e == cudaSuccess) e = launch_eig_split(st, a, sp, nunits, 0, nunits, &l);
+  if (e == cudaSuccess && a.flag_list) e = launch_eig64_flagged(st, a, &l);
+  if (e == cudaSuccess && a.flag_n) e = cudaMemcpyAsync(nfp64, a.flag_n, 4, cudaMemcpyDeviceToHost, st);
   cudaError_t e2 = cudaStreamSynchronize(st);
   cudaFree(buf);
+  if (*nfp64 > (int)n) *nfp64 = (int)n;
   return e != cudaSuccess ? e : e2;
 }
 

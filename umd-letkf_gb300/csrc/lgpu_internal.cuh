@@ -443,7 +443,22 @@ struct EigArgs {
   float *wbar;            // [unit][k] mean weights, or null
   const int *ulist;       // units to solve (the i-th is ulist[i]), or null: units 0..nunits-1
   int *status;            // [1] accumulated error bits
+  // FP64 re-solve (split pipeline): a unit whose FP32 solve failed (no
+  // convergence, a non-positive or non-finite eigenvalue) or whose relevant
+  // FP32 eigenvalues (those above the (k-1)/infl floor by more than the
+  // rounding level) have a relative gap min|l_i - l_j| / max l <= gap_thresh
+  // is appended to flag_list (flag_n[0] = entries written, at most
+  // flag_cap; flag_n[1] = entries already re-solved); null: no flagging
+  int *flag_list, *flag_n;
+  int flag_cap;
+  float gap_thresh;
 };
+// FP64 eigensolve + transform (one warp per unit): units ulist[0..nunits) or
+// ubase + 0..nunits; T (and w-bar) written in FP32
+cudaError_t launch_eig64(cudaStream_t st, const EigArgs &a, int ubase, int *launches);
+// FP64 re-solve of the flagged units not yet re-solved (flag_list entries
+// flag_n[1] .. flag_n[0]); the count stays on the device
+cudaError_t launch_eig64_flagged(cudaStream_t st, const EigArgs &a, int *launches);
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
 // scratch of the split eigensolve pipeline, for `batch` units
 struct EigSplit {

@@ -77,7 +77,8 @@ class Timings(ctypes.Structure):
                 ("gram_ms", ctypes.c_float), ("eig_ms", ctypes.c_float), ("update_ms", ctypes.c_float),
                 ("launches", ctypes.c_int), ("units", ctypes.c_int), ("kept_pairs", ctypes.c_longlong),
                 ("variant", ctypes.c_int), ("tiles_ms", ctypes.c_float), ("mma_chunks", ctypes.c_longlong),
-                ("mma_n", ctypes.c_int)]
+                ("mma_n", ctypes.c_int), ("precision", ctypes.c_int), ("fp64_units", ctypes.c_int),
+                ("fp64_ms", ctypes.c_float)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -85,6 +86,8 @@ class Timings(ctypes.Structure):
 
 VARIANT_AUTO, VARIANT_PLAIN, VARIANT_BATCHED_TC, VARIANT_LEARNED = 0, 1, 2, 3
 VARIANTS = {"auto": 0, "plain": 1, "batched": 2, "learned": 3}
+PREC_FP32, PREC_FP32_RESOLVE, PREC_FP64 = 0, 1, 2
+PRECISIONS = {"fp32": 0, "fp32_resolve": 1, "fp64": 2}
 
 
 class _LearnCfg(ctypes.Structure):
@@ -111,7 +114,7 @@ EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error",
            "lgpu_get_obs_prepared", "lgpu_debug_transform", "lgpu_bind_state",
            "lgpu_debug_weight", "lgpu_learn_init", "lgpu_learn_collect", "lgpu_learn_train", "lgpu_learn_stats_get",
            "lgpu_learn_param_count", "lgpu_learn_get_params", "lgpu_learn_set_params", "lgpu_mlp_debug",
-           "lgpu_learn_set_network"]
+           "lgpu_learn_set_network", "lgpu_set_precision"]
 
 _lib = None
 
@@ -135,6 +138,7 @@ def lib(path=None):
     L.lgpu_loc_init.argtypes = [H, ctypes.POINTER(_LocCfg)]
     L.lgpu_loc_maxgroups.argtypes = [H]
     L.lgpu_set_variant.argtypes = [H, ctypes.c_int]
+    L.lgpu_set_precision.argtypes = [H, ctypes.c_int, ctypes.c_float]
     L.lgpu_set_grid.argtypes = [H, ctypes.c_int, FP, FP, IP]
     L.lgpu_set_state.argtypes = [H, ctypes.c_int, ctypes.c_int, FP, FP, FP, ctypes.c_int, ctypes.POINTER(_Var)]
     L.lgpu_set_obs.argtypes = [H, ctypes.c_int, ctypes.POINTER(_Obs), FP, FP]
@@ -295,6 +299,13 @@ class Solver:
         (128-column tiles on the tensor cores) or 'auto'."""
         v = VARIANTS[variant] if isinstance(variant, str) else int(variant)
         return self._ck(self.L.lgpu_set_variant(self.h, v))
+
+    def set_precision(self, mode, gap_threshold=1e-6):
+        """Eigensolve precision: 'fp32' (the reference's), 'fp32_resolve'
+        (FP32, FP64 re-solve of units with a failed solve or a relative
+        eigenvalue gap <= gap_threshold) or 'fp64' (every unit)."""
+        m = PRECISIONS[mode] if isinstance(mode, str) else int(mode)
+        return self._ck(self.L.lgpu_set_precision(self.h, m, float(gap_threshold)))
 
     # -- letkf_solver_init
     def solver_init(self, cfg=None, **kw):
