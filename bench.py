@@ -223,7 +223,8 @@ def workload_config(args, prob, cfg):
             "columns_total": int(prob.ncol), "columns_active": nact, "ensemble": int(prob.k), "slabs": int(prob.ns),
             "observations": int(prob.nobs), "l2": "flushed (256 MB device write) before every timed step; "
                                                   "state in+out %.1f GB per step" % state_gb,
-            "parallelism": "replicas" if args.gpus > 1 else "single"}
+            "parallelism": "replicas" if args.gpus > 1 else "single",
+            "eig_precision": args.precision}
 
 
 def gpu_arm(args, dist):
@@ -233,6 +234,7 @@ def gpu_arm(args, dist):
     dev = dist.local if dist.world > 1 else 0
     s = Solver(dev)
     s.set_variant(args.variant)
+    s.set_precision(args.precision)
     s.solver_init(cfg["solver"])
     s.loc_init(cfg["localization"], prob.vars, prob.lev_depth)
     s.set_problem(prob)
@@ -275,7 +277,8 @@ def gpu_arm(args, dist):
     stages = {
         "tile_streams": {"ms": stage["tiles_ms"]},
         "gram": {"ms": gram_kernel_ms, "tflops": gram_flop / (gram_kernel_ms * 1e-3) / 1e12},
-        "eig": {"ms": stage["eig_ms"], "tflops": eig_flop / (stage["eig_ms"] * 1e-3) / 1e12},
+        "eig": {"ms": stage["eig_ms"], "tflops": eig_flop / (stage["eig_ms"] * 1e-3) / 1e12,
+                "fp64_units": tims[-1]["fp64_units"], "fp64_ms": tims[-1]["fp64_ms"]},
         "update": {"ms": stage["update_ms"], "gbs": upd_bytes / (stage["update_ms"] * 1e-3) / 1e9},
         "index": {"ms": stage["index_ms"]}, "prep": {"ms": stage["prep_ms"]},
         "kept_pairs": kept, "candidate_pairs": cand}
@@ -521,6 +524,7 @@ def single_run(args):
     s = Solver(0)
     try:
         s.set_variant(args.variant)
+        s.set_precision(args.precision)
         s.solver_init(cfg["solver"])
         s.loc_init(cfg["localization"], prob.vars, prob.lev_depth)
         s.set_problem(prob)
@@ -553,6 +557,8 @@ def main():
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default="auto", choices=["auto", "plain", "batched"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32_resolve", "fp64"],
+                    help="eigensolve precision (FP32 as the reference; FP64 re-solve of flagged units; FP64)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-variant comparison run")
     ap.add_argument("--single-run", action="store_true",
                     help="one analysis of --workload (no timing loop): the case profiled under ncu")
