@@ -110,6 +110,12 @@ def test_learned_form_cycling():
         s.run()
         ip = s.get_state()
         s.learn_set_network(True)
+        # the exact solves of the learned form in FP64: every one counted
+        s.set_precision("fp64")
+        s.run()
+        le64 = s.get_state()
+        st64, t64 = s.learn_stats(), s.timings()
+        s.set_precision("fp32")
     finally:
         s.close()
     act = p.mask == 0
@@ -123,3 +129,8 @@ def test_learned_form_cycling():
     # 1.36% of the background spread at 60 epochs, 1.23% at 25)
     assert err_l < 0.97 * err_i
     assert err_l <= 0.02
+    assert t64["precision"] == 2
+    assert t64["fp64_units"] == st64["coarse"] + st64["judged"] + st64["fallback"] + st64["gated"]
+    assert np.all(np.isfinite(le64[0])) and np.all(np.isfinite(le64[1]))
+    err_64 = float(np.sqrt(np.mean((le64[1][act] - ex[1][act]) ** 2))) / spread
+    assert err_64 <= 0.02

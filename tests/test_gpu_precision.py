@@ -132,3 +132,43 @@ def test_analysis_precision_modes(name):
     # than the FP32 solve beyond rounding of the stored result
     assert errs["fp64"] <= errs["fp32"] * 1.25 + 1e-7, errs
     o.close()
+
+
+@pytest.mark.parametrize("mode,gap", [("fp32_resolve", 1e-4), ("fp64", 1e-6)])
+def test_precision_with_bound_state(mode, gap):
+    """A bound state runs the eigensolve in 8 column chunks: the FP64 re-solve
+    of each chunk takes the units flagged since the previous chunk (a device
+    count); the result equals the unbound run's bit for bit."""
+    from letkf_gb300 import Solver
+    cfg = workload_cfg("c4small")
+    p = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
+
+    def solver():
+        s = Solver(0)
+        s.set_variant("batched")
+        s.set_precision(mode, gap)
+        s.solver_init(cfg["solver"])
+        s.loc_init(cfg["localization"], p.vars, p.lev_depth)
+        s.set_grid(p.lat, p.lon, p.mask)
+        return s
+
+    s = solver()
+    try:
+        s.set_state(p.state, p.mean, p.sprd, p.vars)
+        s.set_obs(p.olat, p.olon, p.oz, p.otime, p.oval, p.oerr, p.oobsid, p.oplatid, p.hx, p.hx_mean)
+        s.run()
+        ref, tref = s.get_state(), s.timings()
+    finally:
+        s.close()
+    arrs = [a.copy() for a in (p.state, p.mean, p.sprd)]
+    s = solver()
+    try:
+        s.bind_state(arrs[0], arrs[1], arrs[2], p.vars)
+        s.set_obs(p.olat, p.olon, p.oz, p.otime, p.oval, p.oerr, p.oobsid, p.oplatid, p.hx, p.hx_mean)
+        s.run()
+        tb = s.timings()
+    finally:
+        s.close()
+    assert tb["fp64_units"] == tref["fp64_units"] and tb["fp64_units"] > 0
+    for got, want in zip(arrs, ref):
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), mode
