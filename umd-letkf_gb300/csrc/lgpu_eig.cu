@@ -658,12 +658,122 @@ __global__ void k_eig_flag(EigArgs a, EigSplit sp, int u0, int nb) {
   }
 }
 
-// FP64 eigensolve + transform, one warp per unit, grid-stride over the
-// units: ulist / ubase + 0..nunits, or (range != null) the flagged entries
-// flag_list[range[1] .. min(range[0], flag_cap))
-template <int NQ>
-__global__ void k_eig64(EigArgs a, int wpb, int ubase, const int *range) {
+// Implicit-shift QL for a team of NW warps: per sweep, warp 0 evaluates the
+// scalar recurrence (as eig_ql_warp: redundantly on its lanes, lane 0
+// writing d, e and the rotations (c, s) of the sweep into cs_c / cs_s), then
+// every thread of the team applies the sweep's rotations to its own rows of
+// Q (rows tt + TS q) in the same order and arithmetic as eig_ql_warp.
+// ctl[0]: the sweep's m (-1: l converged, -2: no convergence), ctl[1]: the
+// lowest rotated column.
+template <int NQ, int NW, class R>
+__device__ __forceinline__ void eig_ql_team(int k, EigWork<R> &W, const Team<NW, R> &T, R *cs_c, R *cs_s,
+                                            int *ctl, int &bad) {
+  const int ld = k + 1, tt = T.tt, TS = T.TS, lane = T.lane;
+  R *A = W.A, *d = W.d, *e = W.e;
+  bool own[NQ];
+  R *qr[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    own[q] = tt + TS * q < k;
+    qr[q] = A + (own[q] ? tt + TS * q : 0) * ld;
+  }
+  const R tabs = ql_abs_tol(k, d, e, 1);
+  for (int l = 0; l < k; l++) {
+    int iter = 0;
+    for (;;) {
+      if (T.warp == 0) {
+        int m = k - 1;
+        for (int base = l; base < k - 1; base += 32) {
+          const int mm = base + lane;
+          bool small = false;
+          if (mm < k - 1) small = ql_negligible(e[mm], d[mm], d[mm + 1], tabs);
+          const unsigned bal = __ballot_sync(0xffffffffu, small);
+          if (bal) { m = base + __ffs(bal) - 1; break; }
+        }
+        int c0 = m, c1 = l;
+        if (m == l) {
+          c0 = -1;
+        } else if (++iter > 60) {
+          c0 = -2;
+        } else {
+          const R dl = d[l], el = e[l];
+          R g = (d[l + 1] - dl) / (R(2) * el);
+          R r = sqrt(g * g + R(1));
+          g = d[m] - dl + el / (g + copysign(r, g));
+          R s = R(1), c = R(1), pp = R(0);
+          R di1 = d[m];
+          R ei = e[m - 1], di = d[m - 1];
+          int i = m - 1;
+          bool deflate = false;
+          for (; i >= l; i--) {
+            const int in = i > 0 ? i - 1 : 0;
+            const R ei_n = e[in], di_n = d[in];
+            const R f = s * ei, b = c * ei;
+            r = sqrt(f * f + g * g);
+            if (lane == 0) e[i + 1] = r;
+            if (r == R(0)) {
+              if (lane == 0) { d[i + 1] = di1 - pp; e[m] = R(0); }
+              deflate = true;
+              break;
+            }
+            const R ir = rcpr(r);
+            s = f * ir;
+            c = g * ir;
+            g = di1 - pp;
+            const R rr = (di - g) * s + R(2) * c * b;
+            pp = s * rr;
+            if (lane == 0) { d[i + 1] = g + pp; cs_c[i] = c; cs_s[i] = s; }
+            g = c * rr - b;
+            di1 = di;
+            ei = ei_n;
+            di = di_n;
+          }
+          c1 = deflate ? i + 1 : l;
+          if (!deflate && lane == 0) { d[l] = d[l] - pp; e[l] = g; e[m] = R(0); }
+        }
+        if (lane == 0) { ctl[0] = c0; ctl[1] = c1; }
+      }
+      T.sync();
+      const int m = ctl[0], ilo = ctl[1];
+      if (m < 0) {
+        if (m == -2) bad = 1;
+        T.sync();   // ctl is read by every thread before warp 0 writes it again
+        break;
+      }
+      R z[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : R(0);
+      for (int i = m - 1; i >= ilo; i--) {
+        const R c = cs_c[i], s = cs_s[i];
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+          if (own[q]) {
+            const R av = qr[q][i];
+            qr[q][i + 1] = s * av + c * z[q];
+            z[q] = c * av - s * z[q];
+          }
+      }
+#pragma unroll
+      for (int q = 0; q < NQ; q++)
+        if (own[q]) qr[q][ilo] = z[q];
+      T.sync();
+    }
+    if (bad) break;
+  }
+  T.sync();
+}
+
+// FP64 eigensolve + transform, a team of NW warps per unit (one unit per
+// block at a time), grid-stride over the units: ulist / ubase + 0..nunits,
+// or (range != null) the flagged entries flag_list[range[1] ..
+// min(range[0], flag_cap)).  GB300 runs FP64 at 1/64 of the FP32 rate, so a
+// single unit's latency (the re-solve of a few flagged units) is spread over
+// the SM's four schedulers.
+template <int NW>
+__global__ void k_eig64(EigArgs a, int ubase, const int *range) {
   extern __shared__ __align__(16) double smd[];
+  __shared__ double tred[NW];
+  __shared__ int ctl[2];
   const int k = a.k;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int beg = 0, end = a.nunits;
@@ -673,17 +783,17 @@ __global__ void k_eig64(EigArgs a, int wpb, int ubase, const int *range) {
     end = min(range[0], a.flag_cap);
     list = a.flag_list;
   }
-  EigWork<double> W(smd + (size_t)warp * eig_floats_per_warp(k), k);
-  const Team<1, double> T{lane, lane, warp, nullptr};
-  for (int un = beg + blockIdx.x * wpb + warp; un < end; un += gridDim.x * wpb) {
+  EigWork<double> W(smd, k);
+  const Team<NW, double> T{(int)threadIdx.x, lane, warp, tred};
+  for (int un = beg + blockIdx.x; un < end; un += gridDim.x) {
     const int unit = list ? list[un] : ubase + un;
     if (a.nkept[unit] <= 0) continue;
-    __syncwarp();   // the previous unit's transform has read the work arrays
+    __syncthreads();   // the previous unit's transform has read the work arrays
     eig_load(a, unit, W, T);
-    eig_tridiag_q<NQ>(k, W, T);
+    eig_tridiag_q<1>(k, W, T);
     int bad = 0;
-    eig_ql_warp<NQ>(k, W, lane, bad);
-    eig_transform<NQ>(a, unit, W, T, bad);
+    eig_ql_team<1>(k, W, T, W.p, W.w, ctl, bad);
+    eig_transform<1>(a, unit, W, T, bad);
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(a.status, bad);
   }
@@ -692,33 +802,40 @@ __global__ void k_eig64(EigArgs a, int wpb, int ubase, const int *range) {
 }  // namespace
 
 namespace {
-int eig64_wpb(int k) {
-  const size_t per = (size_t)eig_floats_per_warp(k) * sizeof(double);
-  return (int)std::max<size_t>(1, std::min<size_t>(8, (160 * 1024) / per));
-}
-cudaError_t eig64_go(cudaStream_t st, const EigArgs &a, int ubase, const int *range, int blocks, int *launches) {
-  const int wpb = eig64_wpb(a.k);
-  const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(double);
-  auto kern = a.k > 64 ? k_eig64<4> : k_eig64<2>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// warps per unit of the FP64 kernel: every row of Q on its own thread
+int eig64_team(int k) { return k <= 64 ? 2 : 4; }
+
+template <int NW>
+cudaError_t eig64_go_t(cudaStream_t st, const EigArgs &a, int ubase, const int *range, int blocks, int *launches) {
+  const size_t smem = (size_t)eig_floats_per_warp(a.k) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_eig64<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<blocks, 32 * wpb, smem, st>>>(a, wpb, ubase, range);
+  k_eig64<NW><<<blocks, 32 * NW, smem, st>>>(a, ubase, range);
   (*launches)++;
   return cudaGetLastError();
+}
+
+cudaError_t eig64_go(cudaStream_t st, const EigArgs &a, int ubase, const int *range, int blocks, int *launches) {
+  return eig64_team(a.k) == 2 ? eig64_go_t<2>(st, a, ubase, range, blocks, launches)
+                              : eig64_go_t<4>(st, a, ubase, range, blocks, launches);
+}
+
+// resident units per SM (one per block), from the shared memory of one unit
+int eig64_per_sm(int k) {
+  const size_t per = (size_t)eig_floats_per_warp(k) * sizeof(double) + 1024;
+  return std::max(1, std::min(16, (int)((227 * 1024) / per)));
 }
 }  // namespace
 
 cudaError_t launch_eig64(cudaStream_t st, const EigArgs &a, int ubase, int *launches) {
   if (a.nunits <= 0) return cudaSuccess;
-  const int wpb = eig64_wpb(a.k);
-  return eig64_go(st, a, ubase, nullptr, std::min((a.nunits + wpb - 1) / wpb, 152 * 16), launches);
+  return eig64_go(st, a, ubase, nullptr, std::min(a.nunits, 152 * eig64_per_sm(a.k)), launches);
 }
 
 cudaError_t launch_eig64_flagged(cudaStream_t st, const EigArgs &a, int *launches) {
   if (!a.flag_list || a.flag_cap <= 0) return cudaSuccess;
-  const int wpb = eig64_wpb(a.k);
-  // flagged units are few; a small grid strides over however many there are
-  cudaError_t e = eig64_go(st, a, 0, a.flag_n, std::min((a.flag_cap + wpb - 1) / wpb, 152 * 2), launches);
+  // one block per flagged unit up to the resident limit; the count stays on the device
+  cudaError_t e = eig64_go(st, a, 0, a.flag_n, std::min(a.flag_cap, 152 * eig64_per_sm(a.k)), launches);
   if (e != cudaSuccess) return e;
   return cudaMemcpyAsync(a.flag_n + 1, a.flag_n, sizeof(int), cudaMemcpyDeviceToDevice, st);
 }
