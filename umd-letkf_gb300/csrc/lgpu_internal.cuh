@@ -453,7 +453,7 @@ struct EigArgs {
   int flag_cap;
   float gap_thresh;
 };
-// FP64 eigensolve + transform (one warp per unit): units ulist[0..nunits) or
+// FP64 eigensolve + transform (a team of warps per unit): units ulist[0..nunits) or
 // ubase + 0..nunits; T (and w-bar) written in FP32
 cudaError_t launch_eig64(cudaStream_t st, const EigArgs &a, int ubase, int *launches);
 // FP64 re-solve of the flagged units not yet re-solved (flag_list entries
