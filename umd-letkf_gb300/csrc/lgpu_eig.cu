@@ -938,7 +938,8 @@ cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G,
   const size_t per = eig_split_bytes_per_unit(k);
   const size_t n = nunits > 0 ? nunits : 1;
   unsigned char *buf = nullptr;
-  cudaError_t e = cudaMalloc(&buf, per * n + 256 + 16 + 4 * n + 256);
+  // six arrays, each start rounded up to 256 bytes (at most 5 * 255 bytes of padding)
+  cudaError_t e = cudaMalloc(&buf, per * n + 16 + 4 * n + 6 * 256);
   if (e != cudaSuccess) return e;
   EigSplit sp;
   size_t off = 0;
