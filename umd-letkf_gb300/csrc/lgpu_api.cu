@@ -77,6 +77,7 @@ struct lgpu_handle {
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev_in[2] = {};       // bound state: mean/spread, members uploaded
   cudaEvent_t ev_tune[3] = {};     // AUTO: timing of the two Gram forms
+  cudaEvent_t ev_cull[3] = {};     // batched Gram: timing of its two producer forms
   // per column chunk: eigensolve start, update start, update end, FP64 eigensolve start
   cudaEvent_t ev_chunk[kOutChunks][4] = {};
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
@@ -101,6 +102,8 @@ struct lgpu_handle {
   int mma_n = 0;
   int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
   int gram_nseg = 1;     // accumulation segments of the last batched Gram
+  int tc_cull = -1;      // batched Gram producers: 1 with the warp-level cull, 0 without, -1 not yet measured
+  float tc_tune_ms = 0.0f;   // time of the producer form the tuning run discarded (left out of AUTO's comparison)
   int prec = LGPU_PREC_FP32;   // eigensolve precision mode
   float gap_thresh = 1e-6f;    // FP32_RESOLVE: relative eigenvalue gap that sends a unit to FP64
   DevBuf buf[B_COUNT_ALL];
@@ -242,6 +245,8 @@ int lgpu_create(int device, lgpu_handle **out) {
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_tune)
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_cull)
+    if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &row : h->ev_chunk)
     for (auto &ev : row)
       if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
@@ -265,6 +270,7 @@ void lgpu_destroy(lgpu_handle *h) {
   for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_in) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_tune) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : h->ev_cull) if (ev) cudaEventDestroy(ev);
   for (auto &row : h->ev_chunk)
     for (auto &ev : row) if (ev) cudaEventDestroy(ev);
   if (h->st) cudaStreamDestroy(h->st);
@@ -345,6 +351,7 @@ int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *c) {
   h->loc = L;
   h->loc_ok = true;
   h->auto_choice = 0;
+  h->tc_cull = -1;
   h->ran = false;
   return LGPU_OK;
 }
@@ -403,6 +410,7 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
   CK(cudaStreamSynchronize(h->st), "set_grid sync");
   h->ntiles = (int)(tiles.size() / 128);
   h->auto_choice = 0;
+  h->tc_cull = -1;
   h->ncol = nij;
   h->nact = (int)act.size();
   h->h_col2act = c2a;
@@ -462,7 +470,7 @@ int prepare_state(lgpu_handle *h, int k, int ns, const float *state, const float
   CK(cudaMemcpyAsync(h->buf[B_VARLB].p, lb.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D lb");
   CK(cudaMemcpyAsync(h->buf[B_VARUB].p, ub.data(), nvars * 4, cudaMemcpyHostToDevice, h->st), "H2D ub");
   CK(cudaStreamSynchronize(h->st), "set_state sync");
-  if (h->k != k) h->auto_choice = 0;
+  if (h->k != k) { h->auto_choice = 0; h->tc_cull = -1; }
   h->k = k;
   h->ns = ns;
   h->kp = (k + 3) & ~3;
@@ -928,7 +936,28 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
     }
   }
   h->gram_nseg = ta.nseg;
-  CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+  if (h->tc_cull < 0) {
+    // the first batched Gram of a configuration runs both producer forms,
+    // timed, and keeps the faster; their outputs are bit-identical, and every
+    // output of the Gram kernels is overwritten by the second run (the
+    // executed-MMA counter is reset between them)
+    float tm[2] = {0.0f, 0.0f};
+    for (int v = 0; v < 2; v++) {
+      ta.cull = v;
+      if (v == 1) CK(cudaMemsetAsync(h->buf[B_STATUS].as<int>() + 2, 0, sizeof(int), st), "memset");
+      CK(cudaEventRecord(h->ev_cull[v], st), "event");
+      CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+    }
+    CK(cudaEventRecord(h->ev_cull[2], st), "event");
+    CK(cudaEventSynchronize(h->ev_cull[2]), "tune sync");
+    CK(cudaEventElapsedTime(&tm[0], h->ev_cull[0], h->ev_cull[1]), "timing");
+    CK(cudaEventElapsedTime(&tm[1], h->ev_cull[1], h->ev_cull[2]), "timing");
+    h->tc_cull = tm[1] < tm[0] ? 1 : 0;
+    h->tc_tune_ms = std::max(tm[0], tm[1]);
+  } else {
+    ta.cull = h->tc_cull;
+    CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
+  }
   CK(launch_gram_segsum(st, ta, h->buf[B_ACTIVE].as<int>(), &launches), "gram segment sum");
   
     return LGPU_OK;
@@ -984,6 +1013,8 @@ int lgpu_solver_run(lgpu_handle *h) {
     float tp = 0.0f, tb = 0.0f;
     CK(cudaEventElapsedTime(&tp, h->ev_tune[0], h->ev_tune[1]), "timing");
     CK(cudaEventElapsedTime(&tb, h->ev_tune[1], h->ev_tune[2]), "timing");
+    tb -= h->tc_tune_ms;   // the batched form's producer tuning ran its Gram twice
+    h->tc_tune_ms = 0.0f;
     h->auto_choice = tb <= tp ? LGPU_VARIANT_BATCHED_TC : LGPU_VARIANT_PLAIN;
     // the kept result is the chosen form's
     if (h->auto_choice == LGPU_VARIANT_PLAIN && (rc = run_plain()) != LGPU_OK) return rc;

@@ -333,8 +333,12 @@ __device__ __forceinline__ void bar_arrive(unsigned long long *b) {
 // weight cache as the stage's TF32 hi/lo operand block, with the chunk's
 // MMA flag (first feature pass of a tile); 2 = the operand block is
 // bulk-copied from the cache into the stage (later passes: the producers
-// form only the feature products)
-template <int LOC, int NS, int NR, int WMODE>
+// form only the feature products).  CULL (WMODE 0, 1): a warp whose 32
+// columns have none of its four records within their search chords skips
+// the distance and localizer evaluation (their weights are zero either way;
+// results are bit-identical); pays where search radii are small next to the
+// tile caps, costs registers where they are not
+template <int LOC, int NS, int NR, int WMODE, bool CULL>
 __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(16) TcSmem S;
@@ -443,24 +447,37 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         }
       } else {
       // ---- weights: four observations, fast path without branches
-      float w[4];
+      float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
       unsigned unsure = 0, inr = 0;
+      unsigned candm = 0xfu;
+      if constexpr (CULL) {
+        candm = 0;
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int e = wq * 4 + u;
-        const float4 A = RA[e];
-        const float4 B = RA[16 + e];
-        const float c2f = chord2_fast(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
-        const bool cand = (ch * KC + e < ntile) && (c2f <= c2max);
-        const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
-        const float d = 12742000.0f * asin_fast(fminf(hf, 0.5f), short_asin);
-        const float rl = loc_fast<LOC>(lk, cp, g, d, B);
-        const bool in = cand && d <= cp.rmax;
-        const bool uns = cand && (hf > 0.5f || (d >= rlo && d <= rhi) || (in && fabsf(rl - kKeep) <= kGuardFast));
-        const bool kept = in && rl > kKeep;
-        w[u] = kept ? rl : 0.0f;
-        unsure |= (uns ? 1u : 0u) << u;
-        inr |= (in ? 1u : 0u) << u;
+        for (int u = 0; u < 4; u++) {
+          const int e = wq * 4 + u;
+          const float4 A = RA[e];
+          const float c2f = chord2_fast(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
+          candm |= ((ch * KC + e < ntile) && (c2f <= c2max) ? 1u : 0u) << u;
+        }
+      }
+      if (!CULL || __any_sync(0xffffffffu, candm != 0)) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = wq * 4 + u;
+          const float4 A = RA[e];
+          const float4 B = RA[16 + e];
+          const float c2f = chord2_fast(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
+          const bool cand = (ch * KC + e < ntile) && (c2f <= c2max);
+          const float hf = 0.5f * c2f * rsqrtf(fmaxf(c2f, 1e-30f));
+          const float d = 12742000.0f * asin_fast(fminf(hf, 0.5f), short_asin);
+          const float rl = loc_fast<LOC>(lk, cp, g, d, B);
+          const bool in = cand && d <= cp.rmax;
+          const bool uns = cand && (hf > 0.5f || (d >= rlo && d <= rhi) || (in && fabsf(rl - kKeep) <= kGuardFast));
+          const bool kept = in && rl > kKeep;
+          w[u] = kept ? rl : 0.0f;
+          unsure |= (uns ? 1u : 0u) << u;
+          inr |= (in ? 1u : 0u) << u;
+        }
       }
       // ---- rare: exact metric and the per-column localizer
       if (__any_sync(0xffffffffu, unsure != 0)) {
@@ -768,13 +785,19 @@ cudaError_t launch_tile_fill(cudaStream_t st, int ntiles, const TilePar *tp, con
   return cudaGetLastError();
 }
 
+template <int LOC, int NS, int NR, int WMODE, bool CULL>
+static cudaError_t launch_gram_tc_c(cudaStream_t st, const TcArgs &a, size_t smem, long long grid) {
+  cudaError_t e = cudaFuncSetAttribute(k_gram_tc<LOC, NS, NR, WMODE, CULL>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_gram_tc<LOC, NS, NR, WMODE, CULL><<<(int)grid, NT, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 template <int LOC, int NS, int NR, int WMODE>
 static cudaError_t launch_gram_tc_t(cudaStream_t st, const TcArgs &a, size_t smem, long long grid) {
-  cudaError_t e =
-      cudaFuncSetAttribute(k_gram_tc<LOC, NS, NR, WMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_gram_tc<LOC, NS, NR, WMODE><<<(int)grid, NT, smem, st>>>(a);
-  return cudaGetLastError();
+  if (WMODE != 2 && a.cull) return launch_gram_tc_c<LOC, NS, NR, WMODE, WMODE != 2>(st, a, smem, grid);
+  return launch_gram_tc_c<LOC, NS, NR, WMODE, false>(st, a, smem, grid);
 }
 
 template <int LOC>

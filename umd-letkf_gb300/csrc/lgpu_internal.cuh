@@ -409,6 +409,7 @@ struct TcArgs {
   // counts at cnt + s * units * 3 (segment 0 too when nseg > 1), summed in
   // segment order by launch_gram_segsum
   int nseg;
+  int cull;               // 1: a warp skips the distance and localizer of four records none of its columns can reach
   long long units;
   float *Gpart;
   float *cnt;                // [nseg][units][3]: kept, candidates, sum rho (when nseg > 1)
