@@ -16,6 +16,9 @@ pytestmark = pytest.mark.gpu
 def _solver(cfg, p):
     from letkf_gb300 import Solver
     s = Solver(0)
+    # one Gram form for both solvers: AUTO decides by timing, and the two
+    # forms agree to rounding, not bit for bit
+    s.set_variant("batched")
     s.solver_init(cfg["solver"])
     s.loc_init(cfg["localization"], p.vars, p.lev_depth)
     s.set_grid(p.lat, p.lon, p.mask)

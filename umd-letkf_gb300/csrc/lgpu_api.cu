@@ -104,6 +104,7 @@ struct lgpu_handle {
   int gram_nseg = 1;     // accumulation segments of the last batched Gram
   int tc_cull = -1;      // batched Gram producers: 1 with the warp-level cull, 0 without, -1 not yet measured
   float tc_tune_ms = 0.0f;   // time of the producer form the tuning run discarded (left out of AUTO's comparison)
+  bool preloaded = false;    // the Gram kernels are loaded (before the first timed trial)
   int prec = LGPU_PREC_FP32;   // eigensolve precision mode
   float gap_thresh = 1e-6f;    // FP32_RESOLVE: relative eigenvalue gap that sends a unit to FP64
   DevBuf buf[B_COUNT_ALL];
@@ -352,6 +353,7 @@ int lgpu_loc_init(lgpu_handle *h, const lgpu_loc_config *c) {
   h->loc_ok = true;
   h->auto_choice = 0;
   h->tc_cull = -1;
+  h->preloaded = false;
   h->ran = false;
   return LGPU_OK;
 }
@@ -411,6 +413,7 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
   h->ntiles = (int)(tiles.size() / 128);
   h->auto_choice = 0;
   h->tc_cull = -1;
+  h->preloaded = false;
   h->ncol = nij;
   h->nact = (int)act.size();
   h->h_col2act = c2a;
@@ -1003,6 +1006,12 @@ int lgpu_solver_run(lgpu_handle *h) {
   int choice = h->variant;
   if (choice == LGPU_VARIANT_AUTO) choice = k < 8 ? LGPU_VARIANT_PLAIN : h->auto_choice;
   int rc = LGPU_OK;
+  if (!h->preloaded && (choice == 0 || (choice == LGPU_VARIANT_BATCHED_TC && h->tc_cull < 0))) {
+    // the trials below time kernels: load them first
+    CK(preload_gram(), "kernel load");
+    CK(preload_gram_tc(h->loc.cls), "kernel load");
+    h->preloaded = true;
+  }
   if (choice == 0) {
     CK(cudaEventRecord(h->ev_tune[0], st), "event");
     if ((rc = run_plain()) != LGPU_OK) return rc;

@@ -451,6 +451,18 @@ cudaError_t launch_gram(cudaStream_t st, const GramArgs &a, int *launches) {
   }
 }
 
+// loads the plain Gram kernels (CUDA loads a kernel at its first use, which
+// must not fall inside a timed trial)
+cudaError_t preload_gram(void) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, k_gram<1>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_gram<2>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_gram<3>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_gram<4>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_gram<5>);
+  return e;
+}
+
 cudaError_t launch_obslist(cudaStream_t st, int col, int gid, int group_slot, const ColPar *cp_col, const DevLoc &loc,
                            ObsSorted obs, const IndexGeom *geom, int cap, int *d_idx, float *d_r, int *d_counts) {
   (void)col; (void)group_slot;

@@ -887,4 +887,37 @@ size_t gram_tc_wcache_bytes(int groups, int nchunk_total) {
   return (size_t)groups * nchunk_total * (WCB + sizeof(int));   // operand blocks, then the MMA flags
 }
 
+template <int LOC>
+static cudaError_t preload_gram_tc_loc() {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaSuccess;
+  auto get = [&](const void *f) { if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, f); };
+  get((const void *)k_gram_tc<LOC, 3, 3, 0, false>);
+  get((const void *)k_gram_tc<LOC, 3, 3, 0, true>);
+  get((const void *)k_gram_tc<LOC, 3, 3, 1, false>);
+  get((const void *)k_gram_tc<LOC, 3, 3, 1, true>);
+  get((const void *)k_gram_tc<LOC, 3, 3, 2, false>);
+  get((const void *)k_gram_tc<LOC, 2, 6, 0, false>);
+  get((const void *)k_gram_tc<LOC, 2, 6, 0, true>);
+  get((const void *)k_gram_tc<LOC, 2, 6, 1, false>);
+  get((const void *)k_gram_tc<LOC, 2, 6, 1, true>);
+  get((const void *)k_gram_tc<LOC, 2, 6, 2, false>);
+  get((const void *)k_tile_prep);
+  get((const void *)k_tile_count);
+  get((const void *)k_tile_scan);
+  get((const void *)k_tile_fill);
+  get((const void *)k_gram_segsum);
+  return e;
+}
+
+// loads the batched Gram's kernels for a localizer class (CUDA loads a
+// kernel at its first use, which must not fall inside a timed trial)
+cudaError_t preload_gram_tc(int loc_cls) {
+  switch (loc_cls) {
+  case LOC_OCEAN: return preload_gram_tc_loc<LOC_OCEAN>();
+  case LOC_VTGC: return preload_gram_tc_loc<LOC_VTGC>();
+  default: return preload_gram_tc_loc<LOC_NOVRT>();
+  }
+}
+
 }  // namespace lgpu

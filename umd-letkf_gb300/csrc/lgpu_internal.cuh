@@ -432,6 +432,10 @@ cudaError_t launch_tile_fill(cudaStream_t st, int ntiles, const TilePar *tp, con
                              const ObsSorted &obs, int k, int kp, const int *tile_off, unsigned char *rec,
                              int *status, int *launches);
 cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a, int *launches);
+// CUDA loads a kernel at its first use: these load the plain and the batched
+// (for one localizer class) Gram kernels ahead of a timed trial
+cudaError_t preload_gram(void);
+cudaError_t preload_gram_tc(int loc_cls);
 size_t gram_tc_wcache_bytes(int groups, int nchunk_total);
 void gram_tc_passes(int k, int *npass, int *np);
 
