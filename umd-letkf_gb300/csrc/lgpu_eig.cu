@@ -110,6 +110,9 @@ __device__ __forceinline__ void eig_load(const EigArgs &a, int unit, EigWork<R> 
 
 }
 
+template <int NQ, int NW, class R>
+__device__ __forceinline__ void eig_form_q(int k, EigWork<R> &W, const Team<NW, R> &T);
+
 // Householder tridiagonalisation (d, e, tau; reflector vectors in the
 // columns of A) and Q formed in place.  NQ: rows / columns per lane
 // (tt + TS q, q < NQ).
@@ -171,11 +174,20 @@ __device__ __forceinline__ void eig_tridiag_q(int k, EigWork<R> &W, const Team<N
     e[k - 1] = R(0);
   }
   T.sync();
+  eig_form_q<NQ>(k, W, T);
+}
 
-  // ---- Q = H_0 H_1 ... H_{k-3} formed in place, last reflector first: the
-  // trailing block [j+1:, j+1:] holds H_{j+1}..H_{k-3} (identity on row and
-  // column j+1); v_j is still in column j, outside the block.  Each thread
-  // owns columns tt + TS q.
+// Q = H_0 H_1 ... H_{k-3} formed in place from the reflectors in the columns
+// of A below the diagonal (v_j in column j, tau[j]), last reflector first:
+// the trailing block [j+1:, j+1:] holds H_{j+1}..H_{k-3} (identity on row
+// and column j+1); v_j is still in column j, outside the block.  Each thread
+// owns columns tt + TS q.  The entries on and above the diagonal are not read
+// before they are written.
+template <int NQ, int NW, class R>
+__device__ __forceinline__ void eig_form_q(int k, EigWork<R> &W, const Team<NW, R> &T) {
+  const int ld = k + 1, tt = T.tt, TS = T.TS;
+  R *A = W.A, *tau = W.tau;
+  R *vv = W.fl;
   {
     for (int j = k - 2; j >= 0; j--) {
       // identity on row and column j + 1 of the block
@@ -432,6 +444,126 @@ __global__ void k_eig(EigArgs a, int wpb) {
 
 // NW = 1: wpb units per CTA, one warp each; NW > 1: one unit per CTA of NW
 // warps (wpb = 1)
+// ---- packed reduction: the symmetric work matrix as its lower triangle,
+// L[i][j] (j <= i) at i(i+1)/2 + j, half the shared memory of the full
+// matrix (twice the units per SM).  Triangular numbers of 32 consecutive rows
+// are distinct modulo 32, so a warp reading one element of each of its rows
+// is conflict-free.
+__host__ __device__ __forceinline__ int ptri(int i) { return i * (i + 1) / 2; }
+
+__host__ __device__ __forceinline__ int eig_pk_floats(int k) { return ((ptri(k) + 3) & ~3) + 6 * k + 8; }
+
+struct EigPk {
+  float *L, *d, *e, *tau, *p, *w, *vv;
+  __device__ EigPk(float *base, int k) {
+    L = base;
+    d = L + ((ptri(k) + 3) & ~3);
+    e = d + k; tau = e + k; p = tau + k; w = p + k; vv = w + k;
+  }
+};
+
+// The Householder reduction of eig_tridiag_q on the packed lower triangle:
+// the same steps, with the trailing block read as A22[r][c] = L[max][min]
+// and its rank-two update applied to the lower triangle only (v_j stays in
+// column j below the diagonal, tau[j] and d, e as in eig_tridiag_q).
+template <int NW>
+__device__ __forceinline__ void eig_householder_pk(int k, EigPk &P, const Team<NW> &T) {
+  const int tt = T.tt, TS = T.TS;
+  float *L = P.L, *d = P.d, *e = P.e, *tau = P.tau, *p = P.p, *w = P.w, *vv = P.vv;
+  for (int j = 0; j < k - 2; j++) {
+    const int m = k - j - 1;                 // length of x = A[j+1:, j]
+    float s = 0.0f;
+    for (int r = tt; r < m; r += TS) { const float x = L[ptri(j + 1 + r) + j]; s += x * x; }
+    const float sig = T.sum(s);
+    const float x0 = L[ptri(j + 1) + j];
+    const float s1 = sig - x0 * x0;
+    if (!(s1 > Lim<float>::tiny * sig) || sig == 0.0f) {
+      if (tt == 0) { tau[j] = 0.0f; e[j] = x0; d[j] = L[ptri(j) + j]; }
+      T.sync();
+      continue;
+    }
+    const float alpha = -copysign(sqrt(sig), x0);
+    const float v0 = x0 - alpha;
+    const float t = 2.0f / (v0 * v0 + s1);
+    T.sync();
+    if (tt == 0) { L[ptri(j + 1) + j] = v0; tau[j] = t; e[j] = alpha; d[j] = L[ptri(j) + j]; }
+    for (int r = tt; r < m; r += TS) vv[r] = r == 0 ? v0 : L[ptri(j + 1 + r) + j];
+    T.sync();
+    // p = t * A22 v: row r's own segment for c <= r, its column below for c > r
+    for (int r = tt; r < m; r += TS) {
+      const int R = j + 1 + r;
+      const float *rowR = L + ptri(R) + (j + 1);
+      int ci = ptri(j + 1) + R;              // L[j+1+c][R], c > r
+      float acc = 0.0f;
+      for (int c = 0; c < m; c++) {
+        const float av = c <= r ? rowR[c] : L[ci];
+        acc = fmar(av, vv[c], acc);
+        ci += j + 2 + c;
+      }
+      p[r] = t * acc;
+    }
+    T.sync();
+    float pv = 0.0f;
+    for (int r = tt; r < m; r += TS) pv = fmar(p[r], vv[r], pv);
+    const float beta = 0.5f * t * T.sum(pv);
+    for (int r = tt; r < m; r += TS) w[r] = p[r] - beta * vv[r];
+    T.sync();
+    // A22 -= v w^T + w v^T on the lower triangle
+    for (int r = tt; r < m; r += TS) {
+      float *rowR = L + ptri(j + 1 + r) + (j + 1);
+      const float vr = vv[r], wr = w[r];
+      for (int c = 0; c <= r; c++) rowR[c] = rowR[c] - fmar(vr, w[c], wr * vv[c]);
+    }
+    T.sync();
+  }
+  if (tt == 0) {
+    if (k >= 2) {
+      d[k - 2] = L[ptri(k - 2) + (k - 2)];
+      e[k - 2] = L[ptri(k - 1) + (k - 2)];
+    }
+    d[k - 1] = L[ptri(k - 1) + (k - 1)];
+    e[k - 1] = 0.0f;
+  }
+  T.sync();
+}
+
+// Split pipeline, packed first stage: A from the packed Gram block into the
+// lower triangle, the reduction, then the reflectors (strictly lower part,
+// row-major k x k) with tau on the diagonal to the scratch Q, and d, e;
+// k_eig_vec<.., true> forms Q from them
+template <int NW>
+__global__ void k_eig_trip(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ float tred[NW];
+  const int k = a.k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = NW == 1 ? warp : 0;
+  const int ub = blockIdx.x * wpb + slot;
+  if (ub >= nb) return;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  EigPk P(sm + (size_t)slot * eig_pk_floats(k), k);
+  const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
+  const int tt = T.tt, TS = T.TS;
+  const float *Gin = a.G + (size_t)unit * packed_size(k);
+  // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
+  const float shift = (float)(k - 1) * 1.0f / a.infl;
+  for (int i = 0; i < k; i++)
+    for (int j = tt; j <= i; j += TS) {
+      float v = Gin[tri_idx(j, i, k)];
+      if (i == j) v += shift;
+      P.L[ptri(i) + j] = v;
+    }
+  T.sync();
+  eig_householder_pk(k, P, T);
+  float *Q = sp.Q + (size_t)ub * k * k;
+  for (int i = 0; i < k; i++)
+    for (int j = tt; j < k; j += TS)
+      Q[i * k + j] = j < i ? P.L[ptri(i) + j] : ((j == i && i < k - 2) ? P.tau[i] : 0.0f);
+  float *de = sp.DE + (size_t)ub * 2 * k;
+  for (int t = tt; t < k; t += TS) { de[t] = P.d[t]; de[k + t] = P.e[t]; }
+}
+
 template <int NQ, int NW>
 __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
@@ -525,7 +657,7 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
   if (bad && !a.flag_list) atomicOr(a.status, bad);   // with flagging, the FP64 re-solve takes the unit
 }
 
-template <int NQ, int NW>
+template <int NQ, int NW, bool PK>
 __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
   __shared__ float tred[NW];
@@ -544,6 +676,12 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   float *A = W.A;
   const float *Q = sp.Q + (size_t)ub * k * k;
   for (int t = tt; t < k * k; t += TS) A[(t / k) * ld + (t % k)] = Q[t];
+  if constexpr (PK) {
+    // the scratch holds the reflectors (below the diagonal) and tau (on it): form Q
+    for (int j = tt; j < k; j += TS) W.tau[j] = Q[j * k + j];
+    T.sync();
+    eig_form_q<NQ>(k, W, T);
+  }
   const float *lam = sp.lam + (size_t)ub * k;
   for (int t = tt; t < k; t += TS) W.d[t] = lam[t];
   const float *G = a.G + (size_t)unit * packed_size(k);
@@ -842,9 +980,9 @@ cudaError_t launch_eig64_flagged(cudaStream_t st, const EigArgs &a, int *launche
 
 cudaError_t launch_eig(cudaStream_t st, const EigArgs &a, int *launches);
 
-static int eig_wpb(int k) {
+static int eig_wpb_floats(int floats) {
   // warps per block: the most resident warps per SM for this unit size
-  const size_t per = (size_t)eig_floats_per_warp(k) * sizeof(float);
+  const size_t per = (size_t)floats * sizeof(float);
   const size_t sm_bytes = 227 * 1024;
   int wpb = 1, best = 0;
   for (int c = 1; c <= 8; c++) {
@@ -858,24 +996,42 @@ static int eig_wpb(int k) {
   return wpb;
 }
 
+static int eig_wpb(int k) { return eig_wpb_floats(eig_floats_per_warp(k)); }
+
 // warps per unit of the split kernels, measured on GB300 (206k units per
 // analysis): k <= 64 one warp (two rows per lane; k = 40: 26 ms, against 33
 // with two warps), k > 64 two warps (two rows per thread; k = 100: 273 ms,
 // against 414 with one warp and 308 / 359 with four / eight)
 static int eig_team(int k) { return k <= 64 ? 1 : 2; }
 
-template <int NQ, int NW>
+// the split pipeline's first stage on the packed lower triangle, Q formed in
+// k_eig_vec (above k = 48), or on the full matrix, forming Q: measured on
+// GB300 (206k units per analysis, eigensolve ms full -> packed): k = 40
+// 25.8 -> 26.6, k = 64 57.2 -> 53.8; C4 (824k units) k = 100 1057 -> 974
+static bool eig_packed(int k) { return k > 48; }
+
+template <int NQ, int NW, bool kPackedTri>
 static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart,
                                   int ucount, int *launches) {
+  // first stage: the packed reduction (kPackedTri) or the full-matrix
+  // reduction + Q; its own warps per block from its shared memory
   const int wpb = NW == 1 ? eig_wpb(a.k) : 1;
   const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
   const int threads = NW == 1 ? 32 * wpb : 32 * NW;
+  const int wpt = !kPackedTri ? wpb : (NW == 1 ? eig_wpb_floats(eig_pk_floats(a.k)) : 1);
+  const size_t smt = !kPackedTri ? smem : (size_t)wpt * eig_pk_floats(a.k) * sizeof(float);
+  const int tht = NW == 1 ? 32 * wpt : 32 * NW;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_eig_tri<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-      cudaSuccess)
+  if (kPackedTri) {
+    if ((e = cudaFuncSetAttribute(k_eig_trip<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt)) !=
+        cudaSuccess)
+      return e;
+  } else if ((e = cudaFuncSetAttribute(k_eig_tri<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem)) != cudaSuccess) {
     return e;
-  if ((e = cudaFuncSetAttribute(k_eig_vec<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-      cudaSuccess)
+  }
+  if ((e = cudaFuncSetAttribute(k_eig_vec<NQ, NW, kPackedTri>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem)) != cudaSuccess)
     return e;
   const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
   if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
@@ -883,9 +1039,10 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
   const int uend = ustart + ucount;
   for (int u0 = ustart; u0 < uend; u0 += batch) {
     const int nb = uend - u0 < batch ? uend - u0 : batch;
-    k_eig_tri<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    if (kPackedTri) k_eig_trip<NW><<<(nb + wpt - 1) / wpt, tht, smt, st>>>(a, sp, wpt, u0, nb);
+    else k_eig_tri<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
-    k_eig_vec<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
     (*launches) += 3;
     if (a.flag_list) {
       k_eig_flag<<<(nb + 7) / 8, 256, 0, st>>>(a, sp, u0, nb);
@@ -906,8 +1063,12 @@ cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &
                              int *launches) {
   if (ucount <= 0) return cudaSuccess;
   const int k = a.k, nw = eig_team(k);
-  if (nw == 1) return launch_split_t<2, 1>(st, a, sp, batch, ustart, ucount, launches);   // k <= 64
-  return launch_split_t<2, 2>(st, a, sp, batch, ustart, ucount, launches);   // k <= 128
+  if (nw == 1) {   // k <= 64
+    return eig_packed(k) ? launch_split_t<2, 1, true>(st, a, sp, batch, ustart, ucount, launches)
+                         : launch_split_t<2, 1, false>(st, a, sp, batch, ustart, ucount, launches);
+  }
+  return eig_packed(k) ? launch_split_t<2, 2, true>(st, a, sp, batch, ustart, ucount, launches)   // k <= 128
+                       : launch_split_t<2, 2, false>(st, a, sp, batch, ustart, ucount, launches);
 }
 
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
