@@ -252,22 +252,32 @@ __global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps
                                                   unsigned char *rec, int *status) {
   __shared__ Window W;
   __shared__ int wsc[WT / 32];
+  __shared__ int qpos[2 * WT];   // in-cap window positions not yet written, in window order
   const int tile = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const TilePar tp = tps[tile];
   build_window(W, tp, geom, obs.cell_start);
   const int c0 = tile_off[tile];
   const int cap = (tile_off[tile + 1] - c0) * KC;
   unsigned char *rec0 = rec + (size_t)c0 * cb;
-  int base = 0;
+  // the in-cap observations are queued in window order and written WT at a
+  // time by the whole block (about a third of a window is in the cap)
+  auto write = [&](int q, int p) {
+    if (q < cap) {
+      const float4 A = obs.A[p];
+      put_record(rec0, cb, k, kp, kr, q, make_float4(A.x, A.y, A.z, __frcp_rn(A.w)), obs.B[p],
+                 obs.hx + (size_t)p * kp);
+    } else {
+      atomicOr(status, 16);
+    }
+  };
+  int base = 0, pend = 0;
   for (int jb = 0; jb < W.total; jb += WT) {
     const int j = jb + tid;
     int p = 0;
-    float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
     bool ok = false;
     if (j < W.total) {
       p = window_pos(W, j);
-      A = obs.A[p];
-      ok = in_cap(tp, A);
+      ok = in_cap(tp, obs.A[p]);
     }
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     if (lane == 0) wsc[wid] = __popc(m);
@@ -277,16 +287,20 @@ __global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps
       before += w < wid ? wsc[w] : 0;
       cnt += wsc[w];
     }
-    const int q = base + before + __popc(m & ((1u << lane) - 1u));
-    if (ok) {
-      if (q < cap)
-        put_record(rec0, cb, k, kp, kr, q, make_float4(A.x, A.y, A.z, __frcp_rn(A.w)), obs.B[p],
-                   obs.hx + (size_t)p * kp);
-      else atomicOr(status, 16);
-    }
-    base += cnt;
+    if (ok) qpos[pend + before + __popc(m & ((1u << lane) - 1u))] = p;
+    pend += cnt;
     __syncthreads();
+    if (pend >= WT) {
+      write(base + tid, qpos[tid]);
+      base += WT;
+      pend -= WT;
+      __syncthreads();
+      if (tid < pend) qpos[tid] = qpos[WT + tid];
+      __syncthreads();
+    }
   }
+  if (tid < pend) write(base + tid, qpos[tid]);
+  base += pend;
   const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int q = base + tid; q < cap; q += WT) put_record(rec0, cb, k, kp, kr, q, z, z, nullptr);
   if (tid == 0 && (base > cap || cap - base >= KC)) atomicOr(status, 16);   // count and fill disagree
