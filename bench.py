@@ -89,8 +89,8 @@ class Clocks:
 
     def __init__(self, gpu):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/lgpu_clocks.csv"
+        # the raw samples (the JSON line carries their summary)
+        self.path = os.environ.get("LGPU_CLOCKS_CSV", "/tmp/lgpu_clocks.csv")
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -262,7 +262,7 @@ def gpu_arm(args, dist):
     cand = float(np.sum(diag["obscount"], dtype=np.float64))
     k, ns, ncol = prob.k, prob.ns, prob.ncol
     units = tims[-1]["units"]
-    # algorithmic work per launch (see DESIGN.md): the Gram kernel does one
+    # algorithmic work per launch: the Gram kernel does one
     # multiply-add per packed feature (k(k+3)/2 of them: upper triangle of G
     # and the right-hand side) per kept (column, observation) pair; the
     # eigensolve ~9k^3 + transform 4k^3 per unit; the update reads the
@@ -310,7 +310,7 @@ def gpu_arm(args, dist):
     variant = {1: "plain", 2: "batched_tc"}.get(tims[-1]["variant"], "?")
     plain = None
     if variant != "plain" and not args.no_plain:
-        # the plain per-column FP32 path on the same inputs (spec comparison)
+        # the plain per-column FP32 path on the same inputs (the headline ratio's denominator)
         s.set_variant("plain")
         for _ in range(2):
             s.run()

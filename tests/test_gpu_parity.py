@@ -23,7 +23,7 @@ from helpers import compare, gpu_run, oracle_for, workload_cfg
 
 pytestmark = pytest.mark.gpu
 
-PERT_TOL = 1e-5          # plain FP32 path (spec bar)
+PERT_TOL = 1e-5          # plain FP32 path
 PERT_TOL_TC = 2e-5       # batched tensor-core path: TF32 x3 split, FP32 tensor-core accumulation
 MEAN_TOL = 1e-5
 INC_TOL = 2e-3
