@@ -57,3 +57,28 @@ def test_missing_library_fails_loudly(tmp_path):
     from letkf_gb300 import LgpuError, lib
     with pytest.raises(LgpuError):
         lib(str(tmp_path / "nope.so"))
+
+
+def test_no_device_fails_loudly_and_null_handles_are_rejected():
+    """Without a GPU the library refuses to start (there is no CPU path), and
+    every setter rejects a null handle with LGPU_ERR_ARG."""
+    from letkf_gb300 import _build
+    path = _build.lgpu_lib_path()
+    if not os.path.exists(path):
+        _build.build_lgpu()
+    lib = ctypes.CDLL(path)
+    H = ctypes.c_void_p
+    lib.lgpu_set_precision.argtypes = [H, ctypes.c_int, ctypes.c_float]
+    lib.lgpu_set_variant.argtypes = [H, ctypes.c_int]
+    lib.lgpu_solver_run.argtypes = [H]
+    lib.lgpu_create.argtypes = [ctypes.c_int, ctypes.POINTER(H)]
+    lib.lgpu_destroy.argtypes = [H]
+    assert lib.lgpu_set_precision(None, 1, 1e-6) == 1
+    assert lib.lgpu_set_variant(None, 2) == 1
+    assert lib.lgpu_solver_run(None) == 1
+    h = H()
+    rc = lib.lgpu_create(0, ctypes.byref(h))
+    if rc == 0:   # a GPU is present: nothing to check here
+        lib.lgpu_destroy(h)
+        pytest.skip("a CUDA device is present")
+    assert rc == 2 and not h.value   # LGPU_ERR_CUDA, no handle
