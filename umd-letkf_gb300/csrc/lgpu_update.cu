@@ -204,20 +204,29 @@ __global__ void __launch_bounds__(UT) k_update(UpdateArgs a, int tsm_groups, int
 }
 
 // Thread-per-slab form for k a multiple of 4 (k <= KMAX): one CTA per
-// column, thread s owns slab s.  The column's background block (ns x k
-// floats, contiguous) and its group transforms arrive in shared memory by
-// two bulk async copies completing on one mbarrier; the slab's analysis
-// members stay in registers, so the epilogue's member sums run sequentially
-// in member order (the reference's SUM) without shuffles; the analysis block
-// is written back over the background block in shared memory and leaves by
-// one bulk async store.  A copy wait that runs out sets status bit 64.
-template <int KMAX>
-__global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
+// column, TPS threads per slab (1, or 2 for large k, where the k member
+// accumulators of one thread would limit the CTAs per SM by registers).  The
+// column's background block (ns x k floats, contiguous) and its group
+// transforms arrive in shared memory by two bulk async copies completing on
+// one mbarrier; the slab's analysis members stay in registers (with TPS = 2
+// the even thread holds members [0, sp), the odd one [sp, k)).  The
+// epilogue's member sums run sequentially in member order (the reference's
+// SUM): with TPS = 2 the odd thread continues the even thread's partial sum,
+// so the order and the result are those of one thread.  The analysis block is
+// written back over the background block in shared memory and leaves by one
+// bulk async store.  A copy wait that runs out sets status bit 64.
+template <int KMAX, int TPS>
+__global__ void __launch_bounds__(256, TPS) k_update_rows(UpdateArgs a) {
   extern __shared__ __align__(128) float usm[];   // X [ns][k] | T [groups][k][k]
   __shared__ __align__(8) uint64_t bar;
+  constexpr int KH = KMAX / TPS;   // members per thread (a multiple of 4)
   const int col = a.col0 + blockIdx.x;
-  const int k = a.k, ns = a.ns, G = a.groups, kk = k * k, k4 = k >> 2;
-  const int s = threadIdx.x;
+  const int k = a.k, ns = a.ns, G = a.groups, kk = k * k;
+  const int s = threadIdx.x / TPS, half = TPS == 2 ? (threadIdx.x & 1) : 0;
+  const int lane = threadIdx.x & 31;
+  // this thread's members [jb, jb + nj)
+  const int sp = TPS == 2 ? ((k + 7) / 8) * 4 : k;
+  const int jb = half ? sp : 0, nj = half ? k - sp : sp, nj4 = nj >> 2;
   const size_t cbase = (size_t)col * ns * k;
   const int act = a.col2act[col];
   const bool skip = a.mask[col] || act < 0;
@@ -243,31 +252,61 @@ __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
     }
     return;
   }
+  // lanes whose slab exists (both threads of a slab share it)
+  const unsigned amask = __ballot_sync(0xffffffffu, s < ns);
+  // sequential member reduction acc = step(acc, j) over [0, k) from 0: the
+  // even thread's partial is continued by the odd thread, whose total both
+  // receive (step is written as the reference's expression, e.g. acc + x*x)
+  auto msum = [&](auto step) -> float {
+    float acc = 0.0f;
+    if (TPS == 1) {
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if (j < nj) acc = step(acc, j);
+      return acc;
+    }
+    if (half == 0) {
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if (j < nj) acc = step(acc, j);
+    }
+    const float from0 = __shfl_sync(amask, acc, lane & ~1);
+    if (half == 1) {
+      acc = from0;
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if (j < nj) acc = step(acc, j);
+    }
+    return __shfl_sync(amask, acc, lane | 1);
+  };
   const size_t ms = (size_t)col * ns + s;
   if (s < ns) {
-    const float4 *xb4 = reinterpret_cast<const float4 *>(Xs + (size_t)s * k);
-    float4 *out4 = reinterpret_cast<float4 *>(Xs + (size_t)s * k);
+    const float4 *xb4 = reinterpret_cast<const float4 *>(Xs + (size_t)s * k + jb);
+    float4 *out4 = reinterpret_cast<float4 *>(Xs + (size_t)s * k + jb);
     if (skip) {   // src/letkf_solver.F90:207: the block leaves unchanged
-      a.mean_a[ms] = a.mean_b[ms];
-      a.sprd_a[ms] = a.sprd_b[ms];
+      if (half == 0) {
+        a.mean_a[ms] = a.mean_b[ms];
+        a.sprd_a[ms] = a.sprd_b[ms];
+      }
     } else {
       const int g = slab_group(a, a.slab_lev[s], a.cp[col].mld);
       const bool has = g < G && a.nkept[(size_t)act * G + g] > 0;
-      float x[KMAX];
+      float x[KH];
 #pragma unroll
-      for (int j = 0; j < KMAX; j++) x[j] = 0.0f;
+      for (int j = 0; j < KH; j++) x[j] = 0.0f;
       if (has) {
         // x_a = x_b T_g (src/letkf_solver.F90:285-289), members accumulated in i order
-        const float *T = Tsm + (size_t)g * kk;
-        for (int i4 = 0; i4 < k4; i4++) {
-          const float4 xv = xb4[i4];
+        const float *T = Tsm + (size_t)g * kk + jb;
+        const float4 *xr4 = reinterpret_cast<const float4 *>(Xs + (size_t)s * k);
+        for (int i4 = 0; i4 < (k >> 2); i4++) {
+          const float4 xv = xr4[i4];
           const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
 #pragma unroll
           for (int u = 0; u < 4; u++) {
             const float4 *Tr = reinterpret_cast<const float4 *>(T + (size_t)(4 * i4 + u) * k);
 #pragma unroll
-            for (int q = 0; q < KMAX / 4; q++) {
-              if (q < k4) {
+            for (int q = 0; q < KH / 4; q++) {
+              if (q < nj4) {
                 const float4 t = Tr[q];
                 x[4 * q + 0] = __fmaf_rn(xs[u], t.x, x[4 * q + 0]);
                 x[4 * q + 1] = __fmaf_rn(xs[u], t.y, x[4 * q + 1]);
@@ -279,8 +318,8 @@ __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
         }
       } else {
 #pragma unroll
-        for (int q = 0; q < KMAX / 4; q++)
-          if (q < k4) {
+        for (int q = 0; q < KH / 4; q++)
+          if (q < nj4) {
             const float4 v = xb4[q];
             x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
           }
@@ -289,13 +328,13 @@ __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
       const int v = a.slab_var[s];
       const float mb = a.mean_b[ms], sb = a.sprd_b[ms];
       // recenter (:299-303)
-      float m = 0.0f;
 #pragma unroll
-      for (int j = 0; j < KMAX; j++)
-        if (j < k) { x[j] = x[j] + mb; m = m + x[j]; }
+      for (int j = 0; j < KH; j++)
+        if (j < nj) x[j] = x[j] + mb;
+      float m = msum([&](float acc, int j) { return acc + x[j]; });
       m = m / kf;
 #pragma unroll
-      for (int j = 0; j < KMAX; j++) x[j] = x[j] - m;
+      for (int j = 0; j < KH; j++) x[j] = x[j] - m;
       // mean increment clip and bounds (:308-318)
       const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
       {
@@ -305,21 +344,18 @@ __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
         m = r + mb;
       }
       if (a.rtps > 0.0f) {   // (:322-335)
-        float q2 = 0.0f;
-#pragma unroll
-        for (int j = 0; j < KMAX; j++)
-          if (j < k) q2 = q2 + x[j] * x[j];
+        const float q2 = msum([&](float acc, int j) { return acc + x[j] * x[j]; });
         const float sa = sqrtf(q2 / km1);
         if (sa > 0.0f) {
           const float f = a.rtps * (sb - sa) / sa + 1.0f;
 #pragma unroll
-          for (int j = 0; j < KMAX; j++) x[j] = x[j] * f;
+          for (int j = 0; j < KH; j++) x[j] = x[j] * f;
         }
       }
       if (a.rtpp > 0.0f) {   // (:339-344)
 #pragma unroll
-        for (int q = 0; q < KMAX / 4; q++)
-          if (q < k4) {
+        for (int q = 0; q < KH / 4; q++)
+          if (q < nj4) {
             const float4 b = xb4[q];
             x[4 * q + 0] = a.rtpp * b.x + (1.0f - a.rtpp) * x[4 * q + 0];
             x[4 * q + 1] = a.rtpp * b.y + (1.0f - a.rtpp) * x[4 * q + 1];
@@ -329,32 +365,29 @@ __global__ void __launch_bounds__(256) k_update_rows(UpdateArgs a) {
       }
       if (a.mul != 1.0f) {   // (:347-349)
 #pragma unroll
-        for (int j = 0; j < KMAX; j++) x[j] = x[j] * a.mul;
+        for (int j = 0; j < KH; j++) x[j] = x[j] * a.mul;
       }
       {   // member bounds and re-mean (:357-371)
-        float r = 0.0f;
 #pragma unroll
-        for (int j = 0; j < KMAX; j++)
-          if (j < k) {
-            x[j] = fminf(fmaxf(x[j], lb - m), ub - m);
-            r = r + x[j];
-          }
+        for (int j = 0; j < KH; j++)
+          if (j < nj) x[j] = fminf(fmaxf(x[j], lb - m), ub - m);
+        float r = msum([&](float acc, int j) { return acc + x[j]; });
         r = r / kf;
 #pragma unroll
-        for (int j = 0; j < KMAX; j++) x[j] = x[j] - r;
+        for (int j = 0; j < KH; j++) x[j] = x[j] - r;
         m = m + r;
       }
-      float q2 = 0.0f;   // spread (:375-379)
-#pragma unroll
-      for (int j = 0; j < KMAX; j++)
-        if (j < k) q2 = q2 + x[j] * x[j];
+      // spread (:375-379)
+      const float q2 = msum([&](float acc, int j) { return acc + x[j] * x[j]; });
       const float sa = sqrtf(q2 / km1);
 #pragma unroll
-      for (int q = 0; q < KMAX / 4; q++)
-        if (q < k4) out4[q] = make_float4(x[4 * q] + m, x[4 * q + 1] + m, x[4 * q + 2] + m, x[4 * q + 3] + m);
-      a.mean_a[ms] = m;
-      a.sprd_a[ms] = sa;
-      if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
+      for (int q = 0; q < KH / 4; q++)
+        if (q < nj4) out4[q] = make_float4(x[4 * q] + m, x[4 * q + 1] + m, x[4 * q + 2] + m, x[4 * q + 3] + m);
+      if (half == 0) {
+        a.mean_a[ms] = m;
+        a.sprd_a[ms] = sa;
+        if (!isfinite(m) || !isfinite(sa)) atomicOr(a.status, 4);
+      }
     }
   }
   // the analysis block (generic-proxy writes) -> global by the async proxy
@@ -373,20 +406,22 @@ cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   if (a.ncol <= 0 || a.ncols <= 0) return cudaSuccess;
   const size_t rbytes = ((size_t)a.ns * a.k + (size_t)a.groups * a.k * a.k) * sizeof(float);
   if (a.k % 4 == 0 && a.ns <= 256 && rbytes <= 200 * 1024) {
-    const int nt = (a.ns + 31) & ~31;
     const int k = a.k;
-    auto kern = k <= 8    ? k_update_rows<8>
-                : k <= 16 ? k_update_rows<16>
-                : k <= 24 ? k_update_rows<24>
-                : k <= 32 ? k_update_rows<32>
-                : k <= 40 ? k_update_rows<40>
-                : k <= 48 ? k_update_rows<48>
-                : k <= 56 ? k_update_rows<56>
-                : k <= 64 ? k_update_rows<64>
-                : k <= 80 ? k_update_rows<80>
-                : k <= 96 ? k_update_rows<96>
-                : k <= 112 ? k_update_rows<112>
-                           : k_update_rows<128>;
+    // above k = 64 two threads per slab (when the slabs fit one CTA)
+    const int tps = k > 64 && 2 * a.ns <= 256 ? 2 : 1;
+    const int nt = (tps * a.ns + 31) & ~31;
+    auto kern = k <= 8    ? k_update_rows<8, 1>
+                : k <= 16 ? k_update_rows<16, 1>
+                : k <= 24 ? k_update_rows<24, 1>
+                : k <= 32 ? k_update_rows<32, 1>
+                : k <= 40 ? k_update_rows<40, 1>
+                : k <= 48 ? k_update_rows<48, 1>
+                : k <= 56 ? k_update_rows<56, 1>
+                : k <= 64 ? k_update_rows<64, 1>
+                : k <= 80 ? (tps == 2 ? k_update_rows<80, 2> : k_update_rows<80, 1>)
+                : k <= 96 ? (tps == 2 ? k_update_rows<96, 2> : k_update_rows<96, 1>)
+                : k <= 112 ? (tps == 2 ? k_update_rows<112, 2> : k_update_rows<112, 1>)
+                           : (tps == 2 ? k_update_rows<128, 2> : k_update_rows<128, 1>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbytes);
     if (e != cudaSuccess) return e;
     kern<<<a.ncols, nt, rbytes, st>>>(a);
