@@ -1,5 +1,6 @@
-// lgpu_eig.cu -- batched symmetric eigensolve and LETKF transform, one warp
-// per (column, group) unit, FP32.
+// lgpu_eig.cu -- batched symmetric eigensolve and LETKF transform per
+// (column, group) unit: FP32 (the reference's ssyev precision), with an FP64
+// form for the units flagged by the eigenvalue-gap test or for every unit.
 //
 // Replaces src/letkf_core.F90:100-141: with A = G + (k-1)/infl I (G from
 // the Gram stage, upper triangle as ssyev('V','U') reads it),
@@ -17,7 +18,8 @@
 // spread over the team's threads (tt + TS q, two per thread).  The fused
 // kernel evaluates the QL scalar recurrence redundantly on every lane of its
 // warp (shared memory broadcasts) with lane 0 as the only writer; the split
-// pipeline runs it once per unit and replays the logged rotations.
+// pipeline runs it once per unit and replays the logged rotations.  The FP64
+// form (k_eig64) runs the same phases in double on a team of 2 or 4 warps.
 #include "lgpu_internal.cuh"
 #include <algorithm>
 
@@ -433,17 +435,20 @@ __global__ void k_eig(EigArgs a, int wpb) {
 }
 
 // ---------------------------------------------------------------------------
-// Split pipeline (same arithmetic as k_eig, bit-identical results):
-//   k_eig_tri  warp per unit: Householder + Q (to global), d and e
+// Split pipeline (same arithmetic as k_eig, bit-identical results up to
+// k = 48):
+//   k_eig_tri  team per unit: Householder + Q (to global), d and e; above
+//              k = 48 k_eig_trip: the reduction on the packed lower triangle,
+//              reflectors and tau to global
 //   k_eig_ql   thread per unit: the QL recurrence on (d, e) alone, logging
 //              every sweep (start index, rotation count) and rotation (c, s)
-//   k_eig_vec  warp per unit: the logged rotations applied to Q's columns
-//              (V = Q Z), then the spectral functions and T
+//   k_eig_vec  team per unit: (above k = 48) Q formed from the reflectors,
+//              the logged rotations applied to Q's columns (V = Q Z), then
+//              the spectral functions and T
+//   k_eig_flag (FP32_RESOLVE) warp per unit: units for the FP64 re-solve
 // The scalar recurrence, which the fused kernel evaluates redundantly on all
 // 32 lanes, runs once per unit.
 
-// NW = 1: wpb units per CTA, one warp each; NW > 1: one unit per CTA of NW
-// warps (wpb = 1)
 // ---- packed reduction: the symmetric work matrix as its lower triangle,
 // L[i][j] (j <= i) at i(i+1)/2 + j, half the shared memory of the full
 // matrix (twice the units per SM).  Triangular numbers of 32 consecutive rows
@@ -564,6 +569,8 @@ __global__ void k_eig_trip(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   for (int t = tt; t < k; t += TS) { de[t] = P.d[t]; de[k + t] = P.e[t]; }
 }
 
+// NW = 1: wpb units per CTA, one warp each; NW > 1: one unit per CTA of NW
+// warps (wpb = 1)
 template <int NQ, int NW>
 __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
