@@ -44,6 +44,12 @@
 // of each unit.  Every wait is bounded; a wait that runs out sets status bit
 // 16, the MMA thread waits (bounded) for its copies in flight and TMEM is
 // freed.
+//
+// Long tile streams are split into up to 4 accumulation segments, each its
+// own CTA, summed in order by k_gram_segsum.  The producers come in two forms
+// with bit-identical output (with and without a warp-level cull of records
+// out of every column's reach); the first analysis of a configuration times
+// both and keeps the faster.
 #include "lgpu_internal.cuh"
 #include "lgpu_tc.cuh"
 
