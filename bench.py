@@ -352,17 +352,20 @@ def gpu_arm(args, dist):
         refill()
         e2e_step()
     dist.barrier()
-    et, ev = [], []
+    et, ev, etim = [], [], []
     for _ in range(args.steps):
         refill()
         s.flush_l2(256 << 20)
         t0 = time.perf_counter()
         e2e_step()
         et.append(time.perf_counter() - t0)
-        ev.append(s.timings()["variant"])
+        tm = s.timings()
+        ev.append(tm["variant"])
+        etim.append(tm)
     dist.barrier()
     e2e_ms = dist.max(1000.0 * statistics.mean(et))
     e2e_val = dist.world * nact / (e2e_ms / 1000.0)
+    link = link_summary(etim)
     ok = bool(np.all(np.isfinite(outp[1].array)))
     for p in list(pin.values()) + outp:
         p.free()
@@ -373,7 +376,7 @@ def gpu_arm(args, dist):
             "config": workload_config(args, prob, cfg), "clocks": ck, "gpu_launches": launches * args.steps,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": e2e_ms, "step_ms": [round(1000.0 * t, 3) for t in et],
-                    "variant": [{1: "plain", 2: "batched_tc"}.get(v, "?") for v in ev]},
+                    "variant": [{1: "plain", 2: "batched_tc"}.get(v, "?") for v in ev], "link": link},
             "roofline": roof, "stages": stages, "analysis_finite": ok, "variant": variant, "plain_variant": plain}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         rate, n, nth, dt = cpu_rate(prob, cfg)
@@ -383,6 +386,23 @@ def gpu_arm(args, dist):
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def link_summary(tims):
+    """Where the end-to-end step goes, from the library's CUDA events and host
+    clocks (means over the timed steps): observation upload, background
+    upload and analysis download with their rates, the device span of the run
+    (start to the last download) and the host time of the two calls."""
+    m = lambda key: statistics.mean(t[key] for t in tims)
+    up, down = m("h2d_state_ms"), m("d2h_state_ms")
+    ub, db = m("h2d_state_bytes"), m("d2h_state_bytes")
+    return {"h2d_obs_ms": m("h2d_obs_ms"), "h2d_state_ms": up, "d2h_state_ms": down,
+            "h2d_state_gbs": ub / (up * 1e-3) / 1e9 if up > 0 else None,
+            "d2h_state_gbs": db / (down * 1e-3) / 1e9 if down > 0 else None,
+            "device_span_ms": m("span_ms"), "device_compute_ms": m("total_ms"),
+            "host_set_obs_ms": m("host_obs_ms"), "host_run_ms": m("host_run_ms"),
+            "span_ms_per_step": [round(t["span_ms"], 2) for t in tims],
+            "host_run_ms_per_step": [round(t["host_run_ms"], 2) for t in tims]}
 
 
 def learned_arm(args, dist):

@@ -146,6 +146,15 @@ typedef struct lgpu_timings {
   int precision;     /* eigensolve precision mode of the run (LGPU_PREC_*) */
   int fp64_units;    /* units whose eigensolve ran in FP64 (re-solved, or all under LGPU_PREC_FP64) */
   float fp64_ms;     /* part of eig_ms spent in the FP64 eigensolve */
+  /* host link and host time (the end-to-end view of a run) */
+  float h2d_obs_ms;      /* the last lgpu_set_obs: observation upload (CUDA events around its copies) */
+  float host_obs_ms;     /* the last lgpu_set_obs: host wall time of the call */
+  float h2d_state_ms;    /* bound state: background upload, on the copy stream (0 otherwise) */
+  float d2h_state_ms;    /* bound state: analysis download, summed over the column chunks (0 otherwise) */
+  float span_ms;         /* run start to the end of the last analysis download (total_ms without a bound state) */
+  float host_run_ms;     /* host wall time of lgpu_solver_run */
+  long long h2d_state_bytes;  /* bound state: bytes uploaded by the run */
+  long long d2h_state_bytes;  /* bound state: bytes downloaded by the run */
 } lgpu_timings;
 
 /* Gram variants.  PLAIN: one CTA per (column, group), FP32 on the CUDA
@@ -257,19 +266,20 @@ int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, i
 /* lgpu_get_obslist for callers that cannot allocate device memory.
  * No counterpart in the reference (the reference builds its lists in Fortran
  * automatic arrays on the host stack).  It is meant for hosts that drive the
- * analysis from inside their own memory manager -- a model's pre-allocated
- * device pool, a cycling driver that forbids allocation after start-up, code
- * running while a stream is being captured -- where the lazily grown list
- * buffer of lgpu_get_obslist is not allowed.  Same arguments, results and
- * canonical order as lgpu_get_obslist.  It calls no cudaMalloc/cudaFree: its
- * scratch is one fixed __device__ array of 4 * LGPU_NOALLOC_MAX_LIST + 64
- * ints (about 4 MB) that every device loading the library holds until the
- * process exits.  Handles whose observation table is larger than
- * LGPU_NOALLOC_MAX_LIST are rejected with LGPU_ERR_CAPACITY.  All calls
- * share that array (the counters are cleared on each call): calls that
- * overlap on the GPU race and must be serialised by the caller.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture. */
+ * analysis from inside their own memory manager -- a model that takes its
+ * device memory as one pool at start-up and hands it out itself, or a
+ * cycling driver whose memory footprint is fixed once it starts -- where the
+ * lazily grown list buffer of lgpu_get_obslist is not allowed.  Same
+ * arguments, results and canonical order as lgpu_get_obslist.  It calls no
+ * cudaMalloc/cudaFree: its scratch is one fixed __device__ array of
+ * 4 * LGPU_NOALLOC_MAX_LIST + 64 ints (about 4 MB) that every device loading
+ * the library holds until the process exits.  Handles whose observation
+ * table is larger than LGPU_NOALLOC_MAX_LIST are rejected with
+ * LGPU_ERR_CAPACITY.  All calls share that array, which keeps the last
+ * call's contents (each call clears its counters and flags first): calls
+ * that overlap on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks up the array's address; make it before any
+ * stream capture. */
 #define LGPU_NOALLOC_MAX_LIST 262144
 int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
                              int *n, int *ncand);

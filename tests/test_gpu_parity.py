@@ -91,7 +91,8 @@ def test_fast_weight_path_bounds(solver):
     assert np.max(np.abs(rf.astype(np.float64) - re)) <= 1e-6
 
 
-LIST_CASES = [("simple3d", None), ("ocean", None), ("c1", None), ("c2small", 150), ("c3small", 150)]
+LIST_CASES = [("simple3d", None), ("ocean", None), ("c1", None), ("c2small", 150), ("c3small", 150),
+              ("c2ocean", 150)]
 
 
 @pytest.mark.parametrize("variant", ["plain", "batched"])
@@ -178,7 +179,7 @@ def test_simple3d_variants(variant, gram):
 
 
 @pytest.mark.parametrize("gram", ["plain", "batched"])
-@pytest.mark.parametrize("name", ["ocean", "c1", "c2small", "c3small"])
+@pytest.mark.parametrize("name", ["ocean", "c1", "c2small", "c3small", "c2ocean"])
 def test_analysis_parity(name, gram):
     cfg = workload_cfg(name)
     prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
@@ -186,6 +187,55 @@ def test_analysis_parity(name, gram):
     rng = np.random.default_rng(2)
     cols = np.sort(rng.choice(active, size=min(600, len(active)), replace=False))
     _check_analysis(prob, cfg["localization"], cfg["solver"], cols, label=name, variant=gram)
+
+
+@pytest.mark.parametrize("gram", ["plain", "batched"])
+def test_ocean_time_and_surface_ids(gram):
+    """loc_ocean with temporal localisation and both surface-id lists
+    (src/subclass.letkf_localizer/letkf_loc_ocean.F90:467-499), through the
+    GPU: SSH swath obs (id 3, platform 2) are surface obs and never enter the
+    sub-mixed-layer group; SST swath obs (id 4, platform 2) fail the id list
+    and are used in both groups with the profile radius; the weights carry
+    the temporal factor (lower than without tloc, same keep decisions as the
+    oracle, which the list tests check bit-exactly)."""
+    from dataclasses import replace
+    cfg = workload_cfg("c2ocean")
+    prob = workload(cfg["gen"]["workload"], **{k: v for k, v in cfg["gen"].items() if k != "workload"})
+    assert np.any(prob.otime > 0.5) and np.any(prob.otime < -0.5)
+    loc_nt = dict(cfg["localization"], tloc_prof=-1.0, tloc_sat=-1.0)
+    res = gpu_run(prob, cfg["localization"], cfg["solver"], keep_open=True, variant=gram)
+    res_nt = gpu_run(prob, loc_nt, cfg["solver"], keep_open=True, variant=gram)
+    s, s_nt = res["solver"], res_nt["solver"]
+    try:
+        assert s.maxgroups == 2
+        # columns next to swath observations of both kinds
+        cols = []
+        for kind in (3, 4):
+            for i in np.nonzero(prob.oobsid == kind)[0][::97][:12]:
+                d = (prob.lat - prob.olat[i]) ** 2 + ((prob.lon - prob.olon[i] + 180) % 360 - 180) ** 2
+                c = int(np.argmin(d + 1e9 * prob.mask))
+                cols.append(c)
+        sst_below, lower = 0, 0
+        for c in cols:
+            for g in (0, 1):
+                gi, gr, _ = s.obslist(c, g)
+                ni, nr, _ = s_nt.obslist(c, g)
+                kinds = prob.oobsid[gi]
+                if g == 1:
+                    assert not np.any(kinds == 3), c      # surface obs never below the mixed layer
+                    sst_below += int(np.sum(kinds == 4))
+                # the temporal factor only lowers weights (and can drop
+                # entries); 1e-6 covers the fast/exact evaluations near the
+                # keep threshold
+                assert set(gi.tolist()) <= set(ni.tolist())
+                wt = dict(zip(ni.tolist(), nr.tolist()))
+                for i, r in zip(gi.tolist(), gr.tolist()):
+                    assert r <= wt[i] + 1e-6
+                    lower += r < 0.999 * wt[i]
+        assert sst_below > 0 and lower > 0
+    finally:
+        s.close()
+        s_nt.close()
 
 
 @pytest.mark.parametrize("k", [12, 20])

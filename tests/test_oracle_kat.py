@@ -229,6 +229,50 @@ def test_scalar_kalman_update_at_observation():
     o.close()
 
 
+def test_ocean_temporal_gc_and_surface_ids():
+    """loc_ocean (src/subclass.letkf_localizer/letkf_loc_ocean.F90:451-499):
+    an observation is a surface observation only when its id is in sat_obs AND
+    its platform in sat_plats; a surface observation takes the satellite radius
+    and tloc_sat and is dropped below the mixed layer, any other the profile
+    radius and tloc_prof.  The temporal factor is letkf_loc_gc(time, tloc),
+    which takes |time|: the sign of the time does not matter.  The weight is
+    the REAL product of the two REAL factors."""
+    from dataclasses import replace
+    from oracle import oracle as O
+    prob = workload("simple3d")
+    col = int(np.argmin((prob.lat - 41.0) ** 2 + (prob.lon - 221.0) ** 2))
+    loc = {"class": "loc_ocean", "hzloc_prof": [(0.0, 500e3), (90.0, 50e3)], "hzloc_sat": [(0.0, 300e3)],
+           "tloc_prof": 2.0, "tloc_sat": 1.5, "sat_obs": [3], "sat_plats": [2],
+           "vtloc_surf": {"type": "bkg_t", "bkg_t_delta": 0.2, "bkg_t_var": prob.vars[0]["name"]}}
+    dist = O.dist(O.unitvec(prob.lat[col], prob.lon[col]), O.unitvec(prob.olat[0], prob.olon[0]))
+    Lp = O.lib().or_interp_get(O.interp([(0.0, 500e3), (90.0, 50e3)]), float(prob.lat[col]))
+    Ls = O.lib().or_interp_get(O.interp([(0.0, 300e3)]), float(prob.lat[col]))
+    seen = {}
+    for obsid, platid, surf in [(1, 1, False), (3, 2, True), (4, 2, False), (3, 1, False)]:
+        for t in (1.25, -1.25, 0.0):
+            ids = prob.oobsid.copy()
+            plats = prob.oplatid.copy()
+            times = prob.otime.copy()
+            ids[0], plats[0], times[0] = obsid, platid, t
+            o = _oracle(replace(prob, oobsid=ids, oplatid=plats, otime=times), loc)
+            assert o.maxgroups == 2
+            idx, rr, _ = o.obslist(col, 0)
+            rh = np.float32(O.gc(dist, Ls if surf else Lp))
+            rt = np.float32(O.gc(t, 1.5 if surf else 2.0))
+            assert 0 in list(idx), (obsid, platid, t)
+            got = rr[list(idx).index(0)]
+            assert got == np.float32(rh * rt), (obsid, platid, t, got, rh * rt)
+            seen[(obsid, platid, abs(t))] = seen.get((obsid, platid, abs(t)), got)
+            assert seen[(obsid, platid, abs(t))] == got      # t and -t give the same weight
+            # below the mixed layer: surface observations are dropped
+            idx1 = list(o.obslist(col, 1)[0])
+            assert (0 in idx1) == (not surf), (obsid, platid, t)
+            o.close()
+    # the temporal factor is active: a nonzero time lowers the weight
+    assert seen[(1, 1, 1.25)] < seen[(1, 1, 0.0)]
+    assert seen[(3, 2, 1.25)] < seen[(3, 2, 0.0)]
+
+
 def test_bounds_semantics():
     """bounds_check: clipped means stay inside ana_bounds and inside
     bkg_mean +- ana_inc_max; members stay inside the bounds."""

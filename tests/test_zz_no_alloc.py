@@ -1,6 +1,6 @@
 """lgpu_get_obslist_noalloc: the local-observation-list query for callers that
-cannot allocate device memory (hosts running the analysis inside their own
-memory manager or while a stream is being captured).  Its scratch is a fixed
+cannot allocate device memory (hosts that hand out their own pre-allocated
+device pool, or whose memory footprint is fixed once they start).  Its scratch is a fixed
 __device__ array inside the library; these tests call it through the C ABI
 and check it against lgpu_get_obslist (same lists, same order, same weights,
 same candidate counts) on consecutive calls, and that tables larger than the
@@ -61,7 +61,7 @@ def test_noalloc_rejects_tables_over_capacity():
     from letkf_gb300 import LgpuError
     prob = workload("simple3d")
     rng = np.random.default_rng(11)
-    n = 262145                         # one more than the fixed list capacity
+    n = 262144 + 4096                  # above the fixed list capacity with a margin
     hx = rng.standard_normal((n, prob.k)).astype(np.float32)
     hx -= hx.mean(1, keepdims=True)
     big = replace(prob, olat=np.degrees(np.arcsin(rng.uniform(-1, 1, n))).astype(np.float32),
@@ -73,6 +73,7 @@ def test_noalloc_rejects_tables_over_capacity():
     res = gpu_run(big, cfg["localization"], {}, keep_open=True, variant="batched")
     s = res["solver"]
     try:
+        assert s.nobs > 262144, "the table must exceed the fixed capacity for the refusal to be tested"
         with pytest.raises(LgpuError) as e:
             s.obslist_noalloc(0, 0)
         assert e.value.code == 7 and "exceed" in e.value.msg

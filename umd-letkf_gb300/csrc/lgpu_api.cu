@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <array>
 #include <cctype>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -19,7 +20,7 @@ size_t gram_smem_bytes(int k);
 cudaError_t noalloc_scratch(int device, int **out);
 int noalloc_max_list();
 cudaError_t launch_obslist_noalloc(cudaStream_t st, int gid, const ColPar *cp_col, const DevLoc &loc, ObsSorted obs,
-                                   const IndexGeom *geom, int nmax, int *scratch);
+                                   const IndexGeom *geom, int nobs, int *scratch);
 cudaError_t launch_hx_stats(cudaStream_t st, int nobs, int k, float *hx, float *hx_mean, const int *qc, int *flag,
                             int *pos, int *total);
 cudaError_t launch_compact(cudaStream_t st, int nobs, int k, const int *flag, const int *pos, const float *const *src_f,
@@ -80,6 +81,10 @@ struct lgpu_handle {
   cudaEvent_t ev_cull[3] = {};     // batched Gram: timing of its two producer forms
   // per column chunk: eigensolve start, update start, update end, FP64 eigensolve start
   cudaEvent_t ev_chunk[kOutChunks][4] = {};
+  cudaEvent_t ev_obs[2] = {};        // lgpu_set_obs: observation upload
+  cudaEvent_t ev_up[2] = {};         // bound state: background upload (copy stream)
+  cudaEvent_t ev_down[kOutChunks][2] = {};   // bound state: analysis download per chunk (copy stream)
+  float obs_h2d_ms = 0.0f, obs_host_ms = 0.0f;
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
   std::string err;
   bool solver_ok = false, loc_ok = false, grid_ok = false, state_ok = false, obs_ok = false, ran = false;
@@ -251,6 +256,13 @@ int lgpu_create(int device, lgpu_handle **out) {
   for (auto &row : h->ev_chunk)
     for (auto &ev : row)
       if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_obs)
+    if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_up)
+    if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &row : h->ev_down)
+    for (auto &ev : row)
+      if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   build_geom(h->geom, h->ncell);
   if (h->buf[B_GEOM].ensure(sizeof(IndexGeom)) != cudaSuccess ||
       cudaMemcpy(h->buf[B_GEOM].p, &h->geom, sizeof(IndexGeom), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -273,6 +285,10 @@ void lgpu_destroy(lgpu_handle *h) {
   for (auto &ev : h->ev_tune) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_cull) if (ev) cudaEventDestroy(ev);
   for (auto &row : h->ev_chunk)
+    for (auto &ev : row) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : h->ev_obs) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : h->ev_up) if (ev) cudaEventDestroy(ev);
+  for (auto &row : h->ev_down)
     for (auto &ev : row) if (ev) cudaEventDestroy(ev);
   if (h->st) cudaStreamDestroy(h->st);
   if (h->cst) cudaStreamDestroy(h->cst);
@@ -531,21 +547,26 @@ int lgpu_set_obs(lgpu_handle *h, int nobs, const lgpu_obs *o, const float *hx, c
   for (int i = 0; i < nobs; i++)
     if (!(o->err[i] > 0.0f)) return fail(h, LGPU_ERR_ARG, "set_obs: observation error must be > 0 at obs " + std::to_string(i));
   CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const auto t_host = std::chrono::steady_clock::now();
   const size_t n = std::max(nobs, 1), k = h->k;
   int bi[8] = {B_OLAT, B_OLON, B_OZ, B_OTIME, B_OVAL, B_OERR, B_OOBSID, B_OPLATID};
   const void *src[8] = {o ? o->lat : nullptr, o ? o->lon : nullptr, o ? o->zdim : nullptr, o ? o->time : nullptr,
                         o ? o->val : nullptr, o ? o->err : nullptr, o ? o->obsid : nullptr, o ? o->platid : nullptr};
-  for (int q = 0; q < 8; q++) {
-    CK(h->buf[bi[q]].ensure(n * 4), "alloc obs");
-    if (nobs > 0) CK(cudaMemcpyAsync(h->buf[bi[q]].p, src[q], (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D obs");
-  }
+  for (int q = 0; q < 8; q++) CK(h->buf[bi[q]].ensure(n * 4), "alloc obs");
   CK(h->buf[B_HX].ensure(n * k * 4), "alloc hx");
   CK(h->buf[B_HXM].ensure(n * 4), "alloc hx_mean");
+  CK(cudaEventRecord(h->ev_obs[0], h->st), "event");
+  for (int q = 0; q < 8; q++) {
+    if (nobs > 0) CK(cudaMemcpyAsync(h->buf[bi[q]].p, src[q], (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D obs");
+  }
   if (nobs > 0) {
     CK(cudaMemcpyAsync(h->buf[B_HX].p, hx, (size_t)nobs * k * 4, cudaMemcpyHostToDevice, h->st), "H2D hx");
     CK(cudaMemcpyAsync(h->buf[B_HXM].p, hx_mean, (size_t)nobs * 4, cudaMemcpyHostToDevice, h->st), "H2D hxm");
   }
+  CK(cudaEventRecord(h->ev_obs[1], h->st), "event");
   CK(cudaStreamSynchronize(h->st), "set_obs sync");
+  CK(cudaEventElapsedTime(&h->obs_h2d_ms, h->ev_obs[0], h->ev_obs[1]), "timing");
+  h->obs_host_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t_host).count();
   h->nobs = nobs;
   h->obs_ok = true;
   h->ran = false;
@@ -731,11 +752,13 @@ static int prepare_run(lgpu_handle *h, ObsSorted &os, int &launches) {
     // search, Gram and eigensolve stages (the update waits for it)
     const size_t nx = (size_t)h->ncol * ns * k, nm = (size_t)h->ncol * ns;
     CK(cudaStreamWaitEvent(h->cst, h->ev[0], 0), "stream wait");
+    CK(cudaEventRecord(h->ev_up[0], h->cst), "event");
     CK(cudaMemcpyAsync(h->buf[B_MEANB].p, h->bound_mean, nm * 4, cudaMemcpyHostToDevice, h->cst), "H2D mean");
     CK(cudaMemcpyAsync(h->buf[B_SPRDB].p, h->bound_sprd, nm * 4, cudaMemcpyHostToDevice, h->cst), "H2D sprd");
     CK(cudaEventRecord(h->ev_in[0], h->cst), "event");
     CK(cudaMemcpyAsync(h->buf[B_BKG].p, h->bound_state, nx * 4, cudaMemcpyHostToDevice, h->cst), "H2D state");
     CK(cudaEventRecord(h->ev_in[1], h->cst), "event");
+    CK(cudaEventRecord(h->ev_up[1], h->cst), "event");
   }
   // ---- observation index (kd_init counterpart) ----
   CK(launch_obs_index(st, h->nobs, k, kp, h->buf[B_OLAT].as<float>(), h->buf[B_OLON].as<float>(),
@@ -966,10 +989,21 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
     return LGPU_OK;
 }
 
+static int solver_run(lgpu_handle *h);
+
 // letkf_solver_run (src/letkf_solver.F90:150-389)
 int lgpu_solver_run(lgpu_handle *h) {
   if (!h) return LGPU_ERR_ARG;
-  if (h->variant == LGPU_VARIANT_LEARNED) return learned_run(h);
+  const auto t0 = std::chrono::steady_clock::now();
+  h->tim = lgpu_timings{};
+  const int rc = h->variant == LGPU_VARIANT_LEARNED ? learned_run(h) : solver_run(h);
+  h->tim.h2d_obs_ms = h->obs_h2d_ms;
+  h->tim.host_obs_ms = h->obs_host_ms;
+  h->tim.host_run_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+static int solver_run(lgpu_handle *h) {
   ObsSorted os;
   int launches = 0;
   int rc0 = prepare_run(h, os, launches);
@@ -1093,6 +1127,7 @@ int lgpu_solver_run(lgpu_handle *h) {
     nrec = c + 1;
     if (bound) {
       CK(cudaStreamWaitEvent(h->cst, h->ev_chunk[c][2], 0), "stream wait");
+      CK(cudaEventRecord(h->ev_down[c][0], h->cst), "event");
       const size_t xo = (size_t)c0 * ns * k, xn = (size_t)(c1 - c0) * ns * k;
       const size_t mo = (size_t)c0 * ns, mn = (size_t)(c1 - c0) * ns;
       CK(cudaMemcpyAsync(h->bound_state + xo, h->buf[B_ANA].as<float>() + xo, xn * 4, cudaMemcpyDeviceToHost, h->cst),
@@ -1101,6 +1136,7 @@ int lgpu_solver_run(lgpu_handle *h) {
          "D2H mean");
       CK(cudaMemcpyAsync(h->bound_sprd + mo, h->buf[B_SPRDA].as<float>() + mo, mn * 4, cudaMemcpyDeviceToHost, h->cst),
          "D2H sprd");
+      CK(cudaEventRecord(h->ev_down[c][1], h->cst), "event");
     }
   }
   CK(cudaEventRecord(h->ev[5], st), "event");
@@ -1139,6 +1175,19 @@ int lgpu_solver_run(lgpu_handle *h) {
   h->tim.precision = h->prec;
   h->tim.fp64_units = fp64 ? h->nunits : std::min(nflag, ea.flag_cap);   // with a fused-kernel fallback: 0
   h->tim.fp64_ms = fp64_ms;
+  h->tim.span_ms = h->tim.total_ms;
+  if (bound) {
+    const long long nx = (long long)h->ncol * ns * k, nm = (long long)h->ncol * ns;
+    CK(cudaEventElapsedTime(&h->tim.h2d_state_ms, h->ev_up[0], h->ev_up[1]), "timing");
+    for (int c = 0; c < nrec; c++) {
+      float td = 0.0f;
+      CK(cudaEventElapsedTime(&td, h->ev_down[c][0], h->ev_down[c][1]), "timing");
+      h->tim.d2h_state_ms += td;
+    }
+    if (nrec > 0) CK(cudaEventElapsedTime(&h->tim.span_ms, h->ev[0], h->ev_down[nrec - 1][1]), "timing");
+    h->tim.h2d_state_bytes = 4 * (nx + 2 * nm);
+    h->tim.d2h_state_bytes = 4 * (nx + 2 * nm);
+  }
   const int status = stat4[0];
   h->ran = true;
   if (status & 1) return fail(h, LGPU_ERR_EIG, "eigensolver did not converge for at least one unit");
@@ -1261,7 +1310,7 @@ int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float 
   os.idx = h->buf[B_SIDX].as<int>();
   os.cell_start = h->buf[B_CSTART].as<int>();
   CK(launch_obslist_noalloc(h->st, group, h->buf[B_CP].as<ColPar>() + ij, h->loc, os, h->buf[B_GEOM].as<IndexGeom>(),
-                            nmax, scr),
+                            h->nobs, scr),
      "obslist kernel (no alloc)");
   int cnt[2] = {0, 0};
   CK(cudaMemcpyAsync(cnt, scr, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st), "D2H counts");
@@ -2011,6 +2060,7 @@ static int learned_run(lgpu_handle *h) {
   h->tim.precision = h->prec;
   h->tim.fp64_units = h->prec == LGPU_PREC_FP64 ? nex + ngate : std::min(nflag, 2 * std::max(1, h->nunits));
   h->tim.fp64_ms = 0.0f;   // inside exact_ms of the learned statistics
+  h->tim.span_ms = h->tim.total_ms;
   L->st.coarse = ncoarse;
   L->st.judged = nj;
   L->st.fallback = (int)L->fine_miss.size();

@@ -339,47 +339,16 @@ __global__ void __launch_bounds__(GT) k_gram(GramArgs a) {
   }
 }
 
-// Verification: one column/group list, in cell order; the host sorts it.
+// Verification: one column/group list, in arrival order; the host sorts it.
+// The slot counter is counts[2] (counts[0] counts every kept entry, also
+// those beyond cap).
 __global__ void k_obslist(int gid, const ColPar *cpp, DevLoc loc, ObsSorted obs, const IndexGeom *geom, int cap,
                           int *out_idx, float *out_r, int *counts) {
   const ColPar cp = *cpp;
-  const float hq = fminf(cp.rmax / 12742000.0f, 1.5707963f);
-  const float sh = sinf(hq);
-  const float c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
-  for (int b = cp.b0; b <= cp.b1; b++) {
-    int nl = geom->nlon[b], off = geom->off[b];
-    int runs[2][2] = {{0, 0}, {0, 0}};
-    bool whole = cp.dlon >= 180.0f;
-    int clo = 0, chi = nl - 1;
-    if (!whole) {
-      clo = (int)floorf((cp.lonn - cp.dlon) * (float)nl / 360.0f);
-      chi = (int)floorf((cp.lonn + cp.dlon) * (float)nl / 360.0f);
-      if (chi - clo + 1 >= nl) whole = true;
-    }
-    if (whole) { runs[0][0] = obs.cell_start[off]; runs[0][1] = obs.cell_start[off + nl]; }
-    else if (clo < 0) {
-      runs[0][0] = obs.cell_start[off + clo + nl]; runs[0][1] = obs.cell_start[off + nl];
-      runs[1][0] = obs.cell_start[off]; runs[1][1] = obs.cell_start[off + chi + 1];
-    } else if (chi >= nl) {
-      runs[0][0] = obs.cell_start[off + clo]; runs[0][1] = obs.cell_start[off + nl];
-      runs[1][0] = obs.cell_start[off]; runs[1][1] = obs.cell_start[off + chi - nl + 1];
-    } else { runs[0][0] = obs.cell_start[off + clo]; runs[0][1] = obs.cell_start[off + chi + 1]; }
-    for (int q = 0; q < 2; q++)
-      for (int p = runs[q][0] + threadIdx.x; p < runs[q][1]; p += blockDim.x) {
-        const float4 A = obs.A[p];
-        const float c2 = chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
-        if (c2 > c2max) continue;
-        const float d = dist_from_chord2(c2);
-        if (d > cp.rmax) continue;
-        atomicAdd(&counts[1], 1);
-        const float4 B = obs.B[p];
-        const float r = localize(loc, cp, gid, d, B.y, B.z, B.w);
-        if (r > kKeep) {
-          int s = atomicAdd(&counts[0], 1);
-          if (s < cap) { out_idx[s] = obs.idx[p]; out_r[s] = r; }
-        }
-      }
-  }
+  list_search(gid, cp, loc, obs, geom, counts, [&](int p, float r) {
+    const int s = atomicAdd(&counts[2], 1);
+    if (s < cap) { out_idx[s] = obs.idx[p]; out_r[s] = r; }
+  });
 }
 
 __global__ void k_debug_metric(int n, const float *lat1, const float *lon1, const float *lat2, const float *lon2,
@@ -466,7 +435,7 @@ cudaError_t preload_gram(void) {
 cudaError_t launch_obslist(cudaStream_t st, int col, int gid, int group_slot, const ColPar *cp_col, const DevLoc &loc,
                            ObsSorted obs, const IndexGeom *geom, int cap, int *d_idx, float *d_r, int *d_counts) {
   (void)col; (void)group_slot;
-  cudaError_t e = cudaMemsetAsync(d_counts, 0, 2 * sizeof(int), st);
+  cudaError_t e = cudaMemsetAsync(d_counts, 0, 3 * sizeof(int), st);
   if (e != cudaSuccess) return e;
   k_obslist<<<1, 256, 0, st>>>(gid, cp_col, loc, obs, geom, cap, d_idx, d_r, d_counts);
   return cudaGetLastError();

@@ -351,6 +351,55 @@ struct ObsSorted {
   int *cell_start; // [ncell + 1]
 };
 
+// The local-observation search of one (column, group), the threads of a
+// block striding over the column's index window (kd_search_radius and the
+// keep filter of src/letkf_solver.F90:211-263): every observation within the
+// search radius adds one to counts[1]; each one whose localisation weight
+// passes r > 1e-4 adds one to counts[0] and is handed to emit(p, r), p its
+// position in the sorted table.  Entries arrive in no fixed order.  Used by
+// the verification queries (lgpu_get_obslist and its no-allocation form).
+template <class Emit>
+__device__ __forceinline__ void list_search(int gid, const ColPar &cp, const DevLoc &loc, const ObsSorted &obs,
+                                            const IndexGeom *geom, int *counts, Emit emit) {
+  const float hq = fminf(cp.rmax / 12742000.0f, 1.5707963f);
+  const float sh = sinf(hq);
+  const float c2max = 4.0f * sh * sh * 1.0001f + 1e-12f;
+  for (int b = cp.b0; b <= cp.b1; b++) {
+    const int nl = geom->nlon[b], off = geom->off[b];
+    int runs[2][2] = {{0, 0}, {0, 0}};
+    bool whole = cp.dlon >= 180.0f;
+    int clo = 0, chi = nl - 1;
+    if (!whole) {
+      clo = (int)floorf((cp.lonn - cp.dlon) * (float)nl / 360.0f);
+      chi = (int)floorf((cp.lonn + cp.dlon) * (float)nl / 360.0f);
+      if (chi - clo + 1 >= nl) whole = true;
+    }
+    if (whole) { runs[0][0] = obs.cell_start[off]; runs[0][1] = obs.cell_start[off + nl]; }
+    else if (clo < 0) {
+      runs[0][0] = obs.cell_start[off + clo + nl]; runs[0][1] = obs.cell_start[off + nl];
+      runs[1][0] = obs.cell_start[off]; runs[1][1] = obs.cell_start[off + chi + 1];
+    } else if (chi >= nl) {
+      runs[0][0] = obs.cell_start[off + clo]; runs[0][1] = obs.cell_start[off + nl];
+      runs[1][0] = obs.cell_start[off]; runs[1][1] = obs.cell_start[off + chi - nl + 1];
+    } else { runs[0][0] = obs.cell_start[off + clo]; runs[0][1] = obs.cell_start[off + chi + 1]; }
+    for (int q = 0; q < 2; q++)
+      for (int p = runs[q][0] + threadIdx.x; p < runs[q][1]; p += blockDim.x) {
+        const float4 A = obs.A[p];
+        const float c2 = chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z);
+        if (c2 > c2max) continue;
+        const float d = dist_from_chord2(c2);
+        if (d > cp.rmax) continue;
+        atomicAdd(&counts[1], 1);
+        const float4 B = obs.B[p];
+        const float r = localize(loc, cp, gid, d, B.y, B.z, B.w);
+        if (r > kKeep) {
+          atomicAdd(&counts[0], 1);
+          emit(p, r);
+        }
+      }
+  }
+}
+
 cudaError_t launch_obs_index(cudaStream_t st, int nobs, int k, int kp, const float *lat, const float *lon,
                              const float *zdim, const float *time, const float *val, const float *err,
                              const int *obsid, const int *platid, const float *hx, const float *hx_mean,

@@ -78,7 +78,10 @@ class Timings(ctypes.Structure):
                 ("launches", ctypes.c_int), ("units", ctypes.c_int), ("kept_pairs", ctypes.c_longlong),
                 ("variant", ctypes.c_int), ("tiles_ms", ctypes.c_float), ("mma_chunks", ctypes.c_longlong),
                 ("mma_n", ctypes.c_int), ("precision", ctypes.c_int), ("fp64_units", ctypes.c_int),
-                ("fp64_ms", ctypes.c_float)]
+                ("fp64_ms", ctypes.c_float), ("h2d_obs_ms", ctypes.c_float), ("host_obs_ms", ctypes.c_float),
+                ("h2d_state_ms", ctypes.c_float), ("d2h_state_ms", ctypes.c_float), ("span_ms", ctypes.c_float),
+                ("host_run_ms", ctypes.c_float), ("h2d_state_bytes", ctypes.c_longlong),
+                ("d2h_state_bytes", ctypes.c_longlong)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -21,6 +21,11 @@ sections a reference YAML configuration would carry for them.
             obs, loc_novrt 500 km -> 50 km)
   ocean     test/ocean/vtloc-style (k=10, T/S/u/v, five synthetic obs,
             loc_ocean with the mixed-layer split)
+  c2ocean   c2small's grid and observations under loc_ocean with temporal
+            localisation (tloc_prof 2 h, tloc_sat 1.5 h; observation times
+            of both signs) and both surface-id lists set (sat_obs = [3],
+            sat_plats = [2]: the SSH swath obs are surface obs, the SST swath
+            obs of the same platform are not), mixed-layer split on T
   c2small / c1small / c3small / c4small  reduced grids with the same
             generators for fast tests
 """
@@ -39,6 +44,16 @@ WORKLOADS = {
     "c2small": dict(gen=dict(workload="c2", nx=144, ny=72, nz=10, n_profiles=300, n_swaths=10, swath_len=800),
                     localization=C2_LOC, solver={}),
     "c2mid": dict(gen=dict(workload="c2", nx=360, ny=180, nz=10), localization=C2_LOC, solver={}),
+    "c2ocean": dict(gen=dict(workload="c2", nx=144, ny=72, nz=10, n_profiles=300, n_swaths=10, swath_len=800),
+                    localization={"class": "loc_ocean",
+                                  "hzloc_prof": C2_LOC["hzloc"],
+                                  "hzloc_sat": {"type": "linearinterp_lat",
+                                                "value": [{"lat": 0.0, "radius": 500.0e3},
+                                                          {"lat": 90.0, "radius": 100.0e3}]},
+                                  "tloc_prof": 2.0, "tloc_sat": 1.5,
+                                  "sat_obs": [3], "sat_plats": [2],
+                                  "vtloc_surf": {"type": "bkg_t", "bkg_t_delta": 0.2, "bkg_t_var": "T"}},
+                    solver={}),
     "c3": dict(gen=dict(workload="c3"),
                localization={"class": "loc_novrt",
                              "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 60.0e3}]}},
