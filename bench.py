@@ -421,7 +421,7 @@ def learned_arm(args, dist):
     t_setup = time.perf_counter()
     prob = synth.generate(w, **gen)
     nobs = prob.nobs
-    prob = synth.observe(prob, seed=2000, n_obs=nobs)
+    prob = synth.observe(prob, seed=2000, n_obs=nobs, **{k: cy[k] for k in ("n_clusters", "cluster_sigma_m") if k in cy})
     dev = dist.local if dist.world > 1 else 0
     s = Solver(dev)
     s.solver_init(cfg["solver"])
@@ -429,13 +429,15 @@ def learned_arm(args, dist):
     s.set_problem(prob)
     s.learn_init(prob.nx, prob.ny, **cfg["learn"])
 
+    obs_kw = {k: cy[k] for k in ("n_clusters", "cluster_sigma_m") if k in cy}
+
     def next_cycle(p, ana, c):
         x, m, sp = ana
         p.state[...] = x - m[:, :, None]
         p.mean[...] = m
         p.sprd[...] = sp
         synth.forecast(p, u=cy["u"], kappa=cy["kappa"], dt=cy["dt"])
-        return synth.observe(p, seed=2000 + c, n_obs=nobs)
+        return synth.observe(p, seed=2000 + c, n_obs=nobs, **obs_kw)
 
     for c in range(cy["train"]):
         if c:

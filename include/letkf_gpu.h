@@ -354,8 +354,73 @@ int lgpu_learn_set_params(lgpu_handle *h, const float *params, long long n);
 int lgpu_mlp_debug(int device, int din, int hidden, int dout, int rows, const float *params, const float *x,
                    const float *t, float *loss, float *grad, float *y_simt, float *y_tc);
 
+/* ---- Diagnostics files (save_diag) ----------------------------------------
+ * letkf_solver_final's diag.solver.nc (src/letkf_solver.F90:397-527) from
+ * the last run: dimensions time (1), lat (ny), lon (nx), loc_group; lat and
+ * lon from lat_nom / lon_nom; col_maxhz, col_obscount [time][lat][lon] and
+ * lg_obscount, lg_obsloc [time][loc_group][lat][lon] with the reference's
+ * attributes.  The grid must be nx * ny columns, column ij = i + nx * j.
+ * Masked columns hold 0, as the reference's initialised arrays do. */
+int lgpu_write_diag(lgpu_handle *h, const char *path, int nx, int ny, const float *lat_nom, const float *lon_nom);
+/* loc_ocean with vtloc_surf (src/subclass.letkf_localizer/letkf_loc_ocean.F90
+ * :353-358): the level count of each column's surface localisation group
+ * (calc_mldlvl_bkgt, :408-427) in the last run; 0 on masked columns. */
+int lgpu_get_loc_diag(lgpu_handle *h, float *surf_lvl);
+/* loc_ocean_final's diag.loc_ocean.nc (letkf_loc_ocean.F90:249-322):
+ * vtloc_surf_lvl and vtloc_surf_depth = vert_nom(vtloc_surf_lvl) per column
+ * (vert_nom: the nz nominal level depths, vtgrids(1)%vert_nom). */
+int lgpu_write_loc_diag(lgpu_handle *h, const char *path, int nx, int ny, const float *lat_nom,
+                        const float *lon_nom, int nz, const float *vert_nom);
+
+/* ---- File formats (host code, no device needed) ---------------------------
+ * NetCDF classic files, read and written by the library's own implementation
+ * of the published format: versions CDF-1 (classic), CDF-2 (64-bit offset)
+ * and CDF-5 (64-bit data) are read, any numeric type converted; files are
+ * written as CDF-1 (CDF-2 above 2 GiB), big-endian, data laid out as the
+ * netCDF library lays it out.  NetCDF-4 (HDF5) files are refused with
+ * LGPU_ERR_UNSUPPORTED.  These calls take no handle: their error message is
+ * lgpu_io_last_error() (per thread).  Array arguments are in file order
+ * (slowest dimension first: a Fortran (nx, ny, nz) variable is [nz][ny][nx]). */
+const char *lgpu_io_last_error(void);
+/* parse_ens_filename (src/letkf_state_helper.F90:445-510): "#ENSn#" becomes
+ * the member number zero-padded to n digits (ensmem >= 0), "mean" (-1
+ * background, -2 analysis) or "sprd" (-3, -4); "#TYPE#" becomes "ana" (members,
+ * -2, -4) or "bkg" (-1, -3). */
+int lgpu_ens_filename(const char *pattern, int ensmem, char *out, int cap);
+int lgpu_nc_dim_len(const char *path, const char *dim, long long *len);
+int lgpu_nc_var_info(const char *path, const char *var, int *ndims, long long *dims, int maxdims);
+int lgpu_nc_read_float(const char *path, const char *var, float *out, long long n);
+int lgpu_nc_read_int(const char *path, const char *var, int *out, long long n);
+/* obsio_nc_read_obs (src/subclass.letkf_obsio/letkf_obsio_nc.F90:150-237):
+ * dimension "obs"; variables obid, plat, lat, lon, depth, hr, val, err, qc.
+ * With lat == NULL only *nobs is set (to size the arrays). */
+int lgpu_read_obs_nc(const char *path, int cap, int *nobs, float *lat, float *lon, float *zdim, float *time,
+                     float *val, float *err, int *obsid, int *platid, int *qc);
+/* obsio_nc_read_hx (letkf_obsio_nc.F90:244-306): one member's H(x) ("hx"),
+ * or "val" + "inc" when read_inc is set; the "obs" dimension must equal nobs. */
+int lgpu_read_hx_nc(const char *path, int nobs, int read_inc, float *hx);
+/* stateio_nc_read_state (src/subclass.letkf_stateio/letkf_stateio_nc.F90:
+ * 196-245): variable `var` holding nx * ny * nz values ([nz][ny][nx]). */
+int lgpu_read_state_nc(const char *path, const char *var, int nx, int ny, int nz, float *out);
+/* stateio_nc_write_state (letkf_stateio_nc.F90:252-370) as a classic file
+ * (the reference writes NetCDF-4 with deflate): dimensions time (record),
+ * lon, lat and each vertical grid; coordinate variables lon, lat and the
+ * vertical grids with the reference's attributes; state variable v as
+ * [time][vt][lat][lon] on vertical grid var_vt[v], one record. */
+int lgpu_write_state_nc(const char *path, int nx, int ny, const float *lon_nom, const float *lat_nom, int nvt,
+                        const char *const *vt_names, const int *vt_len, const float *const *vt_nom, int nvar,
+                        const char *const *names, const int *var_vt, const float *const *vals);
+/* The two diagnostics files from host arrays (layouts as lgpu_write_diag /
+ * lgpu_write_loc_diag). */
+int lgpu_write_diag_nc(const char *path, int nx, int ny, int groups, const float *lat_nom, const float *lon_nom,
+                       const float *maxhz, const float *obscount, const float *lg_obscount, const float *lg_obsloc);
+int lgpu_write_loc_diag_nc(const char *path, int nx, int ny, const float *lat_nom, const float *lon_nom,
+                           const float *surf_lvl, const float *surf_depth);
+
 /* Page-locked host memory for callers that stream state in and out every
- * analysis (host<->device copies run at full link speed from it). */
+ * analysis (host<->device copies run at full link speed from it): an
+ * anonymous mapping registered with CUDA (cudaMallocHost where that fails),
+ * zero-filled.  Release it with lgpu_host_free. */
 int lgpu_host_alloc(size_t bytes, void **ptr);
 int lgpu_host_free(void *ptr);
 

@@ -7,10 +7,9 @@ Bars (written here, checked per variable and level):
     1e-6 (products), keep/drop decisions exact;
   - analysis perturbations and analysis mean: relative L2 <= 1e-5 per slab
     against the FP32 oracle (reference arithmetic) and the FP64 oracle,
-    for slabs whose perturbation norm is not negligible (plain FP32 path);
-    the batched tensor-core path (TF32 three-term split, FP32 accumulation
-    in TMEM) is held to 2e-5 on perturbations (measured <= 1.02e-5) and the
-    same 1e-5 on the mean;
+    for slabs whose perturbation norm is not negligible, both Gram forms
+    (the batched tensor-core form accumulates in segments of at most 64
+    chunks of 16 observations, summed in FP64);
   - mean increment: reported; relative L2 <= 2e-3 per slab (FP32 Gram
     accumulation error of ill-conditioned columns, shared by the
     reference's own FP32 path).
@@ -24,7 +23,7 @@ from helpers import compare, gpu_run, oracle_for, workload_cfg
 pytestmark = pytest.mark.gpu
 
 PERT_TOL = 1e-5          # plain FP32 path
-PERT_TOL_TC = 2e-5       # batched tensor-core path: TF32 x3 split, FP32 tensor-core accumulation
+PERT_TOL_TC = PERT_TOL   # batched tensor-core path: TF32 x3 split, segmented FP32 tensor-core accumulation
 MEAN_TOL = 1e-5
 INC_TOL = 2e-3
 

@@ -5,6 +5,11 @@
 #include <array>
 #include <cctype>
 #include <chrono>
+#include <cstdint>
+#include <mutex>
+#include <unordered_map>
+#include <utility>
+#include <sys/mman.h>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -61,13 +66,15 @@ enum {
   B_CP, B_G, B_T, B_NKEPT, B_DMAXHZ, B_DOBSC, B_DLGC, B_DLGL, B_STATUS, B_LEVDEPTH,
   B_LIST_IDX, B_LIST_R, B_LIST_CNT, B_FLUSH, B_TILECOLS, B_TILEPAR, B_TILEN, B_TILEOFF, B_TILEREC, B_EIGSCR, B_WCACHE,
   B_RAW0, B_RAW1, B_RAW2, B_RAW3, B_RAW4, B_RAW5, B_RAW6, B_RAW7, B_RAWQC, B_RAWHX, B_RAWHXM, B_FLAG, B_POS,
-  B_PTRS, B_TOTAL, B_GPART, B_GCNT, B_FLAGLIST,
+  B_PTRS, B_TOTAL, B_GPART, B_GCNT, B_FLAGLIST, B_TCWORK, B_TCSEG,
   B_COUNT_ALL
 };
 
 }  // namespace
 
 constexpr int kOutChunks = 8;   // column chunks of eigensolve / update / analysis download of a bound state
+constexpr int kSegChunks = 256;   // batched Gram: chunks of 16 observations per CTA at most
+constexpr int kDrainChunks = 64;  // batched Gram: chunks per tensor-core accumulation (drained to a partial block)
 
 struct LearnState;   // learned form (below)
 
@@ -106,7 +113,10 @@ struct lgpu_handle {
   bool used_tc = false;
   int mma_n = 0;
   int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
-  int gram_nseg = 1;     // accumulation segments of the last batched Gram
+  int gram_nseg = 1;     // most accumulation segments of a tile in the last batched Gram
+  std::vector<int> h_tile_off;       // tile stream offsets of the last batched Gram (read back)
+  std::vector<TcWork> h_tc_work;     // its accumulation segments
+  std::vector<TcSegTile> h_tc_seg;   // its tiles with more than one segment
   int tc_cull = -1;      // batched Gram producers: 1 with the warp-level cull, 0 without, -1 not yet measured
   float tc_tune_ms = 0.0f;   // time of the producer form the tuning run discarded (left out of AUTO's comparison)
   bool preloaded = false;    // the Gram kernels are loaded (before the first timed trial)
@@ -885,10 +895,14 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
   CK(launch_tile_count(st, ts.ntiles, (*ts.par).as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os,
                        (*ts.n).as<int>(), (*ts.off).as<int>(), &launches),
      "tile count");
-  int nchunk_total = 0;
-  CK(cudaMemcpyAsync(&nchunk_total, (*ts.off).as<int>() + ts.ntiles, sizeof(int), cudaMemcpyDeviceToHost, st),
-     "D2H stream size");
+  // the stream offsets size the record buffer and split each tile's stream
+  // into accumulation segments
+  h->h_tile_off.assign((size_t)ts.ntiles + 1, 0);
+  CK(cudaMemcpyAsync(h->h_tile_off.data(), (*ts.off).as<int>(), sizeof(int) * ((size_t)ts.ntiles + 1),
+                     cudaMemcpyDeviceToHost, st),
+     "D2H stream offsets");
   CK(cudaStreamSynchronize(st), "stream size sync");
+  const int nchunk_total = h->h_tile_off[ts.ntiles];
   CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
   CK(launch_tile_fill(st, ts.ntiles, (*ts.par).as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
                       (*ts.off).as<int>(), h->buf[B_TILEREC].as<unsigned char>(),
@@ -935,33 +949,91 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
       }
     }
   }
-  // accumulation segments: long tile streams are split into up to 4 ranges
-  // accumulated by separate CTAs (the tensor core's FP32 accumulation error
-  // grows with the stream length), partial Grams summed in order afterwards;
-  // the partials take at most 24 GB
+  // accumulation segments: each tile's stream is split into ranges of at most
+  // kSegChunks chunks, each its own CTA (which drains its tensor-core
+  // accumulator into its result rows every 64 chunks: the FP32 accumulation
+  // error grows with the MMAs summed into one accumulator); the partial
+  // Grams of a tile's segments are summed in order afterwards; the partials
+  // take at most 24 GB (longer segments otherwise)
   ta.units = (long long)h->nact * G;
-  ta.nseg = 1;
+  ta.nf = packed_size(k);
   ta.Gpart = nullptr;
   ta.cnt = nullptr;
-  {
-    const double avg = (double)nchunk_total / std::max(1, ts.ntiles);
-    int nseg = avg >= 512.0 ? 4 : (avg >= 256.0 ? 2 : 1);
-    const double per = (double)ta.units * ta.nf * 4.0;
-    while (nseg > 1 && (nseg - 1) * per > 24.0 * (1ull << 30)) nseg--;
-    if (nseg > 1) {
-      const size_t gp = (size_t)(nseg - 1) * (size_t)ta.units * ta.nf * 4;
-      const size_t cn = (size_t)nseg * (size_t)ta.units * 3 * 4;
-      if ((h->buf[B_GPART].cap >= gp || h->buf[B_GPART].ensure(gp) == cudaSuccess) &&
-          (h->buf[B_GCNT].cap >= cn || h->buf[B_GCNT].ensure(cn) == cudaSuccess)) {
-        ta.nseg = nseg;
-        ta.Gpart = h->buf[B_GPART].as<float>();
-        ta.cnt = h->buf[B_GCNT].as<float>();
-      } else {
-        cudaGetLastError();   // clear the failed allocation: one segment
+  auto plan = [&](int seg_chunks, int drain) {
+    h->h_tc_work.clear();
+    h->h_tc_seg.clear();
+    int cblk = 0, blk = 0, most = 1;
+    for (int t = 0; t < ts.ntiles; t++) {
+      const int n = h->h_tile_off[t + 1] - h->h_tile_off[t];
+      const int ns_t = std::max(1, (n + seg_chunks - 1) / seg_chunks);
+      const int len = (n + ns_t - 1) / ns_t;
+      const bool multi = ns_t > 1 || n > drain;   // more than one accumulator for the tile
+      most = std::max(most, ns_t);
+      int nb = 0;
+      for (int q = 0; q < ns_t; q++) {
+        TcWork w{};
+        w.tile = t;
+        w.seg = q;
+        w.cs = std::min(n, q * len);
+        w.ce = std::min(n, (q + 1) * len);
+        w.cblk = multi ? cblk + q : -1;
+        w.blk0 = multi ? blk + nb : -1;
+        nb += std::max(1, (w.ce - w.cs + drain - 1) / drain);
+        h->h_tc_work.push_back(w);
+      }
+      if (multi) {
+        h->h_tc_seg.push_back(TcSegTile{t, ns_t, cblk, nb, blk, 0, 0, 0});
+        cblk += ns_t;
+        blk += nb;
       }
     }
+    return std::make_pair(std::make_pair(cblk, blk), most);
+  };
+  const double block_bytes = (double)G * 128.0 * ta.nf * 4.0;
+  // over 24 GB of partial blocks: longer drain intervals first, then longer
+  // segments (one block each); a segment as long as the longest tile stream
+  // leaves one accumulator per tile and no blocks
+  int longest = 0;
+  for (int t = 0; t < ts.ntiles; t++) longest = std::max(longest, h->h_tile_off[t + 1] - h->h_tile_off[t]);
+  int drain = kDrainChunks, seg_chunks = kSegChunks;
+  auto pl = plan(seg_chunks, drain);
+  while (pl.first.second > 0 && pl.first.second * block_bytes > 24.0 * (1ull << 30)) {
+    if (drain < seg_chunks) {
+      drain *= 2;
+    } else if (seg_chunks < longest) {
+      seg_chunks *= 2;
+      drain = seg_chunks;
+    } else {
+      break;   // unreachable: one segment per tile with drain >= its length has no blocks
+    }
+    pl = plan(seg_chunks, drain);
   }
-  h->gram_nseg = ta.nseg;
+  if (pl.first.second > 0) {
+    const size_t gp = (size_t)pl.first.second * (size_t)block_bytes;
+    const size_t cn = (size_t)pl.first.first * G * 128 * 3 * 4;
+    if ((h->buf[B_GPART].cap >= gp || h->buf[B_GPART].ensure(gp) == cudaSuccess) &&
+        (h->buf[B_GCNT].cap >= cn || h->buf[B_GCNT].ensure(cn) == cudaSuccess)) {
+      ta.Gpart = h->buf[B_GPART].as<float>();
+      ta.cnt = h->buf[B_GCNT].as<float>();
+    } else {
+      cudaGetLastError();   // clear the failed allocation: one accumulator per tile
+      drain = 1 << 30;
+      pl = plan(1 << 30, drain);
+    }
+  }
+  ta.drain = drain;
+  CK(h->buf[B_TCWORK].ensure(sizeof(TcWork) * std::max<size_t>(1, h->h_tc_work.size())), "alloc segments");
+  CK(h->buf[B_TCSEG].ensure(sizeof(TcSegTile) * std::max<size_t>(1, h->h_tc_seg.size())), "alloc segments");
+  CK(cudaMemcpyAsync(h->buf[B_TCWORK].p, h->h_tc_work.data(), sizeof(TcWork) * h->h_tc_work.size(),
+                     cudaMemcpyHostToDevice, st), "H2D segments");
+  if (!h->h_tc_seg.empty())
+    CK(cudaMemcpyAsync(h->buf[B_TCSEG].p, h->h_tc_seg.data(), sizeof(TcSegTile) * h->h_tc_seg.size(),
+                       cudaMemcpyHostToDevice, st), "H2D segments");
+  ta.work = h->buf[B_TCWORK].as<TcWork>();
+  ta.nwork = (int)h->h_tc_work.size();
+  ta.segtiles = h->buf[B_TCSEG].as<TcSegTile>();
+  ta.nsegtiles = (int)h->h_tc_seg.size();
+  h->gram_nseg = pl.second;
   if (h->tc_cull < 0) {
     // the first batched Gram of a configuration runs both producer forms,
     // timed, and keeps the faster; their outputs are bit-identical, and every
@@ -1225,6 +1297,60 @@ int lgpu_get_diag(lgpu_handle *h, float *maxhz, float *obscount, float *lg_obsco
   return LGPU_OK;
 }
 
+// loc_ocean's per-column diagnostic (src/subclass.letkf_localizer/
+// letkf_loc_ocean.F90:353-358): the level count of the surface localisation
+// group (calc_mldlvl_bkgt) of each column of the last run, 0 on masked
+// columns (the reference's solver loop skips them before localizer%groups)
+int lgpu_get_loc_diag(lgpu_handle *h, float *surf_lvl) {
+  if (!h || !surf_lvl) return LGPU_ERR_ARG;
+  if (!h->ran) return fail(h, LGPU_ERR_ORDER, "get_loc_diag before a successful solver_run");
+  if (h->loc.cls != LOC_OCEAN || h->loc.vtloc_surf != 1)
+    return fail(h, LGPU_ERR_CONFIG, "get_loc_diag: the localizer is not loc_ocean with vtloc_surf");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  std::vector<ColPar> cp((size_t)h->ncol);
+  CK(cudaMemcpyAsync(cp.data(), h->buf[B_CP].p, sizeof(ColPar) * (size_t)h->ncol, cudaMemcpyDeviceToHost, h->st),
+     "D2H column parameters");
+  CK(cudaStreamSynchronize(h->st), "get_loc_diag");
+  for (int c = 0; c < h->ncol; c++) surf_lvl[c] = h->h_col2act[c] >= 0 ? (float)cp[(size_t)c].mld : 0.0f;
+  return LGPU_OK;
+}
+
+// letkf_solver_final's diagnostics file (src/letkf_solver.F90:397-527) for a
+// grid of nx * ny columns (column ij = i + nx * j)
+int lgpu_write_diag(lgpu_handle *h, const char *path, int nx, int ny, const float *lat_nom, const float *lon_nom) {
+  if (!h) return LGPU_ERR_ARG;
+  if (!h->ran) return fail(h, LGPU_ERR_ORDER, "write_diag before a successful solver_run");
+  if (nx <= 0 || ny <= 0 || (long long)nx * ny != h->ncol)
+    return fail(h, LGPU_ERR_ARG, "write_diag: nx * ny must equal the column count");
+  const size_t n = (size_t)h->ncol, G = (size_t)h->loc.groups;
+  std::vector<float> maxhz(n), obsc(n), lgc(n * G), lgl(n * G);
+  int rc = lgpu_get_diag(h, maxhz.data(), obsc.data(), lgc.data(), lgl.data());
+  if (rc != LGPU_OK) return rc;
+  rc = lgpu_write_diag_nc(path, nx, ny, (int)G, lat_nom, lon_nom, maxhz.data(), obsc.data(), lgc.data(), lgl.data());
+  if (rc != LGPU_OK) return fail(h, rc, lgpu_io_last_error());
+  return LGPU_OK;
+}
+
+// loc_ocean_final's diagnostics file (letkf_loc_ocean.F90:249-322):
+// vtloc_surf_lvl and its depth vert_nom(vtloc_surf_lvl) per column
+int lgpu_write_loc_diag(lgpu_handle *h, const char *path, int nx, int ny, const float *lat_nom, const float *lon_nom,
+                        int nz, const float *vert_nom) {
+  if (!h) return LGPU_ERR_ARG;
+  if (nx <= 0 || ny <= 0 || (long long)nx * ny != h->ncol || nz <= 0 || !vert_nom)
+    return fail(h, LGPU_ERR_ARG, "write_loc_diag: nx * ny must equal the column count and vert_nom hold nz depths");
+  std::vector<float> lvl((size_t)h->ncol), dep((size_t)h->ncol, 0.0f);
+  int rc = lgpu_get_loc_diag(h, lvl.data());
+  if (rc != LGPU_OK) return rc;
+  for (int c = 0; c < h->ncol; c++) {
+    const int l = (int)lvl[(size_t)c];
+    if (l > nz) return fail(h, LGPU_ERR_ARG, "write_loc_diag: vert_nom has fewer levels than the surface group");
+    dep[(size_t)c] = l >= 1 ? vert_nom[l - 1] : 0.0f;
+  }
+  rc = lgpu_write_loc_diag_nc(path, nx, ny, lat_nom, lon_nom, lvl.data(), dep.data());
+  if (rc != LGPU_OK) return fail(h, rc, lgpu_io_last_error());
+  return LGPU_OK;
+}
+
 int lgpu_get_timings(const lgpu_handle *h, lgpu_timings *t) {
   if (!h || !t) return LGPU_ERR_ARG;
   *t = h->tim;
@@ -1361,16 +1487,58 @@ int lgpu_debug_transform(lgpu_handle *h, int nunits, int k, const float *gram, f
   return LGPU_OK;
 }
 
+// Page-locked host memory: an anonymous mapping (2 MiB aligned, transparent
+// huge pages requested), touched and registered with CUDA.  Measured on the
+// GB300 host: such buffers keep the full host link rate (about 210 GB/s to
+// the device, 190 GB/s back) in a process that starts after other processes
+// have used and released most of the host memory, where buffers from
+// cudaMallocHost fell to 25-100 GB/s.  cudaMallocHost is the fallback.
+namespace {
+std::mutex g_host_mu;
+std::unordered_map<void *, std::pair<void *, size_t>> g_host_maps;   // user pointer -> (mapping, length)
+}  // namespace
+
 int lgpu_host_alloc(size_t bytes, void **ptr) {
   if (!ptr) return LGPU_ERR_ARG;
   *ptr = nullptr;
+  const size_t al = (size_t)2 << 20;
+  const size_t n = (std::max<size_t>(bytes, 16) + al - 1) / al * al;
+  void *raw = mmap(nullptr, n + al, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (raw != MAP_FAILED) {
+    void *p = reinterpret_cast<void *>((reinterpret_cast<uintptr_t>(raw) + al - 1) & ~(uintptr_t)(al - 1));
+    madvise(p, n, MADV_HUGEPAGE);   // advisory; ignored where unsupported
+    std::memset(p, 0, n);
+    if (cudaHostRegister(p, n, cudaHostRegisterDefault) == cudaSuccess) {
+      std::lock_guard<std::mutex> lock(g_host_mu);
+      g_host_maps[p] = std::make_pair(raw, n + al);
+      *ptr = p;
+      return LGPU_OK;
+    }
+    cudaGetLastError();
+    munmap(raw, n + al);
+  }
   cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 16);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? LGPU_ERR_NOMEM : LGPU_ERR_CUDA;
   return LGPU_OK;
 }
 
 int lgpu_host_free(void *ptr) {
-  if (ptr && cudaFreeHost(ptr) != cudaSuccess) return LGPU_ERR_CUDA;
+  if (!ptr) return LGPU_OK;
+  std::pair<void *, size_t> m(nullptr, 0);
+  {
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    auto it = g_host_maps.find(ptr);
+    if (it != g_host_maps.end()) {
+      m = it->second;
+      g_host_maps.erase(it);
+    }
+  }
+  if (m.first) {
+    const cudaError_t e = cudaHostUnregister(ptr);
+    munmap(m.first, m.second);
+    return e == cudaSuccess ? LGPU_OK : LGPU_ERR_CUDA;
+  }
+  if (cudaFreeHost(ptr) != cudaSuccess) return LGPU_ERR_CUDA;
   return LGPU_OK;
 }
 

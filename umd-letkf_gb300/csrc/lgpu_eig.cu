@@ -593,6 +593,198 @@ __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   for (int t = T.tt; t < k; t += T.TS) { de[t] = W.d[t]; de[k + t] = W.e[t]; }
 }
 
+// The first stage for k <= 48 with the work matrix in registers: one warp
+// per unit, lane l holds rows l and l + 32 of A (K = k rounded up to 8
+// columns, zero beyond k).  Step j of the Householder reduction: the lane
+// owning row j publishes x = A[j][j+1:] (= A[j+1:][j]) as the reflector
+// row VH[j] in shared memory (zeros outside j+1..k-1); p = t A v and the
+// rank-two update A -= v w^T + w v^T run on every lane's rows over the full
+// row width (columns and rows outside the trailing block meet zeros in v and
+// w and are left exactly unchanged), in column groups of four skipped while
+// they lie left of the block.  The dot products run over the columns in
+// ascending order as the shared-memory form does.  Q = H_0 ... H_{k-3} is
+// then formed with lane l holding columns l and l + 32 in the same registers
+// (reflectors applied from the last to the first).  Output as k_eig_tri: Q
+// row-major and (d, e) to the scratch.
+constexpr int RWPB = 4;   // warps (units) per block
+
+template <int K>
+__global__ void __launch_bounds__(32 * RWPB, 4) k_eig_tri_r(EigArgs a, EigSplit sp, int u0, int nb) {
+  constexpr int NQ = (K + 31) / 32;
+  constexpr int NR = K > 2 ? K - 2 : 1;   // reflector rows
+  constexpr int K4 = K / 4;
+  __shared__ __align__(16) float sv[RWPB][NR * K + 4 * K];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ub = blockIdx.x * RWPB + warp;
+  if (ub >= nb) return;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  const int k = a.k;
+  float *VH = sv[warp];            // reflector j in row j
+  float *ww = VH + NR * K;         // w of the current step
+  float *dd = ww + K, *ee = dd + K, *tau = ee + K;
+  // A = G + (k-1)/infl I (src/letkf_core.F90:101-104), upper triangle packed
+  const float *Gin = a.G + (size_t)unit * packed_size(k);
+  const float shift = (float)(k - 1) * 1.0f / a.infl;
+  float A[NQ][K];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int r = lane + 32 * q;
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+      float v = 0.0f;
+      if (r < k && c < k) {
+        v = r <= c ? Gin[tri_idx(r, c, k)] : Gin[tri_idx(c, r, k)];
+        if (r == c) v += shift;
+      }
+      A[q][c] = v;
+    }
+  }
+  for (int j = 0; j < k - 2; j++) {
+    float *vj = VH + j * K;
+    __syncwarp();
+    if (lane == (j & 31)) {
+      const int oq = j >> 5;
+#pragma unroll
+      for (int c = 0; c < K; c++) {
+        const float x = (NQ == 1 || oq == 0) ? A[0][c] : A[NQ - 1][c];
+        vj[c] = (c > j && c < k) ? x : 0.0f;
+        if (c == j) dd[j] = x;
+      }
+    }
+    __syncwarp();
+    float s = 0.0f;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int c = lane + 32 * q;
+      if (c < K) { const float x = vj[c]; s += x * x; }
+    }
+    const float sig = wsum<float>(s);
+    const float x0 = vj[j + 1];
+    const float s1 = sig - x0 * x0;
+    if (!(s1 > Lim<float>::tiny * sig) || sig == 0.0f) {
+      if (lane == 0) { tau[j] = 0.0f; ee[j] = x0; }
+      continue;
+    }
+    const float alpha = -copysignf(sqrtf(sig), x0);
+    const float v0 = x0 - alpha;
+    const float t = 2.0f / (v0 * v0 + s1);
+    __syncwarp();
+    if (lane == 0) { vj[j + 1] = v0; tau[j] = t; ee[j] = alpha; }
+    __syncwarp();
+    // p = t A v
+    float p[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int c4 = 0; c4 < K4; c4++) {
+        if (4 * c4 + 3 <= j) continue;
+        const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * c4);
+        acc = __fmaf_rn(A[q][4 * c4 + 0], v4.x, acc);
+        acc = __fmaf_rn(A[q][4 * c4 + 1], v4.y, acc);
+        acc = __fmaf_rn(A[q][4 * c4 + 2], v4.z, acc);
+        acc = __fmaf_rn(A[q][4 * c4 + 3], v4.w, acc);
+      }
+      p[q] = t * acc;
+    }
+    float pv = 0.0f;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int r = lane + 32 * q;
+      if (r < K) pv = __fmaf_rn(p[q], vj[r], pv);
+    }
+    const float beta = 0.5f * t * wsum<float>(pv);
+    float w[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int r = lane + 32 * q;
+      w[q] = (r > j && r < k) ? p[q] - beta * vj[r] : 0.0f;
+      if (r < K) ww[r] = w[q];
+    }
+    __syncwarp();
+    // A -= v w^T + w v^T
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int r = lane + 32 * q;
+      const float vr = r < K ? vj[r] : 0.0f, wr = w[q];
+#pragma unroll
+      for (int c4 = 0; c4 < K4; c4++) {
+        if (4 * c4 + 3 <= j) continue;
+        const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * c4);
+        const float4 w4 = *reinterpret_cast<const float4 *>(ww + 4 * c4);
+        A[q][4 * c4 + 0] = A[q][4 * c4 + 0] - __fmaf_rn(vr, w4.x, wr * v4.x);
+        A[q][4 * c4 + 1] = A[q][4 * c4 + 1] - __fmaf_rn(vr, w4.y, wr * v4.y);
+        A[q][4 * c4 + 2] = A[q][4 * c4 + 2] - __fmaf_rn(vr, w4.z, wr * v4.z);
+        A[q][4 * c4 + 3] = A[q][4 * c4 + 3] - __fmaf_rn(vr, w4.w, wr * v4.w);
+      }
+    }
+  }
+  __syncwarp();
+  // the last 2 x 2 block: d[k-2], d[k-1], e[k-2]
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int r = lane + 32 * q;
+    if (r == k - 2 || r == k - 1) {
+#pragma unroll
+      for (int c = 0; c < K; c++) {
+        if (c == r) dd[r] = A[q][c];
+        if (r == k - 1 && c == k - 2) ee[k - 2] = A[q][c];
+      }
+    }
+  }
+  if (lane == 0) ee[k - 1] = 0.0f;
+  __syncwarp();
+  // Q = H_0 H_1 ... H_{k-3} I, reflectors from the last to the first; lane l
+  // holds columns l and l + 32
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int c = lane + 32 * q;
+#pragma unroll
+    for (int r = 0; r < K; r++) A[q][r] = (r == c && c < k) ? 1.0f : 0.0f;
+  }
+  for (int j = k - 3; j >= 0; j--) {
+    const float t = tau[j];
+    if (t == 0.0f) continue;
+    const float *vj = VH + j * K;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      float s = 0.0f;
+#pragma unroll
+      for (int r4 = 0; r4 < K4; r4++) {
+        if (4 * r4 + 3 <= j) continue;
+        const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * r4);
+        s = __fmaf_rn(v4.x, A[q][4 * r4 + 0], s);
+        s = __fmaf_rn(v4.y, A[q][4 * r4 + 1], s);
+        s = __fmaf_rn(v4.z, A[q][4 * r4 + 2], s);
+        s = __fmaf_rn(v4.w, A[q][4 * r4 + 3], s);
+      }
+      s *= t;
+#pragma unroll
+      for (int r4 = 0; r4 < K4; r4++) {
+        if (4 * r4 + 3 <= j) continue;
+        const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * r4);
+        A[q][4 * r4 + 0] -= v4.x * s;
+        A[q][4 * r4 + 1] -= v4.y * s;
+        A[q][4 * r4 + 2] -= v4.z * s;
+        A[q][4 * r4 + 3] -= v4.w * s;
+      }
+    }
+  }
+  float *Q = sp.Q + (size_t)ub * k * k;
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int c = lane + 32 * q;
+    if (c < k) {
+#pragma unroll
+      for (int r = 0; r < K; r++)
+        if (r < k) Q[(size_t)r * k + c] = A[q][r];
+    }
+  }
+  float *de = sp.DE + (size_t)ub * 2 * k;
+  for (int i = lane; i < k; i += 32) { de[i] = dd[i]; de[k + i] = ee[i]; }
+}
+
 constexpr int QLT = 64;   // threads (units) per block of k_eig_ql
 
 __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, int nb) {
@@ -1017,6 +1209,21 @@ static int eig_team(int k) { return k <= 64 ? 1 : 2; }
 // 25.8 -> 26.6, k = 64 57.2 -> 53.8; C4 (824k units) k = 100 1057 -> 974
 static bool eig_packed(int k) { return k > 48; }
 
+// the register-resident first stage (k <= 48)
+static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
+  const int grid = (nb + RWPB - 1) / RWPB;
+  switch ((a.k + 7) & ~7) {
+  case 8: k_eig_tri_r<8><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
+  case 16: k_eig_tri_r<16><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
+  case 24: k_eig_tri_r<24><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
+  case 32: k_eig_tri_r<32><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
+  case 40: k_eig_tri_r<40><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
+  case 48: k_eig_tri_r<48><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
+  default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 template <int NQ, int NW, bool kPackedTri>
 static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart,
                                   int ucount, int *launches) {
@@ -1033,9 +1240,6 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
     if ((e = cudaFuncSetAttribute(k_eig_trip<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt)) !=
         cudaSuccess)
       return e;
-  } else if ((e = cudaFuncSetAttribute(k_eig_tri<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem)) != cudaSuccess) {
-    return e;
   }
   if ((e = cudaFuncSetAttribute(k_eig_vec<NQ, NW, kPackedTri>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem)) != cudaSuccess)
@@ -1047,7 +1251,7 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
   for (int u0 = ustart; u0 < uend; u0 += batch) {
     const int nb = uend - u0 < batch ? uend - u0 : batch;
     if (kPackedTri) k_eig_trip<NW><<<(nb + wpt - 1) / wpt, tht, smt, st>>>(a, sp, wpt, u0, nb);
-    else k_eig_tri<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    else if ((e = launch_tri_r(st, a, sp, u0, nb)) != cudaSuccess) return e;
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
     k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
     (*launches) += 3;

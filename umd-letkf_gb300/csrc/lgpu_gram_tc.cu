@@ -71,7 +71,6 @@ constexpr size_t kSmemBudget = 227 * 1024 - 4096;   // dynamic shared memory (st
 constexpr int WT = 256;        // threads of the stream kernels
 constexpr int WCB = 2 * WB;   // bytes of one chunk's cached weight operand block (hi | lo)
 constexpr int YS = 20;         // floats per member row of a chunk record (16 observations + 4: conflict-free rows)
-
 __device__ __forceinline__ uint32_t kmaj(int row, int kk) {
   return (uint32_t)(row >> 3) * SBO + (uint32_t)(kk >> 2) * CMB + (uint32_t)(row & 7) * 16u + (uint32_t)(kk & 3) * 4u;
 }
@@ -314,9 +313,12 @@ __global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps
 
 struct TcSmem {
   unsigned long long full[NSMAX], empty[NSMAX], rfull[NRMAX], done;
+  unsigned long long accf;   // drain: the accumulation so far is complete in TMEM (commit + MMA thread)
+  unsigned long long acce;   // drain: warps 0-3 have read TMEM (one arrival per warp)
   int anyk[NSMAX];           // chunk index + 1 of the last chunk of the stage with a kept pair
   uint32_t tmem;
-  int issued;
+  int issued;                // MMAs were issued since the last drain
+  int sub_issued;            // the same, for the accumulation a drain hands over
   int fault;
   unsigned char fi[NPMAX];
   unsigned char fj[NPMAX];
@@ -363,11 +365,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(16) TcSmem S;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int seg = blockIdx.x % a.nseg;
-  const int rest = blockIdx.x / a.nseg;
-  const int pass = a.pass0 + rest % a.npl;
-  const int g = (rest / a.npl) % a.groups;
-  const int tile = rest / (a.npl * a.groups);
+  // block = (work item, group, pass of this launch), pass fastest
+  const int pass = a.pass0 + blockIdx.x % a.npl;
+  const int g = (blockIdx.x / a.npl) % a.groups;
+  const TcWork wk = a.work[blockIdx.x / (a.npl * a.groups)];
+  const int tile = wk.tile, seg = wk.seg;
   const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
   const int slotb = cb;   // ring slot: one chunk record
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
@@ -376,8 +378,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   unsigned char *ring = dsm + (size_t)NS * stage_bytes;
   // this CTA's segment of the tile's chunk stream
   const int t0 = a.tile_off[tile], tn = a.tile_off[tile + 1] - t0;
-  const int seglen = (tn + a.nseg - 1) / a.nseg;
-  const int cs = min(tn, seg * seglen), ce = min(tn, cs + seglen);
+  const int cs = min(tn, wk.cs), ce = min(tn, wk.ce);
   const int c0 = t0 + cs;
   float *wcache = WMODE != 0 ? a.wcache + (size_t)g * a.nchunk_total * (WCB / 4) : nullptr;
   int *wflag = WMODE != 0 ? a.wflag + (size_t)g * a.nchunk_total : nullptr;
@@ -395,7 +396,10 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     }
     for (int r = 0; r < NR; r++) tc::mbar_init(reinterpret_cast<uint64_t *>(&S.rfull[r]), 1);
     tc::mbar_init(reinterpret_cast<uint64_t *>(&S.done), 1);
+    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.accf), 2);
+    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.acce), 4);
     S.issued = 0;
+    S.sub_issued = 0;
     S.fault = 0;
     tc::mbar_fence_init();
   }
@@ -416,6 +420,44 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   const int wc = tid & (TM - 1), wq = (tid >> 7) & 3;
   int ncand = 0, nkeep = 0;
   float rsum = 0.0f;
+
+  // The CTA's results: thread tid < TM (warps 0-3, TMEM lane = column wc)
+  // owns its column.  A tile whose stream is one drain interval writes the
+  // column's G row; otherwise every drain interval goes to its own partial
+  // block, feature-major, so that a warp's stores of one feature are 32
+  // consecutive floats.
+  const int G = a.groups;
+  const int D = a.drain;
+  const int nvalid = nf - pass * NP < NP ? nf - pass * NP : NP;
+  // warps 0-3: the accumulator's lane of this thread (zeros unless
+  // from_tmem, which is CTA-uniform) into partial block blk
+  auto store_block = [&](int blk, bool from_tmem) {
+    float *base = a.Gpart + (((size_t)blk * G + g) * nf + (size_t)pass * NP) * TM + wc;
+    for (int f0 = 0; f0 < NP; f0 += 16) {
+      float v[16];
+      if (from_tmem) {
+        tc::tmem_ld16(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)f0, v);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 16; q++) v[q] = 0.0f;
+      }
+#pragma unroll
+      for (int q = 0; q < 16; q++)
+        if (f0 + q < nvalid) base[(size_t)(f0 + q) * TM] = v[q];
+    }
+  };
+  // drain j: wait until the MMAs before boundary (j + 1) D have completed,
+  // move the accumulator to its block, hand TMEM back to the MMA thread
+  const int nflush = nchunks > 0 ? (nchunks - 1) / D : 0;
+  int nflushed = 0;
+  auto flush = [&](int j) {
+    if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.accf), j & 1)) S.fault = 1;
+    tc::fence_after();
+    store_block(wk.blk0 + j, S.sub_issued != 0 && S.fault == 0);
+    tc::fence_before();
+    __syncwarp();
+    if (lane == 0) bar_arrive(&S.acce);
+  };
 
   if (wid < NPW) {
     const int col = a.tile_cols[(size_t)tile * TM + wc];
@@ -446,6 +488,10 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
 
     for (int ch = 0; ch < nchunks; ch++) {
       const int s = ch % NS, r = ch % NR;
+      // warps 0-3 drain TMEM at boundary b = (j + 1) D once the stages of
+      // chunks b .. b + NS - 1 are produced: the MMA of chunk b + NS needs the
+      // stage chunk b frees, which waits for the drain
+      if (wid < 4 && nflushed < nflush && ch == (nflushed + 1) * D + NS) flush(nflushed++);
       if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[r]), (ch / NR) & 1)) { S.fault = 1; break; }
       if (ch >= NS && !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.empty[s]), ((ch / NS) - 1) & 1)) {
         S.fault = 1;
@@ -563,6 +609,8 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       __syncwarp();
       if (lane == 0) bar_arrive(&S.full[s]);
     }
+    if (wid < 4)
+      while (nflushed < nflush) flush(nflushed++);
   } else if (wid == MMA_WARP) {
     // ================================================= MMA issue + record loads (one thread)
     if (lane == 0) {
@@ -576,10 +624,21 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       for (int ch = 0; ch < n_loaded; ch++) load(ch);
       const int nb0 = NP < 256 ? NP : 256, nb1 = NP - nb0;
       const uint32_t id0 = tc::idesc_tf32(TM, nb0), id1 = nb1 > 0 ? tc::idesc_tf32(TM, nb1) : 0u;
-      bool issued = false;
-      int nmma = 0;
+      bool issued = false;   // since the last drain
+      int nmma = 0, fj = 0;
       for (int ch = 0; ch < nchunks; ch++) {
         const int s = ch % NS;
+        if (ch > 0 && ch % a.drain == 0) {
+          // boundary: hand the accumulation to warps 0-3 and wait until they
+          // have read TMEM; the next MMA starts a fresh accumulation
+          S.sub_issued = issued ? 1 : 0;
+          tc::commit(reinterpret_cast<uint64_t *>(&S.accf));
+          bar_arrive(&S.accf);
+          if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.acce), fj & 1)) { S.fault = 1; break; }
+          tc::fence_after();
+          fj++;
+          issued = false;
+        }
         const int cached_flag = WMODE == 2 ? wflag[c0 + ch] : 0;   // issued before the wait hides its latency
         if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.full[s]), (ch / NS) & 1)) { S.fault = 1; break; }
         // every producer is done with the records of chunk ch: refill the slot
@@ -637,7 +696,6 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   __syncthreads();
 
   // ---- per-column diagnostics, kept counts, epilogue (warps 0-3 = TMEM lanes)
-  const int G = a.groups;
   if (tid < TM) {
     for (int q = 0; q < 3; q++) {
       ncand += dcand[q * TM + wc];
@@ -649,33 +707,44 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     size_t unit = 0;
     if (colv) unit = (size_t)a.col2act[col] * G + g;
     if (colv && pass == 0) {
-      if (a.nseg == 1) {
+      if (wk.cblk < 0) {
         a.nkept[unit] = nkeep;
         if (a.diag_lg_obscount) a.diag_lg_obscount[(size_t)g * a.ncol + col] = (float)nkeep;
         if (a.diag_lg_obsloc) a.diag_lg_obsloc[(size_t)g * a.ncol + col] = rsum;
         if (g == 0 && a.diag_obscount) a.diag_obscount[col] = (float)ncand;
       } else {
-        float *cc = a.cnt + ((size_t)seg * a.units + unit) * 3;
+        float *cc = a.cnt + (((size_t)wk.cblk * G + g) * TM + wc) * 3;
         cc[0] = (float)nkeep;
         cc[1] = (float)ncand;
         cc[2] = rsum;
       }
     }
-    float *Gbase = seg == 0 ? a.G : a.Gpart + (size_t)(seg - 1) * (size_t)a.units * nf;
-    float *Gp = Gbase + unit * (size_t)nf + (size_t)pass * NP;
-    const int nvalid = nf - pass * NP < NP ? nf - pass * NP : NP;
-    for (int f0 = 0; f0 < NP; f0 += 16) {
-      float v[16];
-      if (issued && !fault) {
-        tc::tmem_ld16(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)f0, v);
-      } else {
+    if (wk.blk0 >= 0) {
+      // the last drain interval of the segment
+      store_block(wk.blk0 + nflush, issued && !fault);
+    } else {
+      // the whole stream in one accumulator: the column's G row (16-byte
+      // aligned: nf and NP are multiples of 4)
+      float *Gp = colv ? a.G + unit * (size_t)nf + (size_t)pass * NP : nullptr;
+      for (int f0 = 0; f0 < NP; f0 += 16) {
+        float v[16];
+        if (issued && !fault) {
+          tc::tmem_ld16(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)f0, v);
+        } else {
 #pragma unroll
-        for (int q = 0; q < 16; q++) v[q] = 0.0f;
-      }
-      if (colv) {
+          for (int q = 0; q < 16; q++) v[q] = 0.0f;
+        }
+        if (Gp) {
+          if (f0 + 16 <= nvalid && (nf & 3) == 0) {
 #pragma unroll
-        for (int q = 0; q < 16; q++)
-          if (f0 + q < nvalid) Gp[f0 + q] = v[q];
+            for (int q = 0; q < 16; q += 4)
+              *reinterpret_cast<float4 *>(Gp + f0 + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+              if (f0 + q < nvalid) Gp[f0 + q] = v[q];
+          }
+        }
       }
     }
   }
@@ -825,7 +894,7 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
   int ns, nr;
   size_t smem;
   gram_tc_config(a.k, a.np, &ns, &nr, &smem);
-  const long long per_pass = (long long)a.ntiles * a.groups * a.nseg;
+  const long long per_pass = (long long)a.nwork * a.groups;
   if (per_pass * a.npass > 0x7fffffffLL) return cudaErrorInvalidValue;
   cudaError_t e;
   if (a.npass >= 2 && a.wcache) {
@@ -864,41 +933,66 @@ cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
 }
 
 namespace {
-// G += partial Grams of segments 1..nseg-1, in segment order; counts summed
-// in segment order (the sums of rho in FP32, as a single CTA would)
-__global__ void k_gram_segsum(long long units, int nf, int nseg, int groups, int ncol, const int *active, float *G,
-                              const float *Gpart, const float *cnt, int *nkept, float *diag_obscount,
-                              float *diag_lg_obscount, float *diag_lg_obsloc) {
-  const long long total = units * nf;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-    float v = G[t];
-    for (int s = 1; s < nseg; s++) v += Gpart[(size_t)(s - 1) * total + t];
-    G[t] = v;
-    if (t % nf == 0) {
-      const long long u = t / nf;
+// A tile whose stream spans several drain intervals: G = the sum of its
+// partial blocks in FP64, in stream order, rounded once; kept counts,
+// candidate counts and the sums of rho summed over the segments in segment
+// order (FP32 for rho, as one CTA accumulates it).  One block per (tile,
+// group): 32 features at a time, the sums are formed with threads along the
+// columns (coalesced block reads) and written with a warp along a column's
+// row (coalesced G writes) through shared memory.
+constexpr int SST = 256;
+__global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
+  __shared__ double acc[32][TM + 1];
+  const TcSegTile st = a.segtiles[blockIdx.x / a.groups];
+  const int g = blockIdx.x % a.groups, G = a.groups, nf = a.nf;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c = tid & (TM - 1), fh = tid >> 7;   // column, feature half
+  const size_t bstride = (size_t)G * nf * TM;   // between consecutive blocks
+  const float *P = a.Gpart + ((size_t)st.blk0 * G + g) * nf * TM;
+  for (int f0 = 0; f0 < nf; f0 += 32) {
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+      const int f = f0 + fh * 16 + i;
+      double v = 0.0;
+      if (f < nf)
+        for (int b = 0; b < st.nblk; b++) v += (double)P[b * bstride + (size_t)f * TM + c];
+      acc[fh * 16 + i][c] = v;
+    }
+    __syncthreads();
+    for (int cc = warp; cc < TM; cc += SST / 32) {
+      const int col = a.tile_cols[(size_t)st.tile * TM + cc];
+      if (col < 0 || f0 + lane >= nf) continue;
+      const size_t unit = (size_t)a.col2act[col] * G + g;
+      a.G[unit * nf + f0 + lane] = (float)acc[lane][cc];
+    }
+    __syncthreads();
+  }
+  if (tid < TM) {
+    const int col = a.tile_cols[(size_t)st.tile * TM + c];
+    if (col >= 0) {
+      const size_t unit = (size_t)a.col2act[col] * G + g;
       float kept = 0.0f, cand = 0.0f, rs = 0.0f;
-      for (int s = 0; s < nseg; s++) {
-        const float *cc = cnt + ((size_t)s * units + u) * 3;
+      for (int s = 0; s < st.nseg; s++) {
+        const float *cc = a.cnt + (((size_t)(st.cblk0 + s) * G + g) * TM + c) * 3;
         kept += cc[0];
         cand += cc[1];
         rs += cc[2];
       }
-      const int act = (int)(u / groups), g = (int)(u % groups), col = active[act];
-      nkept[u] = (int)kept;
-      if (diag_lg_obscount) diag_lg_obscount[(size_t)g * ncol + col] = kept;
-      if (diag_lg_obsloc) diag_lg_obsloc[(size_t)g * ncol + col] = rs;
-      if (g == 0 && diag_obscount) diag_obscount[col] = cand;
+      a.nkept[unit] = (int)kept;
+      if (a.diag_lg_obscount) a.diag_lg_obscount[(size_t)g * a.ncol + col] = kept;
+      if (a.diag_lg_obsloc) a.diag_lg_obsloc[(size_t)g * a.ncol + col] = rs;
+      if (g == 0 && a.diag_obscount) a.diag_obscount[col] = cand;
     }
   }
 }
 }  // namespace
 
 cudaError_t launch_gram_segsum(cudaStream_t st, const TcArgs &a, const int *active, int *launches) {
-  if (a.nseg <= 1 || a.units <= 0) return cudaSuccess;
-  const long long total = a.units * a.nf;
-  const int grid = (int)std::min<long long>(152 * 16, (total + 255) / 256);
-  k_gram_segsum<<<grid, 256, 0, st>>>(a.units, a.nf, a.nseg, a.groups, a.ncol, active, a.G, a.Gpart, a.cnt, a.nkept,
-                                       a.diag_obscount, a.diag_lg_obscount, a.diag_lg_obsloc);
+  (void)active;
+  if (a.nsegtiles <= 0) return cudaSuccess;
+  const long long grid = (long long)a.nsegtiles * a.groups;
+  if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+  k_gram_segsum<<<(int)grid, SST, 0, st>>>(a);
   (*launches)++;
   return cudaGetLastError();
 }

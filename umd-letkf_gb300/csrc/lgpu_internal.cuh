@@ -436,6 +436,22 @@ struct TilePar {
   float c2cap;       // squared chord of the cap radius, with margin
   float hmax;        // largest half-chord of a candidate pair of the tile
 };
+// One accumulation segment of a tile's chunk stream, one CTA: chunks [cs, ce)
+// of the tile's stream.  The CTA drains its tensor-core accumulator every
+// `drain` chunks; when the tile's stream holds more than one drain interval,
+// drain j of this segment goes to partial block blk0 + j and the segment's
+// counts to count block cblk (both -1 when the whole stream is one interval:
+// the CTA writes G and the counts directly).
+struct TcWork {
+  int tile, seg, cs, ce, cblk, blk0, pad0, pad1;
+};
+// A tile whose stream spans more than one drain interval: count blocks
+// cblk0 .. cblk0 + nseg - 1 (one per segment), partial blocks blk0 .. blk0 +
+// nblk - 1 (one per drain interval, in stream order).
+struct TcSegTile {
+  int tile, nseg, cblk0, nblk, blk0, pad0, pad1, pad2;
+};
+
 struct TcArgs {
   int ntiles, groups, k, kp, npass, np, nf, ncol;
   const int *tile_cols;   // [ntiles][128] column index or -1
@@ -452,16 +468,20 @@ struct TcArgs {
   int *wflag;                // [groups][chunks]: the chunk has a kept pair (MMA issued)
   int nchunk_total;          // chunks over all tiles (weight cache indexing)
   int pass0, npl;            // feature passes of one launch: [pass0, pass0 + npl) (set by the launcher)
-  // accumulation segments: each tile's chunk stream is split into nseg
-  // consecutive ranges, each accumulated by its own CTA; segment 0 writes G,
-  // segment s > 0 its partial Gram at Gpart + (s - 1) * units * nf and its
-  // counts at cnt + s * units * 3 (segment 0 too when nseg > 1), summed in
-  // segment order by launch_gram_segsum
-  int nseg;
+  // accumulation segments and drains: each tile's chunk stream is split into
+  // segments (one CTA each), and each CTA moves its tensor-core accumulator
+  // out every `drain` chunks (the FP32 accumulation error of the tensor core
+  // grows with the MMAs summed into one accumulator); launch_gram_segsum sums
+  // a tile's drained partials in FP64, in stream order
+  const TcWork *work;     // [nwork] work items (tile order, then segment)
+  int nwork;
+  int drain;              // chunks per drain interval
   int cull;               // 1: a warp skips the distance and localizer of four records none of its columns can reach
   long long units;
-  float *Gpart;
-  float *cnt;                // [nseg][units][3]: kept, candidates, sum rho (when nseg > 1)
+  float *Gpart;              // [partial block][group][nf][128] (feature-major: coalesced drains)
+  float *cnt;                // [count block][group][128][3]: kept, candidates, sum rho
+  const TcSegTile *segtiles; // [nsegtiles] tiles with more than one segment
+  int nsegtiles;
   float *G;
   int *nkept;
   float *diag_obscount, *diag_lg_obscount, *diag_lg_obsloc;

@@ -117,7 +117,10 @@ EXPORTS = ["lgpu_set_variant", "lgpu_create", "lgpu_destroy", "lgpu_last_error",
            "lgpu_get_obs_prepared", "lgpu_debug_transform", "lgpu_bind_state",
            "lgpu_debug_weight", "lgpu_learn_init", "lgpu_learn_collect", "lgpu_learn_train", "lgpu_learn_stats_get",
            "lgpu_learn_param_count", "lgpu_learn_get_params", "lgpu_learn_set_params", "lgpu_mlp_debug",
-           "lgpu_learn_set_network", "lgpu_set_precision"]
+           "lgpu_learn_set_network", "lgpu_set_precision", "lgpu_write_diag", "lgpu_get_loc_diag",
+           "lgpu_write_loc_diag", "lgpu_io_last_error", "lgpu_ens_filename", "lgpu_nc_dim_len", "lgpu_nc_var_info",
+           "lgpu_nc_read_float", "lgpu_nc_read_int", "lgpu_read_obs_nc", "lgpu_read_hx_nc", "lgpu_read_state_nc",
+           "lgpu_write_state_nc", "lgpu_write_diag_nc", "lgpu_write_loc_diag_nc"]
 
 _lib = None
 
@@ -175,6 +178,26 @@ def lib(path=None):
     L.lgpu_learn_set_params.argtypes = [H, FP, ctypes.c_longlong]
     L.lgpu_mlp_debug.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, FP, FP, FP, FP,
                                  FP, FP, FP]
+    C, LLP = ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)
+    CPP = ctypes.POINTER(ctypes.c_char_p)
+    FPP = ctypes.POINTER(FP)
+    L.lgpu_write_diag.argtypes = [H, C, ctypes.c_int, ctypes.c_int, FP, FP]
+    L.lgpu_get_loc_diag.argtypes = [H, FP]
+    L.lgpu_write_loc_diag.argtypes = [H, C, ctypes.c_int, ctypes.c_int, FP, FP, ctypes.c_int, FP]
+    L.lgpu_io_last_error.argtypes = []
+    L.lgpu_io_last_error.restype = ctypes.c_char_p
+    L.lgpu_ens_filename.argtypes = [C, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+    L.lgpu_nc_dim_len.argtypes = [C, C, LLP]
+    L.lgpu_nc_var_info.argtypes = [C, C, IP, LLP, ctypes.c_int]
+    L.lgpu_nc_read_float.argtypes = [C, C, FP, ctypes.c_longlong]
+    L.lgpu_nc_read_int.argtypes = [C, C, IP, ctypes.c_longlong]
+    L.lgpu_read_obs_nc.argtypes = [C, ctypes.c_int, IP, FP, FP, FP, FP, FP, FP, IP, IP, IP]
+    L.lgpu_read_hx_nc.argtypes = [C, ctypes.c_int, ctypes.c_int, FP]
+    L.lgpu_read_state_nc.argtypes = [C, C, ctypes.c_int, ctypes.c_int, ctypes.c_int, FP]
+    L.lgpu_write_state_nc.argtypes = [C, ctypes.c_int, ctypes.c_int, FP, FP, ctypes.c_int, CPP, IP, FPP,
+                                      ctypes.c_int, CPP, IP, FPP]
+    L.lgpu_write_diag_nc.argtypes = [C, ctypes.c_int, ctypes.c_int, ctypes.c_int, FP, FP, FP, FP, FP, FP]
+    L.lgpu_write_loc_diag_nc.argtypes = [C, ctypes.c_int, ctypes.c_int, FP, FP, FP, FP]
     if path is None:
         _lib = L
     return L
@@ -475,6 +498,23 @@ class Solver:
         self._ck(self.L.lgpu_get_diag(self.h, _fp(d["maxhz"]), _fp(d["obscount"]), _fp(d["lg_obscount"]),
                                       _fp(d["lg_obsloc"])))
         return d
+
+    def write_diag(self, path, nx, ny, lat_nom, lon_nom):
+        """letkf_solver_final's diag.solver.nc of the last run (lgpu_write_diag)."""
+        la, lo = _f32(lat_nom), _f32(lon_nom)
+        return self._ck(self.L.lgpu_write_diag(self.h, str(path).encode(), int(nx), int(ny), _fp(la), _fp(lo)))
+
+    def get_loc_diag(self):
+        """loc_ocean: level count of each column's surface localisation group."""
+        out = np.empty(self.ncol, np.float32)
+        self._ck(self.L.lgpu_get_loc_diag(self.h, _fp(out)))
+        return out
+
+    def write_loc_diag(self, path, nx, ny, lat_nom, lon_nom, vert_nom):
+        """loc_ocean_final's diag.loc_ocean.nc of the last run (lgpu_write_loc_diag)."""
+        la, lo, vz = _f32(lat_nom), _f32(lon_nom), _f32(vert_nom)
+        return self._ck(self.L.lgpu_write_loc_diag(self.h, str(path).encode(), int(nx), int(ny), _fp(la), _fp(lo),
+                                                   len(vz), _fp(vz)))
 
     # -- learned form (no counterpart in the reference)
     def learn_init(self, nx, ny, stride=4, hidden=512, judge_frac=0.02, gate_frac=0.05, sample_frac=0.25,

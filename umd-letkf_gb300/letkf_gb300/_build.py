@@ -17,7 +17,7 @@ LGSYNTH = os.path.join(SYNTH, "liblgsynth.so")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["lgpu_api.cu", "lgpu_index.cu", "lgpu_gram.cu", "lgpu_gram_tc.cu", "lgpu_eig.cu", "lgpu_update.cu",
-              "lgpu_noalloc.cu", "lgpu_prep.cu", "lgpu_mlp.cu", "lgpu_learn.cu"]
+              "lgpu_noalloc.cu", "lgpu_prep.cu", "lgpu_mlp.cu", "lgpu_learn.cu", "lgpu_ncio.cpp"]
 NVCC_FLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
               "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xptxas", "-O3", "-I", INCLUDE, "-I", CSRC]
@@ -58,7 +58,7 @@ def build_lgpu(force=False, verbose=False):
     objs, jobs = [], []
     for s in CU_SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(BUILD, s.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]

@@ -13,6 +13,9 @@ sections a reference YAML configuration would carry for them.
   c5        learned form: 720x360x40, k=32, c3's clustered network (persistent
             clusters), loc_novrt 400 km, stride-4 coarse lattice, 5 exact
             training cycles
+  c2learn   the learned form on the headline lattice: 720x360x40, k=40,
+            C2's localisation, 440,000 observations in wide clusters
+            (close to uniform), stride 4, 5 exact training cycles
   c5mid     c5 with 10 levels and 2 training cycles (profiling-sized: the same
             network rows per analysis)
   c2mid     c2 observations on a 360x180x10 grid (profiling-sized: the same
@@ -78,6 +81,16 @@ WORKLOADS = {
                learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.1, sample_frac=0.6, train_cap=600000,
                           seed=5),
                cycles=dict(train=5, u=0.5, kappa=1.0e3, dt=21600.0, epochs=15, batch=1024, lr=1e-3)),
+    # the learned form on the headline lattice and ensemble: 720x360x40, k = 40,
+    # C2's localisation (800 km at the equator to 200 km at the poles),
+    # 440,000 observations from the cycling observer in 12 clusters of
+    # 3,000 km (close to uniform, C2's density), stride-4 coarse lattice
+    "c2learn": dict(gen=dict(workload="c3", k=40, n_obs=440000, cluster_sigma_m=3.0e6),
+                    localization=C2_LOC, solver={},
+                    learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.1, sample_frac=0.6,
+                               train_cap=600000, seed=5),
+                    cycles=dict(train=5, u=0.5, kappa=1.0e3, dt=21600.0, epochs=15, batch=1024, lr=1e-3,
+                                cluster_sigma_m=3.0e6)),
     "c5mid": dict(gen=dict(workload="c3", k=32, nz=10),
                   localization={"class": "loc_novrt",
                                 "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 400.0e3}]}},
