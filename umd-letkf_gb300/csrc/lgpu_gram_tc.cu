@@ -950,14 +950,21 @@ __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
   const size_t bstride = (size_t)G * nf * TM;   // between consecutive blocks
   const float *P = a.Gpart + ((size_t)st.blk0 * G + g) * nf * TM;
   for (int f0 = 0; f0 < nf; f0 += 32) {
-#pragma unroll 4
-    for (int i = 0; i < 16; i++) {
-      const int f = f0 + fh * 16 + i;
-      double v = 0.0;
-      if (f < nf)
-        for (int b = 0; b < st.nblk; b++) v += (double)P[b * bstride + (size_t)f * TM + c];
-      acc[fh * 16 + i][c] = v;
+    // blocks in stream order, the 16 features' loads of a block independent
+    double v[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = 0.0;
+    const int fb = f0 + fh * 16;
+    for (int b = 0; b < st.nblk; b++) {
+      const float *Pb = P + b * bstride + (size_t)fb * TM + c;
+      float x[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++) x[i] = fb + i < nf ? Pb[(size_t)i * TM] : 0.0f;
+#pragma unroll
+      for (int i = 0; i < 16; i++) v[i] += (double)x[i];
     }
+#pragma unroll
+    for (int i = 0; i < 16; i++) acc[fh * 16 + i][c] = v[i];
     __syncthreads();
     for (int cc = warp; cc < TM; cc += SST / 32) {
       const int col = a.tile_cols[(size_t)st.tile * TM + cc];
