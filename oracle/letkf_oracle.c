@@ -11,6 +11,11 @@
  *                 The eigensolver is a double-precision cyclic Jacobi whose
  *                 output is rounded to float (stand-in for LAPACK ssyev).
  *   precision 64: the same steps in double (the FP64 oracle).
+ *   OR_PREC_LAPACK: the reference's own sequence of library calls
+ *                 (sgemm / ssyev / sgemm / sgemm / sgemm, then one sgemm
+ *                 per slab) through an optimised BLAS / LAPACK the caller
+ *                 registers: the timed CPU baseline, with the arithmetic
+ *                 the reference binary runs.
  * In both modes observation distances and localisation weights are the
  * float values the reference passes around (REAL), computed by the shared
  * documented metric below and by letkf_loc_gc in double, as the reference
@@ -220,7 +225,14 @@ static int lower_bound_lon(const double *a, int lo, int hi, double v) {
   return lo;
 }
 
-/* all obs with dist <= rmax, ascending id; returns count, fills ids & dist */
+typedef struct { int id; float d; } id_dist;
+static int cmp_id(const void *a, const void *b) {
+  int x = ((const id_dist *)a)->id, y = ((const id_dist *)b)->id;
+  return (x > y) - (x < y);
+}
+
+/* all obs with dist <= rmax, ascending id; returns count (-1: out of
+ * memory), fills ids & dist */
 static int search(const ctx_t *c, int col, float rmax, int *ids, float *dist) {
   const float *cu = c->cu + 3 * col;
   double latc = c->p.lat[col], lonc = norm_lon(c->p.lon[col]);
@@ -257,12 +269,16 @@ static int search(const ctx_t *c, int col, float rmax, int *ids, float *dist) {
         if (d <= rmax) { ids[n] = id; dist[n] = d; n++; }
       }
   }
-  /* canonical order: ascending observation index */
-  for (int i = 1; i < n; i++) {
-    if (ids[i] > ids[i - 1]) continue;
-    int id = ids[i]; float d = dist[i]; int j = i - 1;
-    while (j >= 0 && ids[j] > id) { ids[j + 1] = ids[j]; dist[j + 1] = dist[j]; j--; }
-    ids[j + 1] = id; dist[j + 1] = d;
+  /* canonical order: ascending observation index (indices are unique) */
+  int sorted = 1;
+  for (int i = 1; i < n && sorted; i++) sorted = ids[i] > ids[i - 1];
+  if (!sorted) {
+    id_dist *t = malloc(sizeof(id_dist) * (size_t)n);
+    if (!t) return -1;
+    for (int i = 0; i < n; i++) { t[i].id = ids[i]; t[i].d = dist[i]; }
+    qsort(t, (size_t)n, sizeof(id_dist), cmp_id);
+    for (int i = 0; i < n; i++) { ids[i] = t[i].id; dist[i] = t[i].d; }
+    free(t);
   }
   return n;
 }
@@ -469,9 +485,60 @@ static int core64(int k, int n, const float *hdxb, const float *rdiag, const flo
   return rc;
 }
 
+/* src/letkf_core.F90:69-146 as the reference calls its libraries: every
+ * product through sgemm with the reference's arguments, the eigensolve
+ * through ssyev('V','U') with its workspace size (64+2)*nbv
+ * (src/letkf_core.F90:60).  The Fortran arrays hdxb(k,n) and trans(k,k) are
+ * the column-major [n][k] and [k][k] buffers here. */
+static or_sgemm_fn g_sgemm;
+static or_ssyev_fn g_ssyev;
+
+int or_set_lapack(or_sgemm_fn sgemm, or_ssyev_fn ssyev) {
+  g_sgemm = sgemm;
+  g_ssyev = ssyev;
+  return (sgemm && ssyev) ? 0 : -1;
+}
+
+static int core_lapack(int k, int n, const float *hdxb, const float *rdiag, const float *rloc,
+                       const float *dep, float infl, float *trans, float *ws) {
+  float *rinv = ws, *work1 = rinv + (size_t)n * k, *eivec = work1 + k * k, *pa = eivec + k * k;
+  float *work2 = pa + k * k, *work3 = work2 + (size_t)k * n, *eival = work3 + k, *evwork = eival + k;
+  int lwork = (64 + 2) * k, info = 0;
+  char cn = 'n', ct = 't', cv = 'V', cu = 'U';
+  float one = 1.0f, zero = 0.0f;
+  for (int j = 0; j < n; j++)                                              /* :92-94 */
+    for (int i = 0; i < k; i++) rinv[(size_t)j * k + i] = hdxb[(size_t)j * k + i] / rdiag[j] * rloc[j];
+  g_sgemm(&cn, &ct, &k, &k, &n, &one, rinv, &k, (float *)hdxb, &k, &zero, work1, &k);   /* :97-98 */
+  float r = (float)(k - 1) * 1.0f / infl;                                  /* :101-104 */
+  for (int i = 0; i < k; i++) work1[i + k * i] = work1[i + k * i] + r;
+  g_ssyev(&cv, &cu, &k, work1, &k, eival, evwork, &lwork, &info);          /* :107 */
+  memcpy(eivec, work1, sizeof(float) * k * k);                             /* :108 */
+  for (int i = 0; i < k; i++)                                              /* :111-113 */
+    for (int r2 = 0; r2 < k; r2++) work1[r2 + k * i] = eivec[r2 + k * i] / eival[i];
+  g_sgemm(&cn, &ct, &k, &k, &k, &one, work1, &k, eivec, &k, &zero, pa, &k);            /* :114-115 */
+  g_sgemm(&cn, &cn, &k, &n, &k, &one, pa, &k, rinv, &k, &zero, work2, &k);              /* :118-119 */
+  for (int i = 0; i < k; i++) work3[i] = 0.0f;                             /* :122-125 */
+  for (int j = 0; j < n; j++) for (int i = 0; i < k; i++) work3[i] = work3[i] + work2[i + (size_t)k * j] * dep[j];
+  for (int j = 0; j < k; j++) {                                            /* :128-131 */
+    float rr = sqrtf((float)(k - 1) / eival[j]);
+    for (int i = 0; i < k; i++) work1[i + k * j] = eivec[i + k * j] * rr;
+  }
+  g_sgemm(&cn, &ct, &k, &k, &k, &one, work1, &k, eivec, &k, &zero, trans, &k);         /* :132-133 */
+  for (int j = 0; j < k; j++) for (int i = 0; i < k; i++) trans[i + k * j] = trans[i + k * j] + work3[i];  /* :139-141 */
+  return info == 0 ? 0 : 1;
+}
+
 int or_core_solve(int precision, int k, int n, const float *hdxb, const float *rdiag,
                   const float *rloc, const float *dep, float infl, float *trans) {
   int rc;
+  if (precision == OR_PREC_LAPACK) {
+    if (!g_sgemm || !g_ssyev) return -2;
+    float *ws = malloc(sizeof(float) * (2 * (size_t)n * k + 3 * k * k + 68 * (size_t)k + 8));
+    if (!ws) return -1;
+    rc = core_lapack(k, n, hdxb, rdiag, rloc, dep, infl, trans, ws);
+    free(ws);
+    return rc;
+  }
   if (precision == 64) {
     double *ws = malloc(sizeof(double) * ((size_t)n * k + 3 * k * k + 4 * k + 8));
     double *tr = malloc(sizeof(double) * k * k);
@@ -549,6 +616,7 @@ static int solve_column(const ctx_t *c, int precision, int col, int slot, or_res
   if (res->maxhz) res->maxhz[slot] = maxhz;
   if (ws_grow(w, p->nobs, k, ns, maxg)) return -1;
   int n = search(c, col, rmax, w->ids, w->dist);           /* :217 */
+  if (n < 0) return -1;
   if (res->obscount) res->obscount[slot] = (float)n;
   for (int i = 0; i < n; i++) {                            /* :224-229 */
     int id = w->ids[i];
@@ -584,6 +652,16 @@ static int solve_column(const ctx_t *c, int precision, int col, int slot, or_res
             for (int i = 0; i < k; i++) acc += (double)bkg_x[s * k + i] * w->tr64[i + k * j];
             w->xd[s * k + j] = acc;
           }
+        }
+      } else if (precision == OR_PREC_LAPACK) {
+        rc |= core_lapack(k, nl, w->khdxb, w->krdiag, w->krloc, w->kdep, 1.0f, w->tr32, (float *)w->core_ws);
+        int one_i = 1;
+        char cn = 'n';
+        float one = 1.0f, zero = 0.0f;
+        for (int s = 0; s < ns; s++) {                     /* :285-289 */
+          if (w->slab_group[s] != g) continue;
+          g_sgemm(&cn, &cn, &one_i, &k, &k, &one, (float *)bkg_x + s * k, &one_i, w->tr32, &k, &zero, xs + s * k,
+                  &one_i);
         }
       } else {
         rc |= core32(k, nl, w->khdxb, w->krdiag, w->krloc, w->kdep, 1.0f, w->tr32, (float *)w->core_ws);
@@ -703,7 +781,8 @@ static int solve_column(const ctx_t *c, int precision, int col, int slot, or_res
 int or_run(void *vc, int precision, const int *cols, int ncl, or_result *res, int nthreads) {
   ctx_t *c = vc;
   if (!c || !res || !res->state || !res->mean || !res->sprd) return -1;
-  if (precision != 32 && precision != 64) return -2;
+  if (precision != 32 && precision != 64 && precision != OR_PREC_LAPACK) return -2;
+  if (precision == OR_PREC_LAPACK && (!g_sgemm || !g_ssyev)) return -2;
   if (c->p.k < 2 || c->loc.maxgroups < 1) return -3;
   int n = cols ? ncl : c->p.ncol;
   int nth = 1;
@@ -739,6 +818,7 @@ int or_obslist(void *vc, int col, int group, int *idx, float *rloc, int cap, int
   if (!p->mask[col]) {
     float rmax = loc_maxhz(c, col) * STDEV2MAX;
     int n = search(c, col, rmax, ids, dist);
+    if (n < 0) n = 0, nl = -1;
     if (ncand) *ncand = n;
     int ng = loc_groups(c, col, sg, gid);
     if (group >= 0 && group < ng)

@@ -79,8 +79,11 @@ void *or_create(const or_problem *p, const or_loc *loc);
 void or_destroy(void *ctx);
 
 /* Run the analysis for the listed columns (all columns when cols == NULL).
- * precision: 32 = float mirror of the reference arithmetic, 64 = double.
+ * precision: 32 = float mirror of the reference arithmetic, 64 = double,
+ * OR_PREC_LAPACK = the reference's own call sequence through the BLAS /
+ * LAPACK routines registered with or_set_lapack (sgemm, ssyev: FP32).
  * Returns 0 on success. */
+#define OR_PREC_LAPACK 1
 int or_run(void *ctx, int precision, const int *cols, int ncl, or_result *res, int nthreads);
 
 /* Local observation list of (column, group) in canonical order (ascending
@@ -97,6 +100,15 @@ float or_dist(const float a[3], const float b[3]);
 int or_eigh(int k, const double *A, double *lam, double *V);   /* Jacobi, ascending */
 int or_core_solve(int precision, int k, int n, const float *hdxb, const float *rdiag,
                   const float *rloc, const float *dep, float infl, float *trans);
+
+/* Fortran-convention BLAS sgemm and LAPACK ssyev (every argument by address)
+ * for OR_PREC_LAPACK, e.g. an optimised library's entry points.  Returns 0
+ * when both are non-NULL. */
+typedef void (*or_sgemm_fn)(char *transa, char *transb, int *m, int *n, int *k, float *alpha, float *a, int *lda,
+                            float *b, int *ldb, float *beta, float *c, int *ldc);
+typedef void (*or_ssyev_fn)(char *jobz, char *uplo, int *n, float *a, int *lda, float *w, float *work, int *lwork,
+                            int *info);
+int or_set_lapack(or_sgemm_fn sgemm, or_ssyev_fn ssyev);
 
 #ifdef __cplusplus
 }

@@ -93,8 +93,44 @@ def lib():
         L.or_eigh.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_double)]
         L.or_core_solve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, FP, FP, FP, FP, ctypes.c_float, FP]
+        L.or_set_lapack.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
+
+
+PREC_LAPACK = 1   # OR_PREC_LAPACK: the reference's sgemm / ssyev call sequence
+
+
+def set_lapack():
+    """Register an optimised BLAS sgemm and LAPACK ssyev with the oracle
+    (the ones SciPy is linked with, taken from scipy.linalg.cython_blas /
+    cython_lapack), enabling precision PREC_LAPACK.  Each call runs on the
+    calling thread when OPENBLAS_NUM_THREADS=1 was set before SciPy loaded;
+    the oracle parallelises over columns.  Returns a description of the
+    library."""
+    from scipy.linalg import cython_blas, cython_lapack
+    get_name = ctypes.pythonapi.PyCapsule_GetName
+    get_name.restype = ctypes.c_char_p
+    get_name.argtypes = [ctypes.py_object]
+    get_ptr = ctypes.pythonapi.PyCapsule_GetPointer
+    get_ptr.restype = ctypes.c_void_p
+    get_ptr.argtypes = [ctypes.py_object, ctypes.c_char_p]
+
+    def ptr(cap):
+        return get_ptr(cap, get_name(cap))
+
+    rc = lib().or_set_lapack(ptr(cython_blas.__pyx_capi__["sgemm"]), ptr(cython_lapack.__pyx_capi__["ssyev"]))
+    if rc != 0:
+        raise RuntimeError("sgemm / ssyev not found in SciPy")
+    desc = "SciPy's BLAS / LAPACK"
+    try:
+        import scipy
+        cfg = scipy.show_config(mode="dicts")
+        blas = cfg.get("Build Dependencies", {}).get("blas", {})
+        desc = "%s %s (SciPy %s)" % (blas.get("name", "BLAS"), blas.get("version", ""), scipy.__version__)
+    except Exception:
+        pass
+    return desc
 
 
 def _fp(a):

@@ -309,3 +309,31 @@ def test_fp32_mirror_close_to_fp64():
     assert np.linalg.norm(pa - pb) / np.linalg.norm(pb) < 1e-5
     assert np.linalg.norm(a["mean"] - b["mean"]) / np.linalg.norm(b["mean"]) < 1e-6
     o.close()
+
+
+def test_lapack_call_sequence():
+    """The oracle's library-call form (the reference's sgemm / ssyev('V','U')
+    sequence through SciPy's BLAS / LAPACK, the timed CPU baseline) agrees
+    with the FP64 oracle as closely as the FP32 restatement does."""
+    pytest.importorskip("scipy")
+    from letkf_gb300.workloads import WORKLOADS
+    from oracle import oracle as O
+    O.set_lapack()
+    rng = np.random.default_rng(3)
+    for k in (3, 10, 40):
+        # the FP64 form is pinned to the closed form above
+        y = rng.standard_normal(k).astype(f32)
+        err, r, d = f32(0.7), f32(0.9), f32(-0.4)
+        got64 = O.core_solve(y[None, :], [err], [r], [d], precision=64)
+        got = O.core_solve(y[None, :], [err], [r], [d], precision=O.PREC_LAPACK)
+        assert np.allclose(got, got64, atol=2e-6, rtol=0), (k, np.abs(got - got64).max())
+    prob = workload("c1")
+    wl = WORKLOADS["c1"]
+    o = _oracle(prob, wl["localization"], rtps=0.6)
+    cols = np.arange(0, prob.ncol, 5)
+    a, b = o.run(O.PREC_LAPACK, cols=cols, nthreads=1), o.run(64, cols=cols)
+    pa, pb = a["state"] - a["mean"][:, :, None], b["state"] - b["mean"][:, :, None]
+    assert np.linalg.norm(pa - pb) / np.linalg.norm(pb) < 1e-5
+    assert np.linalg.norm(a["mean"] - b["mean"]) / np.linalg.norm(b["mean"]) < 1e-6
+    assert np.array_equal(a["lg_obscount"], b["lg_obscount"])
+    o.close()

@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps
 struct TcSmem {
   unsigned long long full[NSMAX], empty[NSMAX], rfull[NRMAX], done;
   unsigned long long accf;   // drain: the accumulation so far is complete in TMEM (commit + MMA thread)
-  unsigned long long acce;   // drain: warps 0-3 have read TMEM (one arrival per warp)
+  unsigned long long acce;   // drain: the producer warps have read TMEM (one arrival per warp)
   int anyk[NSMAX];           // chunk index + 1 of the last chunk of the stage with a kept pair
   uint32_t tmem;
   int issued;                // MMAs were issued since the last drain
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     for (int r = 0; r < NR; r++) tc::mbar_init(reinterpret_cast<uint64_t *>(&S.rfull[r]), 1);
     tc::mbar_init(reinterpret_cast<uint64_t *>(&S.done), 1);
     tc::mbar_init(reinterpret_cast<uint64_t *>(&S.accf), 2);
-    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.acce), 4);
+    tc::mbar_init(reinterpret_cast<uint64_t *>(&S.acce), NPW);
     S.issued = 0;
     S.sub_issued = 0;
     S.fault = 0;
@@ -421,22 +421,24 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   int ncand = 0, nkeep = 0;
   float rsum = 0.0f;
 
-  // The CTA's results: thread tid < TM (warps 0-3, TMEM lane = column wc)
-  // owns its column.  A tile whose stream is one drain interval writes the
-  // column's G row; otherwise every drain interval goes to its own partial
-  // block, feature-major, so that a warp's stores of one feature are 32
-  // consecutive floats.
+  // The CTA's results: TMEM lane = column wc.  A tile whose stream is one
+  // drain interval writes the column's G row (thread tid < TM, warps 0-3);
+  // otherwise every drain interval goes to its own partial block,
+  // feature-major, so that a warp's stores of one feature are 32 consecutive
+  // floats (the 16 producer warps drain, each warp a quarter of the features
+  // of its lane quarter).
   const int G = a.groups;
   const int D = a.drain;
   const int nvalid = nf - pass * NP < NP ? nf - pass * NP : NP;
-  // warps 0-3: the accumulator's lane of this thread (zeros unless
-  // from_tmem, which is CTA-uniform) into partial block blk
-  auto store_block = [&](int blk, bool from_tmem) {
+  // the accumulator's lane of this thread (TMEM lane quarter wid % 4; zeros
+  // unless from_tmem, which is CTA-uniform), features [16 q, 16 q + 16) for
+  // q = q0, q0 + qs, ..., into partial block blk
+  auto store_block = [&](int blk, bool from_tmem, int q0, int qs) {
     float *base = a.Gpart + (((size_t)blk * G + g) * nf + (size_t)pass * NP) * TM + wc;
-    for (int f0 = 0; f0 < NP; f0 += 16) {
+    for (int f0 = 16 * q0; f0 < NP; f0 += 16 * qs) {
       float v[16];
       if (from_tmem) {
-        tc::tmem_ld16(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)f0, v);
+        tc::tmem_ld16(tmem + ((uint32_t)((wid & 3) * 32) << 16) + (uint32_t)f0, v);
       } else {
 #pragma unroll
         for (int q = 0; q < 16; q++) v[q] = 0.0f;
@@ -446,14 +448,15 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         if (f0 + q < nvalid) base[(size_t)(f0 + q) * TM] = v[q];
     }
   };
-  // drain j: wait until the MMAs before boundary (j + 1) D have completed,
-  // move the accumulator to its block, hand TMEM back to the MMA thread
+  // drain j (all 16 producer warps, warp w the features of quarter w / 4):
+  // wait until the MMAs before boundary (j + 1) D have completed, move the
+  // accumulator to its block, hand TMEM back to the MMA thread
   const int nflush = nchunks > 0 ? (nchunks - 1) / D : 0;
   int nflushed = 0;
   auto flush = [&](int j) {
     if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.accf), j & 1)) S.fault = 1;
     tc::fence_after();
-    store_block(wk.blk0 + j, S.sub_issued != 0 && S.fault == 0);
+    store_block(wk.blk0 + j, S.sub_issued != 0 && S.fault == 0, wid >> 2, 4);
     tc::fence_before();
     __syncwarp();
     if (lane == 0) bar_arrive(&S.acce);
@@ -488,10 +491,10 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
 
     for (int ch = 0; ch < nchunks; ch++) {
       const int s = ch % NS, r = ch % NR;
-      // warps 0-3 drain TMEM at boundary b = (j + 1) D once the stages of
-      // chunks b .. b + NS - 1 are produced: the MMA of chunk b + NS needs the
-      // stage chunk b frees, which waits for the drain
-      if (wid < 4 && nflushed < nflush && ch == (nflushed + 1) * D + NS) flush(nflushed++);
+      // the producers drain TMEM at boundary b = (j + 1) D once the stages
+      // of chunks b .. b + NS - 1 are produced: the MMA of chunk b + NS needs
+      // the stage chunk b frees, which waits for the drain
+      if (nflushed < nflush && ch == (nflushed + 1) * D + NS) flush(nflushed++);
       if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[r]), (ch / NR) & 1)) { S.fault = 1; break; }
       if (ch >= NS && !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.empty[s]), ((ch / NS) - 1) & 1)) {
         S.fault = 1;
@@ -609,8 +612,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       __syncwarp();
       if (lane == 0) bar_arrive(&S.full[s]);
     }
-    if (wid < 4)
-      while (nflushed < nflush) flush(nflushed++);
+    while (nflushed < nflush) flush(nflushed++);
   } else if (wid == MMA_WARP) {
     // ================================================= MMA issue + record loads (one thread)
     if (lane == 0) {
@@ -629,8 +631,8 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       for (int ch = 0; ch < nchunks; ch++) {
         const int s = ch % NS;
         if (ch > 0 && ch % a.drain == 0) {
-          // boundary: hand the accumulation to warps 0-3 and wait until they
-          // have read TMEM; the next MMA starts a fresh accumulation
+          // boundary: hand the accumulation to the producer warps and wait
+          // until they have read TMEM; the next MMA starts a fresh accumulation
           S.sub_issued = issued ? 1 : 0;
           tc::commit(reinterpret_cast<uint64_t *>(&S.accf));
           bar_arrive(&S.accf);
@@ -721,7 +723,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     }
     if (wk.blk0 >= 0) {
       // the last drain interval of the segment
-      store_block(wk.blk0 + nflush, issued && !fault);
+      store_block(wk.blk0 + nflush, issued && !fault, 0, 1);
     } else {
       // the whole stream in one accumulator: the column's G row (16-byte
       // aligned: nf and NP are multiples of 4)
@@ -934,7 +936,12 @@ cudaError_t launch_gram_tc(cudaStream_t st, const TcArgs &a_in, int *launches) {
 
 namespace {
 // A tile whose stream spans several drain intervals: G = the sum of its
-// partial blocks in FP64, in stream order, rounded once; kept counts,
+// partial blocks in stream order, compensated in FP32 (Sum2 of Ogita, Rump
+// and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6),
+// 2005: Knuth's error-free TwoSum carries each addition's rounding error
+// into a second accumulator, so the result is as accurate as a sum in twice
+// the working precision, rounded once; GB300's FP64 pipe is 1/64 of its FP32
+// rate, which an FP64 sum of the partials runs into); kept counts,
 // candidate counts and the sums of rho summed over the segments in segment
 // order (FP32 for rho, as one CTA accumulates it).  One block per (tile,
 // group): 32 features at a time, the sums are formed with threads along the
@@ -942,7 +949,7 @@ namespace {
 // row (coalesced G writes) through shared memory.
 constexpr int SST = 256;
 __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
-  __shared__ double acc[32][TM + 1];
+  __shared__ float acc[32][TM + 1];
   const TcSegTile st = a.segtiles[blockIdx.x / a.groups];
   const int g = blockIdx.x % a.groups, G = a.groups, nf = a.nf;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -951,9 +958,9 @@ __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
   const float *P = a.Gpart + ((size_t)st.blk0 * G + g) * nf * TM;
   for (int f0 = 0; f0 < nf; f0 += 32) {
     // blocks in stream order, the 16 features' loads of a block independent
-    double v[16];
+    float hs[16], ls[16];   // running sum, accumulated rounding errors
 #pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = 0.0;
+    for (int i = 0; i < 16; i++) hs[i] = ls[i] = 0.0f;
     const int fb = f0 + fh * 16;
     for (int b = 0; b < st.nblk; b++) {
       const float *Pb = P + b * bstride + (size_t)fb * TM + c;
@@ -961,16 +968,23 @@ __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
 #pragma unroll
       for (int i = 0; i < 16; i++) x[i] = fb + i < nf ? Pb[(size_t)i * TM] : 0.0f;
 #pragma unroll
-      for (int i = 0; i < 16; i++) v[i] += (double)x[i];
+      for (int i = 0; i < 16; i++) {
+        // TwoSum: s + e == hs + x exactly
+        const float s = __fadd_rn(hs[i], x[i]);
+        const float z = __fsub_rn(s, hs[i]);
+        const float e = __fadd_rn(__fsub_rn(hs[i], __fsub_rn(s, z)), __fsub_rn(x[i], z));
+        hs[i] = s;
+        ls[i] = __fadd_rn(ls[i], e);
+      }
     }
 #pragma unroll
-    for (int i = 0; i < 16; i++) acc[fh * 16 + i][c] = v[i];
+    for (int i = 0; i < 16; i++) acc[fh * 16 + i][c] = __fadd_rn(hs[i], ls[i]);
     __syncthreads();
     for (int cc = warp; cc < TM; cc += SST / 32) {
       const int col = a.tile_cols[(size_t)st.tile * TM + cc];
       if (col < 0 || f0 + lane >= nf) continue;
       const size_t unit = (size_t)a.col2act[col] * G + g;
-      a.G[unit * nf + f0 + lane] = (float)acc[lane][cc];
+      a.G[unit * nf + f0 + lane] = acc[lane][cc];
     }
     __syncthreads();
   }
