@@ -944,19 +944,23 @@ namespace {
 // rate, which an FP64 sum of the partials runs into); kept counts,
 // candidate counts and the sums of rho summed over the segments in segment
 // order (FP32 for rho, as one CTA accumulates it).  One block per (tile,
-// group): 32 features at a time, the sums are formed with threads along the
-// columns (coalesced block reads) and written with a warp along a column's
-// row (coalesced G writes) through shared memory.
+// group, 32 features): the sums are formed with threads along the columns
+// (coalesced block reads) and written with a warp along a column's row
+// (coalesced G writes) through shared memory; the first feature block of a
+// (tile, group) also sums the counts.
 constexpr int SST = 256;
 __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
   __shared__ float acc[32][TM + 1];
-  const TcSegTile st = a.segtiles[blockIdx.x / a.groups];
-  const int g = blockIdx.x % a.groups, G = a.groups, nf = a.nf;
+  const int nfc = (a.nf + 31) / 32;
+  const int fc = blockIdx.x % nfc, tg = blockIdx.x / nfc;
+  const TcSegTile st = a.segtiles[tg / a.groups];
+  const int g = tg % a.groups, G = a.groups, nf = a.nf;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int c = tid & (TM - 1), fh = tid >> 7;   // column, feature half
   const size_t bstride = (size_t)G * nf * TM;   // between consecutive blocks
   const float *P = a.Gpart + ((size_t)st.blk0 * G + g) * nf * TM;
-  for (int f0 = 0; f0 < nf; f0 += 32) {
+  {
+    const int f0 = 32 * fc;
     // blocks in stream order, the 16 features' loads of a block independent
     float hs[16], ls[16];   // running sum, accumulated rounding errors
 #pragma unroll
@@ -986,9 +990,8 @@ __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
       const size_t unit = (size_t)a.col2act[col] * G + g;
       a.G[unit * nf + f0 + lane] = acc[lane][cc];
     }
-    __syncthreads();
   }
-  if (tid < TM) {
+  if (fc == 0 && tid < TM) {
     const int col = a.tile_cols[(size_t)st.tile * TM + c];
     if (col >= 0) {
       const size_t unit = (size_t)a.col2act[col] * G + g;
@@ -1011,7 +1014,7 @@ __global__ void __launch_bounds__(SST) k_gram_segsum(TcArgs a) {
 cudaError_t launch_gram_segsum(cudaStream_t st, const TcArgs &a, const int *active, int *launches) {
   (void)active;
   if (a.nsegtiles <= 0) return cudaSuccess;
-  const long long grid = (long long)a.nsegtiles * a.groups;
+  const long long grid = (long long)a.nsegtiles * a.groups * ((a.nf + 31) / 32);
   if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
   k_gram_segsum<<<(int)grid, SST, 0, st>>>(a);
   (*launches)++;
