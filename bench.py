@@ -415,6 +415,7 @@ def link_summary(tims):
             "d2h_state_gbs": db / (down * 1e-3) / 1e9 if down > 0 else None,
             "device_span_ms": m("span_ms"), "device_compute_ms": m("total_ms"),
             "host_set_obs_ms": m("host_obs_ms"), "host_run_ms": m("host_run_ms"),
+            "stage_ms": {k: m(k + "_ms") for k in ("tiles", "gram", "eig", "update", "index", "prep")},
             "span_ms_per_step": [round(t["span_ms"], 2) for t in tims],
             "host_run_ms_per_step": [round(t["host_run_ms"], 2) for t in tims]}
 

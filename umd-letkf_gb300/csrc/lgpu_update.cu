@@ -404,6 +404,10 @@ __global__ void __launch_bounds__(256, TPS) k_update_rows(UpdateArgs a) {
 
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   if (a.ncol <= 0 || a.ncols <= 0) return cudaSuccess;
+  {
+    const cudaError_t e = launch_update_tc(st, a, launches);   // the tensor-core form where it applies
+    if (e != cudaErrorNotSupported) return e;
+  }
   const size_t rbytes = ((size_t)a.ns * a.k + (size_t)a.groups * a.k * a.k) * sizeof(float);
   if (a.k % 4 == 0 && a.ns <= 256 && rbytes <= 200 * 1024) {
     const int k = a.k;

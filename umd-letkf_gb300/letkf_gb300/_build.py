@@ -17,7 +17,7 @@ LGSYNTH = os.path.join(SYNTH, "liblgsynth.so")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["lgpu_api.cu", "lgpu_index.cu", "lgpu_gram.cu", "lgpu_gram_tc.cu", "lgpu_eig.cu", "lgpu_update.cu",
-              "lgpu_noalloc.cu", "lgpu_prep.cu", "lgpu_mlp.cu", "lgpu_learn.cu", "lgpu_ncio.cpp"]
+              "lgpu_update_tc.cu", "lgpu_noalloc.cu", "lgpu_prep.cu", "lgpu_mlp.cu", "lgpu_learn.cu", "lgpu_ncio.cpp"]
 NVCC_FLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
               "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xptxas", "-O3", "-I", INCLUDE, "-I", CSRC]
