@@ -979,32 +979,53 @@ __device__ __forceinline__ void vr_block(float (&R)[NQ][K], float (&z)[NQ], int 
       const float2 cs = ring[(e0 - i) & 63];
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
+        // s av + c z, c av - s z: one FMA on the carried z each
         const float av = R[q][i];
-        R[q][i1] = __fmaf_rn(cs.y, av, __fmul_rn(cs.x, z[q]));
-        z[q] = __fmaf_rn(cs.x, av, -__fmul_rn(cs.y, z[q]));
+        R[q][i1] = __fmaf_rn(cs.x, z[q], __fmul_rn(cs.y, av));
+        z[q] = __fmaf_rn(-cs.y, z[q], __fmul_rn(cs.x, av));
       }
     }
   }
 }
 
-// z = R[q][c] / R[q][c] = z for a warp-uniform column c < K
-template <int K, int NQ>
+// z = R[q][c] / R[q][c] = z for a warp-uniform column c in block B
+template <int B, int K, int NQ>
 __device__ __forceinline__ void vr_get(const float (&R)[NQ][K], float (&z)[NQ], int c) {
 #pragma unroll
-  for (int j = 0; j < K; j++)
-    if (j == c) {
+  for (int jj = 0; jj < 8; jj++) {
+    const int j = 8 * B + jj < K ? 8 * B + jj : K - 1;
+    if ((c & 7) == jj) {
 #pragma unroll
       for (int q = 0; q < NQ; q++) z[q] = R[q][j];
     }
+  }
 }
-template <int K, int NQ>
+template <int B, int K, int NQ>
 __device__ __forceinline__ void vr_put(float (&R)[NQ][K], const float (&z)[NQ], int c) {
 #pragma unroll
-  for (int j = 0; j < K; j++)
-    if (j == c) {
+  for (int jj = 0; jj < 8; jj++) {
+    const int j = 8 * B + jj < K ? 8 * B + jj : K - 1;
+    if ((c & 7) == jj) {
 #pragma unroll
       for (int q = 0; q < NQ; q++) R[q][j] = z[q];
     }
+  }
+}
+
+// f(integral_constant<B>) for the warp-uniform block index b < K / 8, so
+// that f sees B as a compile-time constant
+template <int V> struct IC { static constexpr int value = V; };
+template <int K, class F>
+__device__ __forceinline__ void vr_by_block(int b, F &&f) {
+  switch (b) {
+  case 0: f(IC<0>{}); break;
+  case 1: if constexpr (K > 8) f(IC<(K > 8 ? 1 : 0)>{}); break;
+  case 2: if constexpr (K > 16) f(IC<(K > 16 ? 2 : 0)>{}); break;
+  case 3: if constexpr (K > 24) f(IC<(K > 24 ? 3 : 0)>{}); break;
+  case 4: if constexpr (K > 32) f(IC<(K > 32 ? 4 : 0)>{}); break;
+  case 5: if constexpr (K > 40) f(IC<(K > 40 ? 5 : 0)>{}); break;
+  default: break;
+  }
 }
 
 template <int K>
@@ -1040,14 +1061,28 @@ __global__ void __launch_bounds__(32 * RWPB, K > 40 ? 2 : (K > 32 ? 3 : 4)) k_ei
   // ---- replay the rotations: V = Q Z
   int bad = 0;
   {
+    // the log in chunks of 32 entries (lane j: entry 32 t + j): chunks
+    // t .. t + 3 are in flight in pre0..pre3 (chunk t in pre[t % 4]) while
+    // the ring holds the two before
     const float2 *lg = sp.log + (size_t)ub * sp.cap;
+    auto fetch = [&](int t) {
+      const int idx = 32 * t + lane;
+      return idx < total ? lg[idx] : make_float2(0.0f, 0.0f);
+    };
+    float2 pre0 = fetch(0), pre1 = fetch(1), pre2 = fetch(2), pre3 = fetch(3);
     int loaded = 0;   // log entries [0, loaded) have been copied to the ring
     auto ensure = [&](int upto) {   // warp-uniform
       if (loaded >= upto) return;
       __syncwarp();
       do {
-        const int idx = loaded + lane;
-        ring[idx & 63] = idx < total ? lg[idx] : make_float2(0.0f, 0.0f);
+        const int t = loaded >> 5;
+        float2 *dst = ring + ((loaded + lane) & 63);
+        switch (t & 3) {
+        case 0: *dst = pre0; pre0 = fetch(t + 4); break;
+        case 1: *dst = pre1; pre1 = fetch(t + 4); break;
+        case 2: *dst = pre2; pre2 = fetch(t + 4); break;
+        default: *dst = pre3; pre3 = fetch(t + 4); break;
+        }
         loaded += 32;
       } while (loaded < upto);
       __syncwarp();
@@ -1062,20 +1097,12 @@ __global__ void __launch_bounds__(32 * RWPB, K > 40 ? 2 : (K > 32 ? 3 : 4)) k_ei
       if (cnt == 0) continue;
       const int lo = m - cnt, e0 = pidx + m - 1;   // the rotation on columns (i, i+1) is entry e0 - i
       float z[NQ];
-      vr_get<K, NQ>(R, z, m);
+      vr_by_block<K>(m >> 3, [&](auto BB) { vr_get<decltype(BB)::value, K, NQ>(R, z, m); });
       for (int b = (m - 1) >> 3; b >= (lo >> 3); b--) {
         ensure(e0 - max(8 * b, lo) + 1);
-        switch (b) {
-        case 0: vr_block<0, K, NQ>(R, z, m, lo, e0, ring); break;
-        case 1: if constexpr (K > 8) vr_block<(K > 8 ? 1 : 0), K, NQ>(R, z, m, lo, e0, ring); break;
-        case 2: if constexpr (K > 16) vr_block<(K > 16 ? 2 : 0), K, NQ>(R, z, m, lo, e0, ring); break;
-        case 3: if constexpr (K > 24) vr_block<(K > 24 ? 3 : 0), K, NQ>(R, z, m, lo, e0, ring); break;
-        case 4: if constexpr (K > 32) vr_block<(K > 32 ? 4 : 0), K, NQ>(R, z, m, lo, e0, ring); break;
-        case 5: if constexpr (K > 40) vr_block<(K > 40 ? 5 : 0), K, NQ>(R, z, m, lo, e0, ring); break;
-        default: break;
-        }
+        vr_by_block<K>(b, [&](auto BB) { vr_block<decltype(BB)::value, K, NQ>(R, z, m, lo, e0, ring); });
       }
-      vr_put<K, NQ>(R, z, lo);
+      vr_by_block<K>(lo >> 3, [&](auto BB) { vr_put<decltype(BB)::value, K, NQ>(R, z, lo); });
       pidx += cnt;
     }
   }

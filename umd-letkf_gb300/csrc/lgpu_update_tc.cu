@@ -6,19 +6,21 @@
 //
 // Persistent CTAs, one per SM, each walking the columns
 // blockIdx.x, blockIdx.x + gridDim.x, ...; warp roles:
-//   warps 0-3  epilogue: thread s owns slab s (TMEM lane s); reads its row
+//   epilogue   4 warps, or (k <= 64) two groups of 4 taking alternate
+//              columns: thread s owns slab s (TMEM lane s); reads its row
 //              of X_b T_g from TMEM, runs recenter / mean clip / RTPS / RTPP
 //              / multiplicative inflation / member bounds / spread in the
 //              order and arithmetic of k_update_rows, writes the analysis
-//              row, mean and spread;
-//   warps 4-7  operand producers: from the raw column block in shared memory,
+//              row, mean and spread; the column's scalars are loaded before
+//              the wait for its products, the slab's own once per CTA;
+//   4 warps    operand producers: from the raw column block in shared memory,
 //              chunks of 32 members of A = X_b (128 x 32) and B = T_g^T
 //              (N x 32 per group) split into TF32 hi + lo parts in the
 //              no-swizzle K-major core-matrix layout;
-//   warp 8     one thread bulk-copies each column's background block
+//   1 warp     one thread bulk-copies each column's background block
 //              (ns x k floats, contiguous) and its group transforms into a
 //              raw stage;
-//   warp 9     one thread issues tcgen05.mma kind::tf32 hi*hi + hi*lo + lo*hi
+//   1 warp     one thread issues tcgen05.mma kind::tf32 hi*hi + hi*lo + lo*hi
 //              into a double-buffered TMEM accumulator (FP32), so that the
 //              epilogue of one column overlaps the products of the next.
 // Padding (slabs past ns, members past k) is zero in both operands.  Every
@@ -36,10 +38,16 @@ constexpr int UKC = 32;                        // members per K chunk (4 MMA ste
 constexpr uint32_t UCMB = 128;                 // bytes per core matrix (8 rows x 16 B)
 constexpr uint32_t USBO = (UKC / 4) * UCMB;    // bytes per 8-row group of a chunk operand
 constexpr uint32_t UAB = UM * UKC * 4;         // bytes of one A chunk part (hi or lo)
-constexpr int NEPI = 4, NPROD = 4;
-constexpr int LOAD_WARP = NEPI + NPROD, MMA_WARP = LOAD_WARP + 1;
-constexpr int UNT = 32 * (MMA_WARP + 1);
+constexpr int NPROD = 4;                       // producer warps
 constexpr int URS = 4, UOS = 3;                // most raw / operand stages
+// epilogue warps: two groups of 4 taking alternate columns (one TMEM
+// accumulator buffer each) while a member row fits the registers, else one
+template <int NP> struct URoles {
+  static constexpr int NEPI = NP <= 64 ? 8 : 4;
+  static constexpr int NGRP = NEPI / 4;
+  static constexpr int LOAD_WARP = NEPI + NPROD, MMA_WARP = LOAD_WARP + 1;
+  static constexpr int NT = 32 * (MMA_WARP + 1);
+};
 
 struct UtcBars {
   unsigned long long raw_full[URS], raw_empty[URS], op_full[UOS], op_empty[UOS];
@@ -71,14 +79,18 @@ __device__ __forceinline__ int utc_group(const UpdateArgs &a, int lev, int mld) 
 }
 
 template <int NP>
-__global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
+__global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
+  constexpr int NEPI = URoles<NP>::NEPI, NGRP = URoles<NP>::NGRP;
+  constexpr int LOAD_WARP = URoles<NP>::LOAD_WARP, MMA_WARP = URoles<NP>::MMA_WARP;
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(8) UtcBars S;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int k = a.k, ns = a.ns, G = a.groups;
   unsigned char *raw0 = dsm;
   unsigned char *op0 = dsm + (size_t)cf.rs * cf.raw_stride;
-  auto skip_col = [&](int col) { return a.mask[col] != 0 || a.col2act[col] < 0; };
+  // every role walks the CTA's columns with the next one's active index
+  // (-1: masked, src/letkf_solver.F90:207) loaded one iteration ahead
+  auto act_of = [&](int i) { return i < a.ncols ? a.col2act[a.col0 + i] : -1; };
   auto B = [](unsigned long long &b) { return reinterpret_cast<uint64_t *>(&b); };
 
   if (wid == 0) tc::tmem_alloc(&S.tmem, cf.tmem_cols);
@@ -93,7 +105,7 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
     }
     for (int i = 0; i < 2; i++) {
       tc::mbar_init(B(S.acc_full[i]), 1);
-      tc::mbar_init(B(S.acc_empty[i]), NEPI);
+      tc::mbar_init(B(S.acc_empty[i]), 4);   // the 4 warps of the group that drains buffer i
     }
     tc::mbar_init(B(S.done), 1);
     S.fault = 0;
@@ -107,15 +119,30 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
 
   if (wid < NEPI) {
     // ============================================================ epilogue
-    const int s = tid;
+    // group grp drains the accumulator buffer of the columns n with
+    // n % NGRP == grp (NGRP = 2: buffer grp; NGRP = 1: buffer n % 2)
+    const int s = tid & 127, grp = wid >> 2;
     const float kf = (float)k, km1 = (float)(k - 1);
-    int n = 0;
-    for (int i = blockIdx.x; i < a.ncols; i += gridDim.x) {
+    // the slab's variable, level and bounds (the same for every column)
+    int v = 0, lev = 0;
+    float inc = 0.0f, lb = 0.0f, ub = 0.0f;
+    if (s < ns) {
+      v = a.slab_var[s];
+      lev = a.slab_lev[s];
+      inc = a.var_inc_max[v];
+      lb = a.var_lb[v];
+      ub = a.var_ub[v];
+    }
+    int n = 0, ii = 0;
+    int nxt = act_of(blockIdx.x);
+    for (int i = blockIdx.x; i < a.ncols; i += gridDim.x, ii++) {
       const int col = a.col0 + i;
+      const int act = nxt;
+      nxt = act_of(i + gridDim.x);
       const size_t cbase = (size_t)col * ns * k;
       const size_t ms = (size_t)col * ns + s;
-      if (skip_col(col)) {   // src/letkf_solver.F90:207: the block leaves unchanged
-        if (s < ns) {
+      if (act < 0) {   // src/letkf_solver.F90:207: the block leaves unchanged
+        if (ii % NGRP == grp && s < ns) {
           if (a.ana != a.bkg) {
             const float4 *src = reinterpret_cast<const float4 *>(a.bkg + cbase + (size_t)s * k);
             float4 *dst = reinterpret_cast<float4 *>(a.ana + cbase + (size_t)s * k);
@@ -126,37 +153,43 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
         }
         continue;
       }
+      const int mine = n % NGRP == grp;
       const int ab = n & 1;
-      if (!tc::mbar_wait(B(S.acc_full[ab]), (n >> 1) & 1)) { S.fault = 1; break; }
-      tc::fence_after();
-      const int act = a.col2act[col];
+      const int par = (n >> 1) & 1;
+      n++;
+      if (!mine) continue;
+      // the column's scalars, loaded while the products complete
       int g = 0;
       bool has = false;
+      float mb = 0.0f, sb = 0.0f;
       if (s < ns) {
-        g = utc_group(a, a.slab_lev[s], a.cp[col].mld);
+        g = utc_group(a, lev, a.cp[col].mld);
+        mb = a.mean_b[ms];
+        sb = a.sprd_b[ms];
         has = g < G && a.nkept[(size_t)act * G + g] > 0;
       }
+      if (!tc::mbar_wait(B(S.acc_full[ab]), par)) { S.fault = 1; break; }
+      tc::fence_after();
       // the slab's row of X_b T_g (TMEM loads are warp-wide: every group is
       // read, the thread keeps its own)
       float x[NP];
-      const uint32_t tb = tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)(ab * G * NP);
+      const uint32_t tb = tmem + ((uint32_t)((wid & 3) * 32) << 16) + (uint32_t)(ab * G * NP);
 #pragma unroll
       for (int c0 = 0; c0 < NP; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tb + (uint32_t)c0, v);
+        float vv[16];
+        tc::tmem_ld16(tb + (uint32_t)c0, vv);
 #pragma unroll
-        for (int q = 0; q < 16; q++) x[c0 + q] = v[q];
+        for (int q = 0; q < 16; q++) x[c0 + q] = vv[q];
         if (G > 1) {
-          tc::tmem_ld16(tb + (uint32_t)(NP + c0), v);
+          tc::tmem_ld16(tb + (uint32_t)(NP + c0), vv);
 #pragma unroll
           for (int q = 0; q < 16; q++)
-            if (g == 1) x[c0 + q] = v[q];
+            if (g == 1) x[c0 + q] = vv[q];
         }
       }
       tc::fence_before();
       __syncwarp();
       if (lane == 0) arrive(&S.acc_empty[ab]);
-      n++;
       if (s >= ns) continue;
       const float *xbr = a.bkg + cbase + (size_t)s * k;
       if (!has) {   // no local observations: the background perturbation
@@ -164,8 +197,6 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
         for (int j = 0; j < NP; j++)
           if (j < k) x[j] = xbr[j];
       }
-      const int v = a.slab_var[s];
-      const float mb = a.mean_b[ms], sb = a.sprd_b[ms];
       // recenter (:299-303)
 #pragma unroll
       for (int j = 0; j < NP; j++)
@@ -178,7 +209,6 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
 #pragma unroll
       for (int j = 0; j < NP; j++) x[j] = x[j] - m;
       // mean increment clip and bounds (:308-318)
-      const float inc = a.var_inc_max[v], lb = a.var_lb[v], ub = a.var_ub[v];
       {
         float r = m - mb;
         r = fmaxf(r, -inc); r = fminf(r, inc);
@@ -238,9 +268,11 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
     const int p = tid - 32 * NEPI;   // 0 .. 127: row of A; B items p, p + 128, ...
     int n = 0, c = 0;
     bool stop = false;
+    int nxt = act_of(blockIdx.x);
     for (int i = blockIdx.x; i < a.ncols && !stop; i += gridDim.x) {
-      const int col = a.col0 + i;
-      if (skip_col(col)) continue;
+      const int act = nxt;
+      nxt = act_of(i + gridDim.x);
+      if (act < 0) continue;
       const int rsi = n % cf.rs;
       if (!tc::mbar_wait(B(S.raw_full[rsi]), (n / cf.rs) & 1)) { S.fault = 1; break; }
       const float *X = reinterpret_cast<const float *>(raw0 + (size_t)rsi * cf.raw_stride);
@@ -301,9 +333,12 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
     // ============================================================ loader
     if (lane == 0) {
       int n = 0;
+      int nxt = act_of(blockIdx.x);
       for (int i = blockIdx.x; i < a.ncols; i += gridDim.x) {
         const int col = a.col0 + i;
-        if (skip_col(col)) continue;
+        const int act = nxt;
+        nxt = act_of(i + gridDim.x);
+        if (act < 0) continue;
         const int rsi = n % cf.rs;
         if (n >= cf.rs && !tc::mbar_wait(B(S.raw_empty[rsi]), ((n / cf.rs) - 1) & 1)) { S.fault = 1; break; }
         unsigned char *dst = raw0 + (size_t)rsi * cf.raw_stride;
@@ -311,7 +346,7 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(fb)),
                      "r"(cf.xbytes + cf.tbytes) : "memory");
         tc::bulk_copy_g2s(dst, a.bkg + (size_t)col * ns * k, cf.xbytes, fb);
-        tc::bulk_copy_g2s(dst + cf.toff, a.T + (size_t)a.col2act[col] * G * k * k, cf.tbytes, fb);
+        tc::bulk_copy_g2s(dst + cf.toff, a.T + (size_t)act * G * k * k, cf.tbytes, fb);
         n++;
       }
       // no copy may still be in flight when the CTA exits
@@ -324,9 +359,11 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
       const uint32_t idesc = tc::idesc_tf32(UM, NP);
       int n = 0, c = 0;
       bool stop = false;
+      int nxt = act_of(blockIdx.x);
       for (int i = blockIdx.x; i < a.ncols && !stop; i += gridDim.x) {
-        const int col = a.col0 + i;
-        if (skip_col(col)) continue;
+        const int act = nxt;
+        nxt = act_of(i + gridDim.x);
+        if (act < 0) continue;
         const int ab = n & 1;
         if (n >= 2 && !tc::mbar_wait(B(S.acc_empty[ab]), ((n >> 1) - 1) & 1)) { S.fault = 1; break; }
         tc::fence_after();
@@ -372,7 +409,7 @@ template <int NP>
 cudaError_t launch_np(cudaStream_t st, const UpdateArgs &a, const UtcCfg &cf, size_t smem, int grid) {
   cudaError_t e = cudaFuncSetAttribute(k_update_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_update_tc<NP><<<grid, UNT, smem, st>>>(a, cf);
+  k_update_tc<NP><<<grid, URoles<NP>::NT, smem, st>>>(a, cf);
   return cudaGetLastError();
 }
 
