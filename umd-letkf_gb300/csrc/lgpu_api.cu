@@ -92,7 +92,6 @@ struct lgpu_handle {
   cudaEvent_t ev_up[2] = {};         // bound state: background upload (copy stream)
   cudaEvent_t ev_down[kOutChunks][2] = {};   // bound state: analysis download per chunk (download stream)
   cudaEvent_t ev_upc[kOutChunks] = {};       // bound state: background of column chunk c uploaded
-  cudaEvent_t ev_gram[kOutChunks][2] = {};   // batched Gram of column chunk c (launched per chunk)
   cudaStream_t dst = nullptr;                // bound state: analysis downloads (uploads run on cst)
   float obs_h2d_ms = 0.0f, obs_host_ms = 0.0f;
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
@@ -120,9 +119,6 @@ struct lgpu_handle {
   std::vector<int> h_tile_off;       // tile stream offsets of the last batched Gram (read back)
   std::vector<TcWork> h_tc_work;     // its accumulation segments
   std::vector<TcSegTile> h_tc_seg;   // its tiles with more than one segment
-  std::vector<int> h_chunk_tile0;    // [kOutChunks + 1] first tile of each column chunk (tiles never cross chunks)
-  std::vector<int> h_chunk_w0, h_chunk_s0;   // first work item / multi-segment tile of each chunk
-  TcArgs ta_chunk;                   // the batched Gram's arguments when it is launched per chunk
   int tc_cull = -1;      // batched Gram producers: 1 with the warp-level cull, 0 without, -1 not yet measured
   float tc_tune_ms = 0.0f;   // time of the producer form the tuning run discarded (left out of AUTO's comparison)
   bool preloaded = false;    // the Gram kernels are loaded (before the first timed trial)
@@ -264,9 +260,6 @@ int lgpu_create(int device, lgpu_handle **out) {
   if (cudaStreamCreateWithFlags(&h->dst, cudaStreamNonBlocking) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_upc)
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
-  for (auto &row : h->ev_gram)
-    for (auto &ev : row)
-      if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev)
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_in)
@@ -317,8 +310,6 @@ void lgpu_destroy(lgpu_handle *h) {
   if (h->cst) cudaStreamDestroy(h->cst);
   if (h->dst) cudaStreamDestroy(h->dst);
   for (auto &ev : h->ev_upc) if (ev) cudaEventDestroy(ev);
-  for (auto &row : h->ev_gram)
-    for (auto &ev : row) if (ev) cudaEventDestroy(ev);
   delete h;
 }
 
@@ -444,24 +435,7 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
   CK(cudaMemcpyAsync(h->buf[B_COL2ACT].p, c2a.data(), sizeof(int) * nij, cudaMemcpyHostToDevice, h->st), "H2D c2a");
   if (!act.empty())
     CK(cudaMemcpyAsync(h->buf[B_ACTIVE].p, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, h->st), "H2D act");
-  // tiles per column chunk (the chunks a bound state's analysis is computed
-  // and downloaded in): no tile crosses a chunk boundary
-  std::vector<int> tiles;
-  std::vector<int> chunk_tile0(kOutChunks + 1, 0);
-  {
-    const int per = (nij + kOutChunks - 1) / kOutChunks;
-    size_t a0 = 0;
-    for (int c = 0; c < kOutChunks; c++) {
-      chunk_tile0[c] = (int)(tiles.size() / 128);
-      size_t a1 = a0;
-      while (a1 < act.size() && act[a1] < std::min(nij, (c + 1) * per)) a1++;
-      const std::vector<int> part(act.begin() + a0, act.begin() + a1);
-      const std::vector<int> t = build_tiles(part, lat, lon);
-      tiles.insert(tiles.end(), t.begin(), t.end());
-      a0 = a1;
-    }
-    chunk_tile0[kOutChunks] = (int)(tiles.size() / 128);
-  }
+  const std::vector<int> tiles = build_tiles(act, lat, lon);
   CK(h->buf[B_TILECOLS].ensure(sizeof(int) * std::max<size_t>(1, tiles.size())), "alloc tiles");
   CK(h->buf[B_TILEPAR].ensure(sizeof(TilePar) * std::max<size_t>(1, tiles.size() / 128)), "alloc tiles");
   CK(h->buf[B_TILEN].ensure(sizeof(int) * std::max<size_t>(1, tiles.size() / 128)), "alloc tiles");
@@ -471,7 +445,6 @@ int lgpu_set_grid(lgpu_handle *h, int nij, const float *lat, const float *lon, c
        "H2D tiles");
   CK(cudaStreamSynchronize(h->st), "set_grid sync");
   h->ntiles = (int)(tiles.size() / 128);
-  h->h_chunk_tile0 = chunk_tile0;
   h->auto_choice = 0;
   h->tc_cull = -1;
   h->preloaded = false;
@@ -932,12 +905,7 @@ struct TileSet {
   DevBuf *cols, *par, *n, *off;
 };
 
-// defer: the tile streams, the plan and the records only; the Gram and its
-// segment sum are launched per column chunk by gram_chunk (after the first
-// analysis of a configuration, which tunes the producer forms on the whole
-// set).  Returns whether the Gram was deferred.
-static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet &ts, int &launches, bool defer,
-                             bool *deferred) {
+static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet &ts, int &launches) {
   cudaStream_t st = h->st;
   const int k = h->k, kp = h->kp, G = h->loc.groups;
   CK(launch_tile_prep(st, ts.ntiles, (*ts.cols).as<int>(), h->buf[B_CP].as<ColPar>(),
@@ -1105,39 +1073,9 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
     h->tc_tune_ms = std::max(tm[0], tm[1]);
   } else {
     ta.cull = h->tc_cull;
-    if (defer) {
-      // first work item and multi-segment tile of each column chunk
-      const int nc = (int)h->h_chunk_tile0.size() - 1;
-      h->h_chunk_w0.assign((size_t)nc + 1, (int)h->h_tc_work.size());
-      h->h_chunk_s0.assign((size_t)nc + 1, (int)h->h_tc_seg.size());
-      for (int c = nc - 1; c >= 0; c--) {
-        const int t0 = h->h_chunk_tile0[c];
-        int w = h->h_chunk_w0[c + 1], q = h->h_chunk_s0[c + 1];
-        while (w > 0 && h->h_tc_work[w - 1].tile >= t0) w--;
-        while (q > 0 && h->h_tc_seg[q - 1].tile >= t0) q--;
-        h->h_chunk_w0[c] = w;
-        h->h_chunk_s0[c] = q;
-      }
-      h->ta_chunk = ta;
-      *deferred = true;
-      return LGPU_OK;
-    }
     CK(launch_gram_tc(st, ta, &launches), "tensor-core gram kernel");
   }
   CK(launch_gram_segsum(st, ta, h->buf[B_ACTIVE].as<int>(), &launches), "gram segment sum");
-  return LGPU_OK;
-}
-
-// the deferred batched Gram of column chunk c: its work items, then the
-// segment sum of its multi-segment tiles
-static int gram_chunk(lgpu_handle *h, int c, int &launches) {
-  TcArgs ta = h->ta_chunk;
-  ta.work += h->h_chunk_w0[c];
-  ta.nwork = h->h_chunk_w0[c + 1] - h->h_chunk_w0[c];
-  ta.segtiles += h->h_chunk_s0[c];
-  ta.nsegtiles = h->h_chunk_s0[c + 1] - h->h_chunk_s0[c];
-  if (ta.nwork > 0) CK(launch_gram_tc(h->st, ta, &launches), "tensor-core gram kernel");
-  CK(launch_gram_segsum(h->st, ta, h->buf[B_ACTIVE].as<int>(), &launches), "gram segment sum");
   return LGPU_OK;
 }
 
@@ -1166,10 +1104,7 @@ static int solver_run(lgpu_handle *h) {
   // ---- search + localize + Gram ----
   // ---- Gram: the batched tensor-core form or the plain per-column form ----
   const TileSet grid_tiles{h->ntiles, &h->buf[B_TILECOLS], &h->buf[B_TILEPAR], &h->buf[B_TILEN], &h->buf[B_TILEOFF]};
-  bool deferred = false;
-  auto run_batched = [&](bool defer) -> int {
-    return run_batched_tiles(h, os, grid_tiles, launches, defer, &deferred);
-  };
+  auto run_batched = [&]() -> int { return run_batched_tiles(h, os, grid_tiles, launches); };
   auto run_plain = [&]() -> int {
     GramArgs ga;
     ga.nunits = h->nunits;
@@ -1205,7 +1140,7 @@ static int solver_run(lgpu_handle *h) {
     CK(cudaEventRecord(h->ev_tune[0], st), "event");
     if ((rc = run_plain()) != LGPU_OK) return rc;
     CK(cudaEventRecord(h->ev_tune[1], st), "event");
-    if ((rc = run_batched(false)) != LGPU_OK) return rc;
+    if ((rc = run_batched()) != LGPU_OK) return rc;
     CK(cudaEventRecord(h->ev_tune[2], st), "event");
     CK(cudaEventSynchronize(h->ev_tune[2]), "tune sync");
     float tp = 0.0f, tb = 0.0f;
@@ -1218,10 +1153,9 @@ static int solver_run(lgpu_handle *h) {
     if (h->auto_choice == LGPU_VARIANT_PLAIN && (rc = run_plain()) != LGPU_OK) return rc;
     choice = h->auto_choice;
   } else if (choice == LGPU_VARIANT_BATCHED_TC) {
-    // a bound state: the Gram of each column chunk is launched with that
-    // chunk's eigensolve and update, so that its analysis is downloaded while
-    // the following chunks are computed
-    if ((rc = run_batched(bound)) != LGPU_OK) return rc;
+    // the whole Gram at once (a bound state's background uploads meanwhile):
+    // launched per column chunk its tails cost more than the overlap gains
+    if ((rc = run_batched()) != LGPU_OK) return rc;
   } else {
     if ((rc = run_plain()) != LGPU_OK) return rc;
   }
@@ -1265,11 +1199,6 @@ static int solver_run(lgpu_handle *h) {
     int a0 = -1, a1 = -1;
     for (int j = c0; j < c1 && a0 < 0; j++) if (h->h_col2act[j] >= 0) a0 = h->h_col2act[j];
     for (int j = c1 - 1; j >= c0 && a1 < 0; j--) if (h->h_col2act[j] >= 0) a1 = h->h_col2act[j] + 1;
-    if (deferred) {
-      CK(cudaEventRecord(h->ev_gram[c][0], st), "event");
-      if ((rc = gram_chunk(h, c, launches)) != LGPU_OK) return rc;
-      CK(cudaEventRecord(h->ev_gram[c][1], st), "event");
-    }
     CK(cudaEventRecord(h->ev_chunk[c][0], st), "event");
     if (!fp64 && batch > 0 && a0 >= 0)
       CK(launch_eig_split(st, ea, sp, batch, a0 * G, (a1 - a0) * G, &launches), "eigen kernels");
@@ -1329,12 +1258,6 @@ static int solver_run(lgpu_handle *h) {
   h->tim.index_ms = ms[0];
   h->tim.prep_ms = ms[1];
   h->tim.gram_ms = ms[2];
-  if (deferred)   // the Gram launched per column chunk
-    for (int c = 0; c < nrec; c++) {
-      float tg = 0.0f;
-      CK(cudaEventElapsedTime(&tg, h->ev_gram[c][0], h->ev_gram[c][1]), "timing");
-      h->tim.gram_ms += tg;
-    }
   h->tim.tiles_ms = 0.0f;
   if (h->used_tc) CK(cudaEventElapsedTime(&h->tim.tiles_ms, h->ev[2], h->ev[6]), "timing");
   h->tim.eig_ms = eig_ms;

@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
 }
 
 template <int NQ, int NW, bool PK>
-__global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb, int ovf_only) {
+__global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
   __shared__ float tred[NW];
   const int k = a.k, ld = k + 1;
@@ -869,7 +869,6 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb, int o
   if (a.nkept[unit] <= 0) return;
   const int total = sp.logn[ub];
   if (total == -1) return;                // no convergence: status set by k_eig_ql
-  if (ovf_only && total != -2) return;    // after k_eig_vec_r: the overflowed logs only
   EigWork W(sm + (size_t)slot * eig_floats_per_warp(k), k);
   const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
   const int tt = T.tt, TS = T.TS;
@@ -947,252 +946,6 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb, int o
   }
   T.sync();
   eig_transform<NQ>(a, unit, W, T, bad);
-  bad = __reduce_or_sync(0xffffffffu, bad);
-  if (bad && a.flag_list) {
-    if (lane == 0) sp.logn[ub] = -1;   // k_eig_flag hands the unit to the FP64 re-solve
-  } else if (bad && lane == 0) {
-    atomicOr(a.status, bad);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// k_eig_vec_r<K>: k_eig_vec for k <= K <= 48 (K a multiple of 8) with the
-// rows of V in registers.  Lane l holds rows l and l + 32 of Q (then V); the
-// logged rotations are replayed in blocks of 8 columns, the block selected by
-// a switch so that every column index is a compile-time register index; each
-// rotation's (c, s) is one broadcast load from a 64-entry shared ring that the
-// warp refills 32 log entries at a time.  The transform stages V and U in
-// shared memory: p = diag(1/lambda) V^T b with lane l summing column l down
-// the rows, wbar = V p along each lane's rows, and T = U U^T + wbar 1^T with
-// every lane accumulating a (K/8) x (K/4) tile (8 row groups x 4 column
-// groups; row strides K + 1 keep the tile loads conflict-free).  The sums
-// run in the same order as eig_transform's.  A unit whose log overflowed
-// (logn -2) is left to k_eig_vec, which re-runs its QL.
-template <int B, int K, int NQ>
-__device__ __forceinline__ void vr_block(float (&R)[NQ][K], float (&z)[NQ], int m, int lo, int e0,
-                                         const float2 *ring) {
-#pragma unroll
-  for (int jj = 7; jj >= 0; jj--) {
-    const int i = 8 * B + jj;
-    const int i1 = i + 1 < K ? i + 1 : K - 1;   // i + 1 <= m <= k - 1 wherever the rotation runs
-    if (i < m && i >= lo) {
-      const float2 cs = ring[(e0 - i) & 63];
-#pragma unroll
-      for (int q = 0; q < NQ; q++) {
-        // s av + c z, c av - s z: one FMA on the carried z each
-        const float av = R[q][i];
-        R[q][i1] = __fmaf_rn(cs.x, z[q], __fmul_rn(cs.y, av));
-        z[q] = __fmaf_rn(-cs.y, z[q], __fmul_rn(cs.x, av));
-      }
-    }
-  }
-}
-
-// z = R[q][c] / R[q][c] = z for a warp-uniform column c in block B
-template <int B, int K, int NQ>
-__device__ __forceinline__ void vr_get(const float (&R)[NQ][K], float (&z)[NQ], int c) {
-#pragma unroll
-  for (int jj = 0; jj < 8; jj++) {
-    const int j = 8 * B + jj < K ? 8 * B + jj : K - 1;
-    if ((c & 7) == jj) {
-#pragma unroll
-      for (int q = 0; q < NQ; q++) z[q] = R[q][j];
-    }
-  }
-}
-template <int B, int K, int NQ>
-__device__ __forceinline__ void vr_put(float (&R)[NQ][K], const float (&z)[NQ], int c) {
-#pragma unroll
-  for (int jj = 0; jj < 8; jj++) {
-    const int j = 8 * B + jj < K ? 8 * B + jj : K - 1;
-    if ((c & 7) == jj) {
-#pragma unroll
-      for (int q = 0; q < NQ; q++) R[q][j] = z[q];
-    }
-  }
-}
-
-// f(integral_constant<B>) for the warp-uniform block index b < K / 8, so
-// that f sees B as a compile-time constant
-template <int V> struct IC { static constexpr int value = V; };
-template <int K, class F>
-__device__ __forceinline__ void vr_by_block(int b, F &&f) {
-  switch (b) {
-  case 0: f(IC<0>{}); break;
-  case 1: if constexpr (K > 8) f(IC<(K > 8 ? 1 : 0)>{}); break;
-  case 2: if constexpr (K > 16) f(IC<(K > 16 ? 2 : 0)>{}); break;
-  case 3: if constexpr (K > 24) f(IC<(K > 24 ? 3 : 0)>{}); break;
-  case 4: if constexpr (K > 32) f(IC<(K > 32 ? 4 : 0)>{}); break;
-  case 5: if constexpr (K > 40) f(IC<(K > 40 ? 5 : 0)>{}); break;
-  default: break;
-  }
-}
-
-template <int K>
-__global__ void __launch_bounds__(32 * RWPB, K > 40 ? 2 : (K > 32 ? 3 : 4)) k_eig_vec_r(EigArgs a, EigSplit sp, int u0, int nb) {
-  constexpr int NQ = (K + 31) / 32;
-  constexpr int LD = K + 1;
-  constexpr int TR = K / 8, TC = K / 4;
-  __shared__ float su[RWPB][K * LD];
-  __shared__ __align__(8) float2 sring[RWPB][64];
-  __shared__ float sv[RWPB][4 * K];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ub = blockIdx.x * RWPB + warp;
-  if (ub >= nb) return;
-  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
-  if (a.nkept[unit] <= 0) return;
-  const int total = sp.logn[ub];
-  if (total < 0) return;   // -1: no convergence (status set by k_eig_ql); -2: k_eig_vec
-  const int k = a.k;
-  float *U = su[warp];
-  float2 *ring = sring[warp];
-  float *fl = sv[warp], *pv = fl + K, *wv = pv + K, *bv = wv + K;
-  // rows lane + 32 q of Q (row-major from the first stage)
-  float R[NQ][K];
-  {
-    const float *Q = sp.Q + (size_t)ub * k * k;
-#pragma unroll
-    for (int q = 0; q < NQ; q++) {
-      const int r = lane + 32 * q;
-#pragma unroll
-      for (int c = 0; c < K; c++) R[q][c] = (r < k && c < k) ? Q[(size_t)r * k + c] : 0.0f;
-    }
-  }
-  // ---- replay the rotations: V = Q Z
-  int bad = 0;
-  {
-    // the log in chunks of 32 entries (lane j: entry 32 t + j): chunks
-    // t .. t + 3 are in flight in pre0..pre3 (chunk t in pre[t % 4]) while
-    // the ring holds the two before
-    const float2 *lg = sp.log + (size_t)ub * sp.cap;
-    auto fetch = [&](int t) {
-      const int idx = 32 * t + lane;
-      return idx < total ? lg[idx] : make_float2(0.0f, 0.0f);
-    };
-    float2 pre0 = fetch(0), pre1 = fetch(1), pre2 = fetch(2), pre3 = fetch(3);
-    int loaded = 0;   // log entries [0, loaded) have been copied to the ring
-    auto ensure = [&](int upto) {   // warp-uniform
-      if (loaded >= upto) return;
-      __syncwarp();
-      do {
-        const int t = loaded >> 5;
-        float2 *dst = ring + ((loaded + lane) & 63);
-        switch (t & 3) {
-        case 0: *dst = pre0; pre0 = fetch(t + 4); break;
-        case 1: *dst = pre1; pre1 = fetch(t + 4); break;
-        case 2: *dst = pre2; pre2 = fetch(t + 4); break;
-        default: *dst = pre3; pre3 = fetch(t + 4); break;
-        }
-        loaded += 32;
-      } while (loaded < upto);
-      __syncwarp();
-    };
-    int pidx = 0;
-    while (pidx < total) {
-      ensure(pidx + 1);
-      const float2 h = ring[pidx & 63];
-      pidx++;
-      const int m = __float_as_int(h.x), cnt = __float_as_int(h.y);
-      if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + cnt > total) { bad |= 32; break; }   // malformed log
-      if (cnt == 0) continue;
-      const int lo = m - cnt, e0 = pidx + m - 1;   // the rotation on columns (i, i+1) is entry e0 - i
-      float z[NQ];
-      vr_by_block<K>(m >> 3, [&](auto BB) { vr_get<decltype(BB)::value, K, NQ>(R, z, m); });
-      for (int b = (m - 1) >> 3; b >= (lo >> 3); b--) {
-        ensure(e0 - max(8 * b, lo) + 1);
-        vr_by_block<K>(b, [&](auto BB) { vr_block<decltype(BB)::value, K, NQ>(R, z, m, lo, e0, ring); });
-      }
-      vr_by_block<K>(lo >> 3, [&](auto BB) { vr_put<decltype(BB)::value, K, NQ>(R, z, lo); });
-      pidx += cnt;
-    }
-  }
-  // ---- spectral functions (src/letkf_core.F90:111-113, :128-131): fl holds
-  // sqrt(sqrt((k-1)/lambda)), pv first 1/lambda
-  const float *lam = sp.lam + (size_t)ub * k;
-  const float *G = a.G + (size_t)unit * packed_size(k);
-  for (int l = lane; l < K; l += 32) {
-    float f = 0.0f, g = 0.0f, b = 0.0f;
-    if (l < k) {
-      const float lm = lam[l];
-      if (!(lm > 0.0f)) bad |= 2;
-      f = sqrtf(sqrtf((float)(k - 1) / lm));
-      g = 1.0f / lm;
-      b = G[k * (k + 1) / 2 + l];
-    }
-    fl[l] = f;
-    pv[l] = g;
-    bv[l] = b;
-  }
-  // V to shared memory (rows past k are zero)
-#pragma unroll
-  for (int q = 0; q < NQ; q++) {
-    const int r = lane + 32 * q;
-    if (r < K) {
-#pragma unroll
-      for (int c = 0; c < K; c++) U[r * LD + c] = R[q][c];
-    }
-  }
-  __syncwarp();
-  // p_l = (1/lambda_l) sum_r V[r][l] b_r, rows in order
-  for (int l = lane; l < K; l += 32) {
-    float acc = 0.0f;
-    for (int r = 0; r < k; r++) acc = __fmaf_rn(U[r * LD + l], bv[r], acc);
-    pv[l] = pv[l] * acc;
-  }
-  __syncwarp();
-  // wbar_i = sum_l V[i][l] p_l; U = V diag(fl) over V in shared memory
-#pragma unroll
-  for (int q = 0; q < NQ; q++) {
-    const int r = lane + 32 * q;
-    float acc = 0.0f;
-#pragma unroll
-    for (int c = 0; c < K; c++)
-      if (c < k) acc = __fmaf_rn(R[q][c], pv[c], acc);
-    if (r < K) wv[r] = acc;
-    if (r < k && a.wbar) a.wbar[(size_t)unit * k + r] = acc;
-  }
-  __syncwarp();
-#pragma unroll
-  for (int q = 0; q < NQ; q++) {
-    const int r = lane + 32 * q;
-    if (r < K) {
-#pragma unroll
-      for (int c = 0; c < K; c++) U[r * LD + c] = __fmul_rn(R[q][c], fl[c]);
-    }
-  }
-  __syncwarp();
-  // T_ij = sum_l U[i][l] U[j][l] + wbar_i: rows TR rg .. +TR, columns TC cg .. +TC
-  const int rg = lane & 7, cg = lane >> 3;
-  float acc[TR][TC];
-#pragma unroll
-  for (int x = 0; x < TR; x++)
-#pragma unroll
-    for (int y = 0; y < TC; y++) acc[x][y] = 0.0f;
-  const float *ur = U + (TR * rg) * LD, *uc = U + (TC * cg) * LD;
-  for (int l = 0; l < k; l++) {
-    float xr[TR], yc[TC];
-#pragma unroll
-    for (int x = 0; x < TR; x++) xr[x] = ur[x * LD + l];
-#pragma unroll
-    for (int y = 0; y < TC; y++) yc[y] = uc[y * LD + l];
-#pragma unroll
-    for (int x = 0; x < TR; x++)
-#pragma unroll
-      for (int y = 0; y < TC; y++) acc[x][y] = __fmaf_rn(xr[x], yc[y], acc[x][y]);
-  }
-  float *Tout = a.T + (size_t)unit * k * k;
-#pragma unroll
-  for (int x = 0; x < TR; x++) {
-    const int i = TR * rg + x;
-    if (i < k) {
-      const float wi = wv[i];
-#pragma unroll
-      for (int y = 0; y < TC; y++) {
-        const int j = TC * cg + y;
-        if (j < k) Tout[(size_t)i * k + j] = acc[x][y] + wi;
-      }
-    }
-  }
   bad = __reduce_or_sync(0xffffffffu, bad);
   if (bad && a.flag_list) {
     if (lane == 0) sp.logn[ub] = -1;   // k_eig_flag hands the unit to the FP64 re-solve
@@ -1471,20 +1224,6 @@ static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSpli
   return cudaGetLastError();
 }
 
-static cudaError_t launch_vec_r(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
-  const int grid = (nb + RWPB - 1) / RWPB;
-  switch ((a.k + 7) & ~7) {
-  case 8: k_eig_vec_r<8><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
-  case 16: k_eig_vec_r<16><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
-  case 24: k_eig_vec_r<24><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
-  case 32: k_eig_vec_r<32><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
-  case 40: k_eig_vec_r<40><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
-  case 48: k_eig_vec_r<48><<<grid, 32 * RWPB, 0, st>>>(a, sp, u0, nb); break;
-  default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
 template <int NQ, int NW, bool kPackedTri>
 static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart,
                                   int ucount, int *launches) {
@@ -1514,16 +1253,8 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
     if (kPackedTri) k_eig_trip<NW><<<(nb + wpt - 1) / wpt, tht, smt, st>>>(a, sp, wpt, u0, nb);
     else if ((e = launch_tri_r(st, a, sp, u0, nb)) != cudaSuccess) return e;
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
-    if (!kPackedTri && NW == 1) {
-      // rows of V in registers; units whose rotation log overflowed re-run
-      // their QL in k_eig_vec
-      if ((e = launch_vec_r(st, a, sp, u0, nb)) != cudaSuccess) return e;
-      k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb, 1);
-      (*launches) += 4;
-    } else {
-      k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb, 0);
-      (*launches) += 3;
-    }
+    k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    (*launches) += 3;
     if (a.flag_list) {
       k_eig_flag<<<(nb + 7) / 8, 256, 0, st>>>(a, sp, u0, nb);
       (*launches)++;
