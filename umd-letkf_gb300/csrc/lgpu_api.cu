@@ -117,6 +117,11 @@ struct lgpu_handle {
   int auto_choice = 0;   // AUTO: the Gram variant measured faster (0 = not yet measured)
   int gram_nseg = 1;     // most accumulation segments of a tile in the last batched Gram
   std::vector<int> h_tile_off;       // tile stream offsets of the last batched Gram (read back)
+  // page-locked landing areas of the run's small device-to-host reads: a
+  // pageable destination would queue them behind a bound state's upload
+  int *pin_off = nullptr;            // tile stream offsets
+  size_t pin_off_n = 0;
+  int *pin_scr = nullptr;            // [0..3] status words, [4] FP64 re-solve count
   std::vector<TcWork> h_tc_work;     // its accumulation segments
   std::vector<TcSegTile> h_tc_seg;   // its tiles with more than one segment
   int tc_cull = -1;      // batched Gram producers: 1 with the warp-level cull, 0 without, -1 not yet measured
@@ -278,6 +283,7 @@ int lgpu_create(int device, lgpu_handle **out) {
   for (auto &row : h->ev_down)
     for (auto &ev : row)
       if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  if (cudaMallocHost(&h->pin_scr, 64 * sizeof(int)) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   build_geom(h->geom, h->ncell);
   if (h->buf[B_GEOM].ensure(sizeof(IndexGeom)) != cudaSuccess ||
       cudaMemcpy(h->buf[B_GEOM].p, &h->geom, sizeof(IndexGeom), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -296,6 +302,8 @@ void lgpu_destroy(lgpu_handle *h) {
   if (h->dst) cudaStreamSynchronize(h->dst);
   for (auto &b : h->buf) b.release();
   learn_free(h);
+  if (h->pin_off) cudaFreeHost(h->pin_off);
+  if (h->pin_scr) cudaFreeHost(h->pin_scr);
   for (auto &ev : h->ev) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_in) if (ev) cudaEventDestroy(ev);
   for (auto &ev : h->ev_tune) if (ev) cudaEventDestroy(ev);
@@ -916,11 +924,18 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
      "tile count");
   // the stream offsets size the record buffer and split each tile's stream
   // into accumulation segments
-  h->h_tile_off.assign((size_t)ts.ntiles + 1, 0);
-  CK(cudaMemcpyAsync(h->h_tile_off.data(), (*ts.off).as<int>(), sizeof(int) * ((size_t)ts.ntiles + 1),
-                     cudaMemcpyDeviceToHost, st),
+  if (h->pin_off_n < (size_t)ts.ntiles + 1) {
+    if (h->pin_off) cudaFreeHost(h->pin_off);
+    h->pin_off = nullptr;
+    h->pin_off_n = 0;
+    CK(cudaMallocHost(&h->pin_off, sizeof(int) * ((size_t)ts.ntiles + 1)), "alloc stream offsets");
+    h->pin_off_n = (size_t)ts.ntiles + 1;
+  }
+  CK(cudaMemcpyAsync(h->pin_off, (*ts.off).as<int>(), sizeof(int) * ((size_t)ts.ntiles + 1), cudaMemcpyDeviceToHost,
+                     st),
      "D2H stream offsets");
   CK(cudaStreamSynchronize(st), "stream size sync");
+  h->h_tile_off.assign(h->pin_off, h->pin_off + ts.ntiles + 1);
   const int nchunk_total = h->h_tile_off[ts.ntiles];
   CK(h->buf[B_TILEREC].ensure(std::max<size_t>(16, (size_t)nchunk_total * record_bytes(k))), "alloc tile streams");
   CK(launch_tile_fill(st, ts.ntiles, (*ts.par).as<TilePar>(), h->buf[B_GEOM].as<IndexGeom>(), os, k, kp,
@@ -1236,11 +1251,12 @@ static int solver_run(lgpu_handle *h) {
     }
   }
   CK(cudaEventRecord(h->ev[5], st), "event");
-  int stat4[4] = {0, 0, 0, 0};
-  int nflag = 0;
+  int *stat4 = h->pin_scr;
+  stat4[4] = 0;
   CK(cudaMemcpyAsync(stat4, h->buf[B_STATUS].p, 16, cudaMemcpyDeviceToHost, st), "D2H status");
-  if (ea.flag_n) CK(cudaMemcpyAsync(&nflag, ea.flag_n, 4, cudaMemcpyDeviceToHost, st), "D2H flag count");
+  if (ea.flag_n) CK(cudaMemcpyAsync(stat4 + 4, ea.flag_n, 4, cudaMemcpyDeviceToHost, st), "D2H flag count");
   CK(cudaStreamSynchronize(st), "solver_run");
+  const int nflag = stat4[4];
   if (bound) CK(cudaStreamSynchronize(h->cst), "solver_run copies");
   if (bound) CK(cudaStreamSynchronize(h->dst), "solver_run copies");
   float ms[3];
@@ -2225,14 +2241,15 @@ static int learned_run(lgpu_handle *h) {
   CK(launch_update(st, ua, &launches), "update kernel");
   CK(cudaEventRecord(h->ev_chunk[0][2], st), "event");
   CK(cudaEventRecord(h->ev[5], st), "event");
-  int stat4[4] = {0, 0, 0, 0};
-  float jacc[4] = {0, 0, 0, 0};
-  int nflag = 0;
+  int *stat4 = h->pin_scr;
+  float *jacc = reinterpret_cast<float *>(h->pin_scr + 8);
+  stat4[4] = 0;
   CK(cudaMemcpyAsync(stat4, h->buf[B_STATUS].p, 16, cudaMemcpyDeviceToHost, st), "D2H status");
   if (h->prec == LGPU_PREC_FP32_RESOLVE)
-    CK(cudaMemcpyAsync(&nflag, h->buf[B_FLAGLIST].p, 4, cudaMemcpyDeviceToHost, st), "D2H flag count");
+    CK(cudaMemcpyAsync(stat4 + 4, h->buf[B_FLAGLIST].p, 4, cudaMemcpyDeviceToHost, st), "D2H flag count");
   CK(cudaMemcpyAsync(jacc, L->jacc.p, 16, cudaMemcpyDeviceToHost, st), "D2H judge");
   CK(cudaStreamSynchronize(st), "solver_run");
+  const int nflag = stat4[4];
   float ms[3];
   for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]), "timing");
   float le[5];
