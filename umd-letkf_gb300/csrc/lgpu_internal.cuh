@@ -568,7 +568,8 @@ struct UpdateArgs {
 };
 cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches);
 // the same update on the tensor cores (lgpu_update_tc.cu): k a multiple of
-// 4, k <= 128, ns <= 128, at most 2 groups; cudaErrorNotSupported otherwise
+// 4 with 64 < k <= 128, ns <= 128, at most 2 groups; cudaErrorNotSupported
+// otherwise
 cudaError_t launch_update_tc(cudaStream_t st, const UpdateArgs &a, int *launches);
 
 // ---- weight-correction network of the learned form (lgpu_mlp.cu) ----

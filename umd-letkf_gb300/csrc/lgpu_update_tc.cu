@@ -6,8 +6,7 @@
 //
 // Persistent CTAs, one per SM, each walking the columns
 // blockIdx.x, blockIdx.x + gridDim.x, ...; warp roles:
-//   epilogue   4 warps, or (k <= 64) two groups of 4 taking alternate
-//              columns: thread s owns slab s (TMEM lane s); reads its row
+//   epilogue   4 warps: thread s owns slab s (TMEM lane s); reads its row
 //              of X_b T_g from TMEM, runs recenter / mean clip / RTPS / RTPP
 //              / multiplicative inflation / member bounds / spread in the
 //              order and arithmetic of k_update_rows, writes the analysis
@@ -38,16 +37,10 @@ constexpr int UKC = 32;                        // members per K chunk (4 MMA ste
 constexpr uint32_t UCMB = 128;                 // bytes per core matrix (8 rows x 16 B)
 constexpr uint32_t USBO = (UKC / 4) * UCMB;    // bytes per 8-row group of a chunk operand
 constexpr uint32_t UAB = UM * UKC * 4;         // bytes of one A chunk part (hi or lo)
-constexpr int NPROD = 4;                       // producer warps
+constexpr int NEPI = 4, NPROD = 4;             // epilogue / producer warps
+constexpr int LOAD_WARP = NEPI + NPROD, MMA_WARP = LOAD_WARP + 1;
+constexpr int UNT = 32 * (MMA_WARP + 1);
 constexpr int URS = 4, UOS = 3;                // most raw / operand stages
-// epilogue warps: two groups of 4 taking alternate columns (one TMEM
-// accumulator buffer each) while a member row fits the registers, else one
-template <int NP> struct URoles {
-  static constexpr int NEPI = NP <= 64 ? 8 : 4;
-  static constexpr int NGRP = NEPI / 4;
-  static constexpr int LOAD_WARP = NEPI + NPROD, MMA_WARP = LOAD_WARP + 1;
-  static constexpr int NT = 32 * (MMA_WARP + 1);
-};
 
 struct UtcBars {
   unsigned long long raw_full[URS], raw_empty[URS], op_full[UOS], op_empty[UOS];
@@ -79,9 +72,7 @@ __device__ __forceinline__ int utc_group(const UpdateArgs &a, int lev, int mld) 
 }
 
 template <int NP>
-__global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
-  constexpr int NEPI = URoles<NP>::NEPI, NGRP = URoles<NP>::NGRP;
-  constexpr int LOAD_WARP = URoles<NP>::LOAD_WARP, MMA_WARP = URoles<NP>::MMA_WARP;
+__global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ __align__(8) UtcBars S;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -105,7 +96,7 @@ __global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, U
     }
     for (int i = 0; i < 2; i++) {
       tc::mbar_init(B(S.acc_full[i]), 1);
-      tc::mbar_init(B(S.acc_empty[i]), 4);   // the 4 warps of the group that drains buffer i
+      tc::mbar_init(B(S.acc_empty[i]), NEPI);
     }
     tc::mbar_init(B(S.done), 1);
     S.fault = 0;
@@ -119,9 +110,7 @@ __global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, U
 
   if (wid < NEPI) {
     // ============================================================ epilogue
-    // group grp drains the accumulator buffer of the columns n with
-    // n % NGRP == grp (NGRP = 2: buffer grp; NGRP = 1: buffer n % 2)
-    const int s = tid & 127, grp = wid >> 2;
+    const int s = tid;
     const float kf = (float)k, km1 = (float)(k - 1);
     // the slab's variable, level and bounds (the same for every column)
     int v = 0, lev = 0;
@@ -133,16 +122,16 @@ __global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, U
       lb = a.var_lb[v];
       ub = a.var_ub[v];
     }
-    int n = 0, ii = 0;
+    int n = 0;
     int nxt = act_of(blockIdx.x);
-    for (int i = blockIdx.x; i < a.ncols; i += gridDim.x, ii++) {
+    for (int i = blockIdx.x; i < a.ncols; i += gridDim.x) {
       const int col = a.col0 + i;
       const int act = nxt;
       nxt = act_of(i + gridDim.x);
       const size_t cbase = (size_t)col * ns * k;
       const size_t ms = (size_t)col * ns + s;
       if (act < 0) {   // src/letkf_solver.F90:207: the block leaves unchanged
-        if (ii % NGRP == grp && s < ns) {
+        if (s < ns) {
           if (a.ana != a.bkg) {
             const float4 *src = reinterpret_cast<const float4 *>(a.bkg + cbase + (size_t)s * k);
             float4 *dst = reinterpret_cast<float4 *>(a.ana + cbase + (size_t)s * k);
@@ -153,11 +142,9 @@ __global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, U
         }
         continue;
       }
-      const int mine = n % NGRP == grp;
       const int ab = n & 1;
       const int par = (n >> 1) & 1;
       n++;
-      if (!mine) continue;
       // the column's scalars, loaded while the products complete
       int g = 0;
       bool has = false;
@@ -173,7 +160,7 @@ __global__ void __launch_bounds__(URoles<NP>::NT, 1) k_update_tc(UpdateArgs a, U
       // the slab's row of X_b T_g (TMEM loads are warp-wide: every group is
       // read, the thread keeps its own)
       float x[NP];
-      const uint32_t tb = tmem + ((uint32_t)((wid & 3) * 32) << 16) + (uint32_t)(ab * G * NP);
+      const uint32_t tb = tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)(ab * G * NP);
 #pragma unroll
       for (int c0 = 0; c0 < NP; c0 += 16) {
         float vv[16];
@@ -409,14 +396,17 @@ template <int NP>
 cudaError_t launch_np(cudaStream_t st, const UpdateArgs &a, const UtcCfg &cf, size_t smem, int grid) {
   cudaError_t e = cudaFuncSetAttribute(k_update_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_update_tc<NP><<<grid, URoles<NP>::NT, smem, st>>>(a, cf);
+  k_update_tc<NP><<<grid, UNT, smem, st>>>(a, cf);
   return cudaGetLastError();
 }
 
 }  // namespace
 
+// Used above k = 64: at k = 40 the CUDA-core form (k_update_rows) streams
+// the columns faster (C2: 2.6 against 4.4 ms), at k = 100 this form wins
+// (C4: 63 against 70 ms).
 bool update_tc_eligible(const UpdateArgs &a, size_t *smem_out) {
-  if (a.k < 4 || a.k > 128 || (a.k & 3) || a.ns < 1 || a.ns > UM || a.groups < 1 || a.groups > 2) return false;
+  if (a.k <= 64 || a.k > 128 || (a.k & 3) || a.ns < 1 || a.ns > UM || a.groups < 1 || a.groups > 2) return false;
   const int NP = (a.k + 15) & ~15;
   const uint32_t xbytes = (uint32_t)a.ns * a.k * 4, tbytes = (uint32_t)a.groups * a.k * a.k * 4;
   const uint32_t toff = (xbytes + 127) & ~127u;
@@ -466,10 +456,6 @@ cudaError_t launch_update_tc(cudaStream_t st, const UpdateArgs &a, int *launches
   const int grid = a.ncols < nsm ? a.ncols : nsm;
   cudaError_t e;
   switch (NP) {
-  case 16: e = launch_np<16>(st, a, cf, smem, grid); break;
-  case 32: e = launch_np<32>(st, a, cf, smem, grid); break;
-  case 48: e = launch_np<48>(st, a, cf, smem, grid); break;
-  case 64: e = launch_np<64>(st, a, cf, smem, grid); break;
   case 80: e = launch_np<80>(st, a, cf, smem, grid); break;
   case 96: e = launch_np<96>(st, a, cf, smem, grid); break;
   case 112: e = launch_np<112>(st, a, cf, smem, grid); break;

@@ -29,6 +29,8 @@ sections a reference YAML configuration would carry for them.
             of both signs) and both surface-id lists set (sat_obs = [3],
             sat_plats = [2]: the SSH swath obs are surface obs, the SST swath
             obs of the same platform are not), mixed-layer split on T
+  c4mid     c4's 50 levels and k = 100 on a 240x120 grid (profiling-sized:
+            the same slabs and members per column)
   c2small / c1small / c3small / c4small  reduced grids with the same
             generators for fast tests
 """
@@ -98,6 +100,10 @@ WORKLOADS = {
                   learn=dict(stride=4, hidden=512, judge_frac=0.02, gate_frac=0.05, sample_frac=0.3,
                              train_cap=300000, seed=5),
                   cycles=dict(train=2, u=0.5, kappa=1.0e3, dt=21600.0, epochs=2, batch=1024, lr=1e-3)),
+    "c4mid": dict(gen=dict(workload="c4", nx=240, ny=120, n_obs=40000),
+                  localization={"class": "loc_novrt",
+                                "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
+                  solver={}),
     "c4small": dict(gen=dict(workload="c4", nx=180, ny=90, nz=5, n_obs=40000),
                     localization={"class": "loc_novrt",
                                   "hzloc": {"type": "linearinterp_lat", "value": [{"lat": 0.0, "radius": 150.0e3}]}},
