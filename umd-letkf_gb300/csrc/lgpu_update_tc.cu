@@ -122,12 +122,32 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
       lb = a.var_lb[v];
       ub = a.var_ub[v];
     }
+    // the per-column scalars run two columns ahead: the active index and
+    // mixed-layer level of column j + 2, then the group's kept count and the
+    // slab's background mean and spread of column j + 1
+    const int stride = gridDim.x;
+    auto mld_of = [&](int i) { return i < a.ncols ? a.cp[a.col0 + i].mld : 0; };
+    auto ms_of = [&](int i) { return (size_t)(a.col0 + (i < a.ncols ? i : 0)) * ns + (s < ns ? s : 0); };
+    auto group_of = [&](int act, int mld) { return act >= 0 ? utc_group(a, lev, mld) : 0; };
+    auto kept_of = [&](int act, int g) { return (act >= 0 && s < ns && g < G) ? a.nkept[(size_t)act * G + g] : 0; };
+    int act0 = act_of(blockIdx.x), g0 = group_of(act0, mld_of(blockIdx.x));
+    int nk0 = kept_of(act0, g0);
+    float mb0 = a.mean_b[ms_of(blockIdx.x)], sb0 = a.sprd_b[ms_of(blockIdx.x)];
+    int act1 = act_of(blockIdx.x + stride), mld1 = mld_of(blockIdx.x + stride);
     int n = 0;
-    int nxt = act_of(blockIdx.x);
-    for (int i = blockIdx.x; i < a.ncols; i += gridDim.x) {
+    for (int i = blockIdx.x; i < a.ncols; i += stride) {
       const int col = a.col0 + i;
-      const int act = nxt;
-      nxt = act_of(i + gridDim.x);
+      const int act = act0, g = g0;
+      const bool has = s < ns && g < G && nk0 > 0;
+      const float mb = mb0, sb = sb0;
+      // column j + 1: kept count, mean, spread; column j + 2: index, level
+      g0 = group_of(act1, mld1);
+      nk0 = kept_of(act1, g0);
+      mb0 = a.mean_b[ms_of(i + stride)];
+      sb0 = a.sprd_b[ms_of(i + stride)];
+      act0 = act1;
+      act1 = act_of(i + 2 * stride);
+      mld1 = mld_of(i + 2 * stride);
       const size_t cbase = (size_t)col * ns * k;
       const size_t ms = (size_t)col * ns + s;
       if (act < 0) {   // src/letkf_solver.F90:207: the block leaves unchanged
@@ -137,24 +157,14 @@ __global__ void __launch_bounds__(UNT, 1) k_update_tc(UpdateArgs a, UtcCfg cf) {
             float4 *dst = reinterpret_cast<float4 *>(a.ana + cbase + (size_t)s * k);
             for (int q = 0; q < (k >> 2); q++) dst[q] = src[q];
           }
-          a.mean_a[ms] = a.mean_b[ms];
-          a.sprd_a[ms] = a.sprd_b[ms];
+          a.mean_a[ms] = mb;
+          a.sprd_a[ms] = sb;
         }
         continue;
       }
       const int ab = n & 1;
       const int par = (n >> 1) & 1;
       n++;
-      // the column's scalars, loaded while the products complete
-      int g = 0;
-      bool has = false;
-      float mb = 0.0f, sb = 0.0f;
-      if (s < ns) {
-        g = utc_group(a, lev, a.cp[col].mld);
-        mb = a.mean_b[ms];
-        sb = a.sprd_b[ms];
-        has = g < G && a.nkept[(size_t)act * G + g] > 0;
-      }
       if (!tc::mbar_wait(B(S.acc_full[ab]), par)) { S.fault = 1; break; }
       tc::fence_after();
       // the slab's row of X_b T_g (TMEM loads are warp-wide: every group is
