@@ -83,7 +83,7 @@ struct lgpu_handle {
   cudaStream_t st = nullptr;
   cudaStream_t cst = nullptr;      // host<->device copies of a bound state
   cudaEvent_t ev[8] = {};
-  cudaEvent_t ev_in[2] = {};       // bound state: mean/spread, members uploaded
+  cudaEvent_t ev_in[2] = {};       // bound state: mean/spread uploaded; members' upload started
   cudaEvent_t ev_tune[3] = {};     // AUTO: timing of the two Gram forms
   cudaEvent_t ev_cull[3] = {};     // batched Gram: timing of its two producer forms
   // per column chunk: eigensolve start, update start, update end, FP64 eigensolve start
@@ -92,6 +92,7 @@ struct lgpu_handle {
   cudaEvent_t ev_up[2] = {};         // bound state: background upload (copy stream)
   cudaEvent_t ev_down[kOutChunks][2] = {};   // bound state: analysis download per chunk (download stream)
   cudaEvent_t ev_upc[kOutChunks] = {};       // bound state: background of column chunk c uploaded
+  cudaEvent_t ev_gram_done = nullptr;        // bound state: the Gram has run (the members' upload starts)
   cudaStream_t dst = nullptr;                // bound state: analysis downloads (uploads run on cst)
   float obs_h2d_ms = 0.0f, obs_host_ms = 0.0f;
   float *bound_state = nullptr, *bound_mean = nullptr, *bound_sprd = nullptr;   // caller arrays (in place)
@@ -265,10 +266,11 @@ int lgpu_create(int device, lgpu_handle **out) {
   if (cudaStreamCreateWithFlags(&h->dst, cudaStreamNonBlocking) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_upc)
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  if (cudaEventCreateWithFlags(&h->ev_gram_done, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev)
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
-  for (auto &ev : h->ev_in)
-    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
+  for (auto &ev : h->ev_in)   // also time the background upload
+    if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_tune)
     if (cudaEventCreate(&ev) != cudaSuccess) { delete h; return LGPU_ERR_CUDA; }
   for (auto &ev : h->ev_cull)
@@ -318,6 +320,7 @@ void lgpu_destroy(lgpu_handle *h) {
   if (h->cst) cudaStreamDestroy(h->cst);
   if (h->dst) cudaStreamDestroy(h->dst);
   for (auto &ev : h->ev_upc) if (ev) cudaEventDestroy(ev);
+  if (h->ev_gram_done) cudaEventDestroy(h->ev_gram_done);
   delete h;
 }
 
@@ -776,26 +779,14 @@ static int prepare_run(lgpu_handle *h, ObsSorted &os, int &launches) {
   const bool bound = h->bound_state != nullptr;
   CK(cudaEventRecord(h->ev[0], st), "event");
   if (bound) {
-    // background upload on the copy stream, concurrent with the index,
-    // search, Gram and eigensolve stages (the update waits for it)
-    const size_t nx = (size_t)h->ncol * ns * k, nm = (size_t)h->ncol * ns;
+    // the background mean and spread first (the column parameters read the
+    // mean); the members follow the Gram (upload_members)
+    const size_t nm = (size_t)h->ncol * ns;
     CK(cudaStreamWaitEvent(h->cst, h->ev[0], 0), "stream wait");
     CK(cudaEventRecord(h->ev_up[0], h->cst), "event");
     CK(cudaMemcpyAsync(h->buf[B_MEANB].p, h->bound_mean, nm * 4, cudaMemcpyHostToDevice, h->cst), "H2D mean");
     CK(cudaMemcpyAsync(h->buf[B_SPRDB].p, h->bound_sprd, nm * 4, cudaMemcpyHostToDevice, h->cst), "H2D sprd");
     CK(cudaEventRecord(h->ev_in[0], h->cst), "event");
-    // the members in the column chunks of the update, each with its event
-    const int per = (h->ncol + kOutChunks - 1) / kOutChunks;
-    for (int c = 0; c < kOutChunks; c++) {
-      const size_t c0 = (size_t)std::min(h->ncol, c * per), c1 = (size_t)std::min(h->ncol, (c + 1) * per);
-      if (c1 > c0)
-        CK(cudaMemcpyAsync(h->buf[B_BKG].as<float>() + c0 * ns * k, h->bound_state + c0 * ns * k,
-                           (c1 - c0) * ns * k * 4, cudaMemcpyHostToDevice, h->cst), "H2D state");
-      CK(cudaEventRecord(h->ev_upc[c], h->cst), "event");
-    }
-    (void)nx;
-    CK(cudaEventRecord(h->ev_in[1], h->cst), "event");
-    CK(cudaEventRecord(h->ev_up[1], h->cst), "event");
   }
   // ---- observation index (kd_init counterpart) ----
   CK(launch_obs_index(st, h->nobs, k, kp, h->buf[B_OLAT].as<float>(), h->buf[B_OLON].as<float>(),
@@ -1096,6 +1087,29 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
 
 static int solver_run(lgpu_handle *h);
 
+// A bound state's members, uploaded on the copy stream in the column chunks
+// of the update (each chunk with its event), once `after` has been reached on
+// the compute stream.  They are issued after the Gram: host<->device copies
+// in flight during the tile-stream and Gram kernels slowed them by 12 to
+// 108 ms at C2 (their bulk copies and gathers are latency-bound), while the
+// eigensolve and update ran at full speed beside the same copies.
+static int upload_members(lgpu_handle *h, cudaEvent_t after) {
+  const int ns = h->ns, k = h->k;
+  CK(cudaEventRecord(after, h->st), "event");
+  CK(cudaStreamWaitEvent(h->cst, after, 0), "stream wait");
+  CK(cudaEventRecord(h->ev_in[1], h->cst), "event");
+  const int per = (h->ncol + kOutChunks - 1) / kOutChunks;
+  for (int c = 0; c < kOutChunks; c++) {
+    const size_t c0 = (size_t)std::min(h->ncol, c * per), c1 = (size_t)std::min(h->ncol, (c + 1) * per);
+    if (c1 > c0)
+      CK(cudaMemcpyAsync(h->buf[B_BKG].as<float>() + c0 * ns * k, h->bound_state + c0 * ns * k,
+                         (c1 - c0) * ns * k * 4, cudaMemcpyHostToDevice, h->cst), "H2D state");
+    CK(cudaEventRecord(h->ev_upc[c], h->cst), "event");
+  }
+  CK(cudaEventRecord(h->ev_up[1], h->cst), "event");
+  return LGPU_OK;
+}
+
 // letkf_solver_run (src/letkf_solver.F90:150-389)
 int lgpu_solver_run(lgpu_handle *h) {
   if (!h) return LGPU_ERR_ARG;
@@ -1176,6 +1190,7 @@ static int solver_run(lgpu_handle *h) {
   }
   h->used_tc = choice == LGPU_VARIANT_BATCHED_TC;
   CK(cudaEventRecord(h->ev[3], st), "event");
+  if (bound && (rc = upload_members(h, h->ev_gram_done)) != LGPU_OK) return rc;
   // ---- eigensolve + transform, update + epilogue, in column chunks ----
   // A bound state is processed in kOutChunks column chunks: chunk c's
   // analysis is downloaded into the caller's arrays while the eigensolve and
@@ -1291,7 +1306,10 @@ static int solver_run(lgpu_handle *h) {
   h->tim.span_ms = h->tim.total_ms;
   if (bound) {
     const long long nx = (long long)h->ncol * ns * k, nm = (long long)h->ncol * ns;
-    CK(cudaEventElapsedTime(&h->tim.h2d_state_ms, h->ev_up[0], h->ev_up[1]), "timing");
+    float tms = 0.0f, tmm = 0.0f;   // mean and spread, then the members
+    CK(cudaEventElapsedTime(&tms, h->ev_up[0], h->ev_in[0]), "timing");
+    CK(cudaEventElapsedTime(&tmm, h->ev_in[1], h->ev_up[1]), "timing");
+    h->tim.h2d_state_ms = tms + tmm;
     for (int c = 0; c < nrec; c++) {
       float td = 0.0f;
       CK(cudaEventElapsedTime(&td, h->ev_down[c][0], h->ev_down[c][1]), "timing");
