@@ -149,7 +149,7 @@ typedef struct lgpu_timings {
   /* host link and host time (the end-to-end view of a run) */
   float h2d_obs_ms;      /* the last lgpu_set_obs: observation upload (CUDA events around its copies) */
   float host_obs_ms;     /* the last lgpu_set_obs: host wall time of the call */
-  float h2d_state_ms;    /* bound state: background upload, on the copy stream (0 otherwise) */
+  float h2d_state_ms;    /* bound state: background upload (mean and spread, then the members), on the copy stream (0 otherwise) */
   float d2h_state_ms;    /* bound state: analysis download, summed over the column chunks (0 otherwise) */
   float span_ms;         /* run start to the end of the last analysis download (total_ms without a bound state) */
   float host_run_ms;     /* host wall time of lgpu_solver_run */
@@ -243,11 +243,13 @@ int lgpu_get_state(lgpu_handle *h, float *state, float *mean, float *sprd);
  * state_ij, state_mean_ij, state_sprd_ij with the analysis): binds the
  * caller's arrays (layout and arguments as lgpu_set_state).  Each following
  * lgpu_solver_run reads the background from them and writes the analysis
- * back into them before it returns.  The upload of the members runs on a
- * copy stream concurrently with the search, Gram and eigensolve stages; the
- * update runs in column chunks whose analysis is downloaded while the next
- * chunks are computed.  Page-locked arrays (lgpu_host_alloc) give full link
- * speed.  The arrays must stay allocated and untouched by the caller while
+ * back into them before it returns.  The background mean and spread are
+ * uploaded first; the members follow on a copy stream once the Gram has run,
+ * concurrently with the eigensolve (host<->device copies in flight slow the
+ * tile-stream and Gram kernels, not the eigensolve or update); the
+ * eigensolve and update run in column chunks whose update waits for its
+ * members and whose analysis is downloaded while the next chunks are
+ * computed.  Page-locked arrays (lgpu_host_alloc) give full link speed.  The arrays must stay allocated and untouched by the caller while
  * lgpu_solver_run executes; lgpu_set_state or another lgpu_bind_state
  * releases them. */
 int lgpu_bind_state(lgpu_handle *h, int k, int ns, float *state, float *mean, float *sprd, int nvars,
