@@ -904,7 +904,12 @@ struct TileSet {
   DevBuf *cols, *par, *n, *off;
 };
 
-static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet &ts, int &launches) {
+static int upload_members(lgpu_handle *h, cudaEvent_t after);
+
+// start_upload: a bound state's members start uploading once the tile fill is
+// launched (after the tile-stream offsets are read back), beside the Gram
+static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet &ts, int &launches,
+                             bool start_upload) {
   cudaStream_t st = h->st;
   const int k = h->k, kp = h->kp, G = h->loc.groups;
   CK(launch_tile_prep(st, ts.ntiles, (*ts.cols).as<int>(), h->buf[B_CP].as<ColPar>(),
@@ -934,6 +939,10 @@ static int run_batched_tiles(lgpu_handle *h, const ObsSorted &os, const TileSet 
                       h->buf[B_STATUS].as<int>(), &launches),
      "tile fill");
   CK(cudaEventRecord(h->ev[6], st), "event");
+  if (start_upload) {
+    const int rc = upload_members(h, h->ev_gram_done);
+    if (rc != LGPU_OK) return rc;
+  }
   TcArgs ta;
   ta.ntiles = ts.ntiles;
   ta.groups = G;
@@ -1089,10 +1098,11 @@ static int solver_run(lgpu_handle *h);
 
 // A bound state's members, uploaded on the copy stream in the column chunks
 // of the update (each chunk with its event), once `after` has been reached on
-// the compute stream.  They are issued after the Gram: host<->device copies
-// in flight during the tile-stream and Gram kernels slowed them by 12 to
-// 108 ms at C2 (their bulk copies and gathers are latency-bound), while the
-// eigensolve and update ran at full speed beside the same copies.
+// the compute stream.  They start after the tile streams (batched Gram) or
+// after the Gram (plain): a large copy in flight while the run reads back the
+// tile-stream offsets delayed that small read, and with it the Gram's launch,
+// by 12 to 108 ms at C2; the Gram kernels, the eigensolve and the update ran
+// at full speed beside the same copies.
 static int upload_members(lgpu_handle *h, cudaEvent_t after) {
   const int ns = h->ns, k = h->k;
   CK(cudaEventRecord(after, h->st), "event");
@@ -1133,7 +1143,11 @@ static int solver_run(lgpu_handle *h) {
   // ---- search + localize + Gram ----
   // ---- Gram: the batched tensor-core form or the plain per-column form ----
   const TileSet grid_tiles{h->ntiles, &h->buf[B_TILECOLS], &h->buf[B_TILEPAR], &h->buf[B_TILEN], &h->buf[B_TILEOFF]};
-  auto run_batched = [&]() -> int { return run_batched_tiles(h, os, grid_tiles, launches); };
+  bool uploading = false;   // a bound state's members are on their way
+  auto run_batched = [&](bool start_upload) -> int {
+    uploading = start_upload && bound;
+    return run_batched_tiles(h, os, grid_tiles, launches, start_upload && bound);
+  };
   auto run_plain = [&]() -> int {
     GramArgs ga;
     ga.nunits = h->nunits;
@@ -1169,7 +1183,7 @@ static int solver_run(lgpu_handle *h) {
     CK(cudaEventRecord(h->ev_tune[0], st), "event");
     if ((rc = run_plain()) != LGPU_OK) return rc;
     CK(cudaEventRecord(h->ev_tune[1], st), "event");
-    if ((rc = run_batched()) != LGPU_OK) return rc;
+    if ((rc = run_batched(false)) != LGPU_OK) return rc;
     CK(cudaEventRecord(h->ev_tune[2], st), "event");
     CK(cudaEventSynchronize(h->ev_tune[2]), "tune sync");
     float tp = 0.0f, tb = 0.0f;
@@ -1182,15 +1196,14 @@ static int solver_run(lgpu_handle *h) {
     if (h->auto_choice == LGPU_VARIANT_PLAIN && (rc = run_plain()) != LGPU_OK) return rc;
     choice = h->auto_choice;
   } else if (choice == LGPU_VARIANT_BATCHED_TC) {
-    // the whole Gram at once (a bound state's background uploads meanwhile):
-    // launched per column chunk its tails cost more than the overlap gains
-    if ((rc = run_batched()) != LGPU_OK) return rc;
+    // the whole Gram at once (a bound state's members upload meanwhile)
+    if ((rc = run_batched(true)) != LGPU_OK) return rc;
   } else {
     if ((rc = run_plain()) != LGPU_OK) return rc;
   }
   h->used_tc = choice == LGPU_VARIANT_BATCHED_TC;
   CK(cudaEventRecord(h->ev[3], st), "event");
-  if (bound && (rc = upload_members(h, h->ev_gram_done)) != LGPU_OK) return rc;
+  if (bound && !uploading && (rc = upload_members(h, h->ev_gram_done)) != LGPU_OK) return rc;
   // ---- eigensolve + transform, update + epilogue, in column chunks ----
   // A bound state is processed in kOutChunks column chunks: chunk c's
   // analysis is downloaded into the caller's arrays while the eigensolve and
