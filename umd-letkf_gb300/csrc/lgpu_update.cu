@@ -411,17 +411,17 @@ cudaError_t launch_update(cudaStream_t st, const UpdateArgs &a, int *launches) {
   const size_t rbytes = ((size_t)a.ns * a.k + (size_t)a.groups * a.k * a.k) * sizeof(float);
   if (a.k % 4 == 0 && a.ns <= 256 && rbytes <= 200 * 1024) {
     const int k = a.k;
-    // above k = 32 two threads per slab (when the slabs fit one CTA)
-    const int tps = k > 32 && 2 * a.ns <= 256 ? 2 : 1;
+    // above k = 64 two threads per slab (when the slabs fit one CTA)
+    const int tps = k > 64 && 2 * a.ns <= 256 ? 2 : 1;
     const int nt = (tps * a.ns + 31) & ~31;
     auto kern = k <= 8    ? k_update_rows<8, 1>
                 : k <= 16 ? k_update_rows<16, 1>
                 : k <= 24 ? k_update_rows<24, 1>
                 : k <= 32 ? k_update_rows<32, 1>
-                : k <= 40 ? (tps == 2 ? k_update_rows<40, 2> : k_update_rows<40, 1>)
-                : k <= 48 ? (tps == 2 ? k_update_rows<48, 2> : k_update_rows<48, 1>)
-                : k <= 56 ? (tps == 2 ? k_update_rows<56, 2> : k_update_rows<56, 1>)
-                : k <= 64 ? (tps == 2 ? k_update_rows<64, 2> : k_update_rows<64, 1>)
+                : k <= 40 ? k_update_rows<40, 1>
+                : k <= 48 ? k_update_rows<48, 1>
+                : k <= 56 ? k_update_rows<56, 1>
+                : k <= 64 ? k_update_rows<64, 1>
                 : k <= 80 ? (tps == 2 ? k_update_rows<80, 2> : k_update_rows<80, 1>)
                 : k <= 96 ? (tps == 2 ? k_update_rows<96, 2> : k_update_rows<96, 1>)
                 : k <= 112 ? (tps == 2 ? k_update_rows<112, 2> : k_update_rows<112, 1>)
