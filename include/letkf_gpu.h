@@ -280,8 +280,7 @@ int lgpu_get_obslist(lgpu_handle *h, int ij, int group, int *idx, float *rloc, i
  * LGPU_ERR_CAPACITY.  All calls share that array, which keeps the last
  * call's contents (each call clears its counters and flags first): calls
  * that overlap on the GPU race and must be serialised by the caller.  The
- * first call on a device looks up the array's address; make it before any
- * stream capture. */
+ * first call on a device looks up the array's address. */
 #define LGPU_NOALLOC_MAX_LIST 262144
 int lgpu_get_obslist_noalloc(lgpu_handle *h, int ij, int group, int *idx, float *rloc, int cap,
                              int *n, int *ncand);

@@ -21,8 +21,7 @@
 //     (concurrent calls on several handles/threads of one device) race on
 //     that array and must be serialised by the caller;
 //   - the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current); make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress, with that device current).
 #include <mutex>
 #include <cstdio>
 
