@@ -63,7 +63,7 @@ constexpr int NPW = 16;        // producer warps: 0-7 weights, 8-15 features
 constexpr int MMA_WARP = NPW;
 constexpr int NT = 32 * (NPW + 1);
 constexpr int NPMAX = 432;     // features per pass
-constexpr int NSMAX = 3, NRMAX = 12;
+constexpr int NSMAX = 2, NRMAX = 6;
 constexpr uint32_t CMB = 128;                 // bytes per core matrix (8 rows x 16 B)
 constexpr uint32_t SBO = (KC / 4) * CMB;      // bytes per 8-row group (all K of the chunk)
 constexpr uint32_t WB = (TM / 8) * SBO;       // bytes per W operand copy
@@ -824,18 +824,17 @@ __global__ void k_tile_prep(int ntiles, const int *tile_cols, const ColPar *cp, 
   }
 }
 
-// Stage / ring depths: two operand stages and twelve record slots where they
-// fit, else two stages and six slots (k <= 128: 2 x 70 KB + 6 x 10.8 KB).  The
-// record ring is filled as far ahead as it reaches, so that the producers do
-// not wait on the copies: at k = 40 two stages with six slots made the Gram
-// 1.8 ms faster than three stages with three.
+// Stage / ring depths: two operand stages and six record slots (k <= 128:
+// 2 x 70 KB + 6 x 10.8 KB).  At k = 40 they made the Gram 1.8 ms faster than
+// three stages with three slots (the producers waited on the record copies);
+// twelve slots gained nothing more.
 void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem) {
   const size_t PB = (size_t)(np / 8) * SBO;
   const size_t stage = 2 * WB + 2 * PB;
   const size_t cb = record_bytes(k);
 
   *ns = 2;
-  *nr = 2 * stage + 12 * cb <= kSmemBudget ? 12 : 6;
+  *nr = 6;
   *smem = (size_t)*ns * stage + (size_t)*nr * cb;
 }
 
@@ -899,7 +898,9 @@ template <int LOC>
 static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) {
   int ns, nr;
   size_t smem;
-  gram_tc_config(a.k, a.np, &ns, &nr, &smem);
+  gram_tc_config(a.k, a.np, &ns, &nr, &smem);   // two stages, six record slots
+  (void)ns;
+  (void)nr;
   const long long per_pass = (long long)a.nwork * a.groups;
   if (per_pass * a.npass > 0x7fffffffLL) return cudaErrorInvalidValue;
   cudaError_t e;
@@ -907,19 +908,17 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
     // first pass computes the weights and caches them; later passes read them
     a.pass0 = 0;
     a.npl = 1;
-    e = nr == 12 ? launch_gram_tc_t<LOC, 2, 12, 1>(st, a, smem, per_pass) : launch_gram_tc_t<LOC, 2, 6, 1>(st, a, smem, per_pass);
+    e = launch_gram_tc_t<LOC, 2, 6, 1>(st, a, smem, per_pass);
     if (e != cudaSuccess) return e;
     a.pass0 = 1;
     a.npl = a.npass - 1;
-    e = nr == 12 ? launch_gram_tc_t<LOC, 2, 12, 2>(st, a, smem, per_pass * a.npl)
-                 : launch_gram_tc_t<LOC, 2, 6, 2>(st, a, smem, per_pass * a.npl);
+    e = launch_gram_tc_t<LOC, 2, 6, 2>(st, a, smem, per_pass * a.npl);
     (*launches) += 2;
     return e;
   }
   a.pass0 = 0;
   a.npl = a.npass;
-  e = nr == 12 ? launch_gram_tc_t<LOC, 2, 12, 0>(st, a, smem, per_pass * a.npass)
-               : launch_gram_tc_t<LOC, 2, 6, 0>(st, a, smem, per_pass * a.npass);
+  e = launch_gram_tc_t<LOC, 2, 6, 0>(st, a, smem, per_pass * a.npass);
   (*launches)++;
   return e;
 }
@@ -1034,11 +1033,6 @@ static cudaError_t preload_gram_tc_loc() {
   cudaFuncAttributes fa;
   cudaError_t e = cudaSuccess;
   auto get = [&](const void *f) { if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, f); };
-  get((const void *)k_gram_tc<LOC, 2, 12, 0, false>);
-  get((const void *)k_gram_tc<LOC, 2, 12, 0, true>);
-  get((const void *)k_gram_tc<LOC, 2, 12, 1, false>);
-  get((const void *)k_gram_tc<LOC, 2, 12, 1, true>);
-  get((const void *)k_gram_tc<LOC, 2, 12, 2, false>);
   get((const void *)k_gram_tc<LOC, 2, 6, 0, false>);
   get((const void *)k_gram_tc<LOC, 2, 6, 0, true>);
   get((const void *)k_gram_tc<LOC, 2, 6, 1, false>);
