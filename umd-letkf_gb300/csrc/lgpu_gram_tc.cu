@@ -370,17 +370,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   const int pass = a.pass0 + blockIdx.x % a.npl;
   const int g = (blockIdx.x / a.npl) % a.groups;
   const TcWork wk = a.work[blockIdx.x / (a.npl * a.groups)];
-  const int tile = wk.tile;
+  const int tile = wk.tile, seg = wk.seg;
   const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
-  // record ring: in the later passes (WMODE 2) each slot also holds the
-  // chunk's cached weight operand block (hi | lo), from which the MMA reads A,
-  // so the stages hold only the feature products
-  const int NRR = WMODE == 2 ? a.nring : NR;                 // slots in use
-  const uint32_t wofs = ((uint32_t)cb + 1023u) & ~1023u;     // weight block offset in a slot
-  const int slotb = WMODE == 2 ? (int)(wofs + WCB) : cb;
+  const int slotb = cb;   // ring slot: one chunk record
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
-  const uint32_t wst = WMODE == 2 ? 0u : 2 * WB;             // weight operand bytes in a stage
-  const uint32_t stage_bytes = wst + 2 * PB;
+  const uint32_t stage_bytes = 2 * WB + 2 * PB;
   auto stage_ptr = [&](int s) { return dsm + (size_t)s * stage_bytes; };
   unsigned char *ring = dsm + (size_t)NS * stage_bytes;
   // this CTA's segment of the tile's chunk stream
@@ -397,11 +391,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   if (wid == 0) tc::tmem_alloc(&S.tmem, tmem_cols);
   if (tid == 0) {
     for (int s = 0; s < NS; s++) {
-      tc::mbar_init(reinterpret_cast<uint64_t *>(&S.full[s]), NPW);
+      tc::mbar_init(reinterpret_cast<uint64_t *>(&S.full[s]), WMODE == 2 ? NPW + 1 : NPW);
       tc::mbar_init(reinterpret_cast<uint64_t *>(&S.empty[s]), 1);
       S.anyk[s] = 0;
     }
-    for (int r = 0; r < NRR; r++) tc::mbar_init(reinterpret_cast<uint64_t *>(&S.rfull[r]), 1);
+    for (int r = 0; r < NR; r++) tc::mbar_init(reinterpret_cast<uint64_t *>(&S.rfull[r]), 1);
     tc::mbar_init(reinterpret_cast<uint64_t *>(&S.done), 1);
     tc::mbar_init(reinterpret_cast<uint64_t *>(&S.accf), 2);
     tc::mbar_init(reinterpret_cast<uint64_t *>(&S.acce), NPW);
@@ -497,22 +491,30 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     const int rowi = (fv ? fi : 0) * YS, rowj = (fv ? fj : 0) * YS;
 
     for (int ch = 0; ch < nchunks; ch++) {
-      const int s = ch % NS, r = ch % NRR;
+      const int s = ch % NS, r = ch % NR;
       // the producers drain TMEM at boundary b = (j + 1) D once the stages
       // of chunks b .. b + NS - 1 are produced: the MMA of chunk b + NS needs
       // the stage chunk b frees, which waits for the drain
       if (nflushed < nflush && ch == (nflushed + 1) * D + NS) flush(nflushed++);
-      if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[r]), (ch / NRR) & 1)) { S.fault = 1; break; }
+      if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[r]), (ch / NR) & 1)) { S.fault = 1; break; }
       if (ch >= NS && !tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.empty[s]), ((ch / NS) - 1) & 1)) {
         S.fault = 1;
         break;
       }
       const unsigned char *rec = ring + (size_t)r * slotb;
       const float4 *RA = reinterpret_cast<const float4 *>(rec);
-      unsigned char *Whi = stage_ptr(s), *Wlo = Whi + WB, *Phi = Whi + wst, *Plo = Phi + PB;
+      unsigned char *Whi = stage_ptr(s), *Wlo = Whi + WB, *Phi = Whi + 2 * WB, *Plo = Phi + PB;
       bool anyk = false;
       if (WMODE == 2) {
-        // the chunk's weight operand block arrived with its record
+        // ---- the chunk's weight operand block (hi | lo) from the cache into
+        // the stage, counted on the stage's full barrier (the stage is free:
+        // its empty barrier was waited on above)
+        if (tid == 0) {
+          uint64_t *fb = reinterpret_cast<uint64_t *>(&S.full[s]);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(fb)),
+                       "r"((uint32_t)WCB) : "memory");
+          tc::bulk_copy_g2s(Whi, wcache + (size_t)(c0 + ch) * (WCB / 4), (uint32_t)WCB, fb);
+        }
       } else {
       // ---- weights: four observations, fast path without branches
       float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -617,18 +619,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
     if (lane == 0) {
       const unsigned char *src = a.rec + (size_t)c0 * cb;
       auto load = [&](int ch) {
-        unsigned char *dst = ring + (size_t)(ch % NRR) * slotb;
-        uint64_t *bar = reinterpret_cast<uint64_t *>(&S.rfull[ch % NRR]);
-        if (WMODE == 2) {   // the record and the cached weight block, on one barrier
-          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)),
-                       "r"((uint32_t)cb + (uint32_t)WCB) : "memory");
-          tc::bulk_copy_g2s(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
-          tc::bulk_copy_g2s(dst + wofs, wcache + (size_t)(c0 + ch) * (WCB / 4), (uint32_t)WCB, bar);
-        } else {
-          tc::bulk_load(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
-        }
+        unsigned char *dst = ring + (size_t)(ch % NR) * slotb;
+        uint64_t *bar = reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]);
+        tc::bulk_load(dst, src + (size_t)ch * cb, (uint32_t)cb, bar);
       };
-      int n_loaded = nchunks < NRR ? nchunks : NRR;
+      int n_loaded = nchunks < NR ? nchunks : NR;
       for (int ch = 0; ch < n_loaded; ch++) load(ch);
       const int nb0 = NP < 256 ? NP : 256, nb1 = NP - nb0;
       const uint32_t id0 = tc::idesc_tf32(TM, nb0), id1 = nb1 > 0 ? tc::idesc_tf32(TM, nb1) : 0u;
@@ -650,15 +645,12 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         const int cached_flag = WMODE == 2 ? wflag[c0 + ch] : 0;   // issued before the wait hides its latency
         if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.full[s]), (ch / NS) & 1)) { S.fault = 1; break; }
         // every producer is done with the records of chunk ch: refill the slot
-        // (the later passes' slots also feed the MMA: refilled below)
-        if (WMODE != 2 && n_loaded < nchunks) load(n_loaded++);
+        if (n_loaded < nchunks) load(n_loaded++);
         const bool mma = WMODE == 2 ? cached_flag != 0 : S.anyk[s] == ch + 1;
         if (WMODE == 1) wflag[c0 + ch] = mma ? 1 : 0;
         if (mma) {
           tc::fence_after();
-          const uint32_t whi = WMODE == 2 ? tc::smem_u32(ring + (size_t)(ch % NRR) * slotb + wofs)
-                                          : tc::smem_u32(stage_ptr(s));
-          const uint32_t wlo = whi + WB, phi = tc::smem_u32(stage_ptr(s)) + wst, plo = phi + PB;
+          const uint32_t whi = tc::smem_u32(stage_ptr(s)), wlo = whi + WB, phi = whi + 2 * WB, plo = phi + PB;
 #pragma unroll
           for (int t = 0; t < 3; t++)
 #pragma unroll
@@ -679,14 +671,6 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
         } else {
           bar_arrive(&S.empty[s]);
         }
-        if (WMODE == 2 && ch >= 1 && n_loaded < nchunks) {
-          // the slot of chunk ch - 1 is free once its MMAs have completed
-          if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.empty[(ch - 1) % NS]), ((ch - 1) / NS) & 1)) {
-            S.fault = 1;
-            break;
-          }
-          load(n_loaded++);
-        }
       }
       // every MMA issued by this thread has completed once `done` flips
       tc::commit(reinterpret_cast<uint64_t *>(&S.done));
@@ -694,8 +678,8 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       S.issued = issued ? 1 : 0;
       if (nmma) atomicAdd(a.status + 2, nmma);   // chunks whose MMAs ran (executed-work counter)
       // no record copy may still be in flight when the CTA exits
-      for (int ch = n_loaded > NRR ? n_loaded - NRR : 0; ch < n_loaded; ch++)
-        if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[ch % NRR]), (ch / NRR) & 1)) S.fault = 1;
+      for (int ch = n_loaded > NR ? n_loaded - NR : 0; ch < n_loaded; ch++)
+        if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.rfull[ch % NR]), (ch / NR) & 1)) S.fault = 1;
     }
   }
   tc::fence_before();
@@ -854,19 +838,6 @@ void gram_tc_config(int k, int np, int *ns, int *nr, size_t *smem) {
   *smem = (size_t)*ns * stage + (size_t)*nr * cb;
 }
 
-// The later passes: two stages of feature products, record slots of a chunk
-// record and its cached weight block (at least three: the producers run two
-// chunks ahead of the MMA, which frees a slot one chunk after its MMA)
-void gram_tc_config_cached(int k, int np, int *nring, size_t *smem) {
-  const size_t PB = (size_t)(np / 8) * SBO;
-  const size_t stage = 2 * PB;
-  const size_t slot = ((record_bytes(k) + 1023) & ~(size_t)1023) + WCB;
-  size_t n = (kSmemBudget - 2 * stage) / slot;
-  if (n > (size_t)NRMAX) n = NRMAX;
-  *nring = (int)n;
-  *smem = 2 * stage + n * slot;
-}
-
 }  // namespace
 
 size_t record_bytes(int k) { return 512 + (size_t)(((k + 4) & ~3) * YS) * sizeof(float); }
@@ -941,12 +912,7 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
     if (e != cudaSuccess) return e;
     a.pass0 = 1;
     a.npl = a.npass - 1;
-    // later passes: the stages hold only the feature products; each record
-    // slot also holds the chunk's cached weight block
-    size_t smem2;
-    gram_tc_config_cached(a.k, a.np, &a.nring, &smem2);
-    if (a.nring < 3) return cudaErrorInvalidValue;
-    e = launch_gram_tc_t<LOC, 2, 6, 2>(st, a, smem2, per_pass * a.npl);
+    e = launch_gram_tc_t<LOC, 2, 6, 2>(st, a, smem, per_pass * a.npl);
     (*launches) += 2;
     return e;
   }

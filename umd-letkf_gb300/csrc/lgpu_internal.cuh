@@ -468,7 +468,6 @@ struct TcArgs {
   int *wflag;                // [groups][chunks]: the chunk has a kept pair (MMA issued)
   int nchunk_total;          // chunks over all tiles (weight cache indexing)
   int pass0, npl;            // feature passes of one launch: [pass0, pass0 + npl) (set by the launcher)
-  int nring;                 // record slots of the later passes, each with the chunk's cached weight block (set by the launcher)
   // accumulation segments and drains: each tile's chunk stream is split into
   // segments (one CTA each), and each CTA moves its tensor-core accumulator
   // out every `drain` chunks (the FP32 accumulation error of the tensor core
