@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
   const int pass = a.pass0 + blockIdx.x % a.npl;
   const int g = (blockIdx.x / a.npl) % a.groups;
   const TcWork wk = a.work[blockIdx.x / (a.npl * a.groups)];
-  const int tile = wk.tile, seg = wk.seg;
+  const int tile = wk.tile;
   const int k = a.k, NP = a.np, nf = a.nf, cb = a.cb;
   const int slotb = cb;   // ring slot: one chunk record
   const uint32_t PB = (uint32_t)(NP / 8) * SBO;
