@@ -629,6 +629,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
       const uint32_t id0 = tc::idesc_tf32(TM, nb0), id1 = nb1 > 0 ? tc::idesc_tf32(TM, nb1) : 0u;
       bool issued = false;   // since the last drain
       int nmma = 0, fj = 0;
+      // later passes: the chunks' MMA flags from pass 0, loaded two chunks
+      // ahead into alternating registers (each is read two iterations after
+      // its load is issued)
+      auto flag_at = [&](int c) { return (WMODE == 2 && c < nchunks) ? wflag[c0 + c] : 0; };
+      int flag_even = flag_at(0), flag_odd = flag_at(1);
       for (int ch = 0; ch < nchunks; ch++) {
         const int s = ch % NS;
         if (ch > 0 && ch % a.drain == 0) {
@@ -642,7 +647,11 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
           fj++;
           issued = false;
         }
-        const int cached_flag = WMODE == 2 ? wflag[c0 + ch] : 0;   // issued before the wait hides its latency
+        int cached_flag = 0;
+        if (WMODE == 2) {
+          if (ch & 1) { cached_flag = flag_odd; flag_odd = flag_at(ch + 2); }
+          else { cached_flag = flag_even; flag_even = flag_at(ch + 2); }
+        }
         if (!tc::mbar_wait(reinterpret_cast<uint64_t *>(&S.full[s]), (ch / NS) & 1)) { S.fault = 1; break; }
         // every producer is done with the records of chunk ch: refill the slot
         if (n_loaded < nchunks) load(n_loaded++);
@@ -901,6 +910,7 @@ static cudaError_t launch_gram_tc_loc(cudaStream_t st, TcArgs a, int *launches) 
   gram_tc_config(a.k, a.np, &ns, &nr, &smem);   // two stages, six record slots
   (void)ns;
   (void)nr;
+  if (smem > kSmemBudget) return cudaErrorInvalidValue;   // k <= 128 fits
   const long long per_pass = (long long)a.nwork * a.groups;
   if (per_pass * a.npass > 0x7fffffffLL) return cudaErrorInvalidValue;
   cudaError_t e;
