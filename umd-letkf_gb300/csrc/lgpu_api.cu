@@ -73,6 +73,24 @@ enum {
 }  // namespace
 
 constexpr int kOutChunks = 8;   // column chunks of eigensolve / update / analysis download of a bound state
+
+// Column range [c0, c1) of chunk c of n over ncol columns.  With n =
+// kOutChunks (and at least 1,000 columns, so that none is empty) the chunks
+// shrink towards the end (per mille of the columns below), so that the
+// download of the last chunk, which nothing overlaps, is short; the earlier
+// downloads overlap the following chunks' work.  Otherwise equal chunks,
+// empty ones only at the end.
+static void chunk_bounds(int ncol, int n, int c, int *c0, int *c1) {
+  static const int kShare[kOutChunks + 1] = {0, 150, 300, 450, 590, 720, 840, 940, 1000};
+  if (n == kOutChunks && ncol >= 1000) {
+    *c0 = (int)((long long)ncol * kShare[c] / 1000);
+    *c1 = (int)((long long)ncol * kShare[c + 1] / 1000);
+  } else {
+    const int per = (ncol + n - 1) / n;
+    *c0 = std::min(ncol, c * per);
+    *c1 = std::min(ncol, (c + 1) * per);
+  }
+}
 constexpr int kSegChunks = 256;   // batched Gram: chunks of 16 observations per CTA at most
 constexpr int kDrainChunks = 64;  // batched Gram: chunks per tensor-core accumulation (drained to a partial block)
 
@@ -1108,9 +1126,10 @@ static int upload_members(lgpu_handle *h, cudaEvent_t after) {
   CK(cudaEventRecord(after, h->st), "event");
   CK(cudaStreamWaitEvent(h->cst, after, 0), "stream wait");
   CK(cudaEventRecord(h->ev_in[1], h->cst), "event");
-  const int per = (h->ncol + kOutChunks - 1) / kOutChunks;
   for (int c = 0; c < kOutChunks; c++) {
-    const size_t c0 = (size_t)std::min(h->ncol, c * per), c1 = (size_t)std::min(h->ncol, (c + 1) * per);
+    int b0, b1;
+    chunk_bounds(h->ncol, kOutChunks, c, &b0, &b1);
+    const size_t c0 = (size_t)b0, c1 = (size_t)b1;
     if (c1 > c0)
       CK(cudaMemcpyAsync(h->buf[B_BKG].as<float>() + c0 * ns * k, h->bound_state + c0 * ns * k,
                          (c1 - c0) * ns * k * 4, cudaMemcpyHostToDevice, h->cst), "H2D state");
@@ -1232,11 +1251,11 @@ static int solver_run(lgpu_handle *h) {
     if (batch == 0) CK(launch_eig(st, ea, &launches), "eigen kernel");
   }
   const int nch = bound ? kOutChunks : 1;
-  const int per = (h->ncol + nch - 1) / nch;
   float eig_ms = 0.0f, upd_ms = 0.0f, fp64_ms = 0.0f;
   int nrec = 0;
   for (int c = 0; c < nch; c++) {
-    const int c0 = c * per, c1 = std::min(h->ncol, (c + 1) * per);
+    int c0, c1;
+    chunk_bounds(h->ncol, nch, c, &c0, &c1);
     if (c1 <= c0) break;
     // units of the chunk's active columns
     int a0 = -1, a1 = -1;
