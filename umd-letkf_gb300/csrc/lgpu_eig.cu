@@ -785,6 +785,161 @@ __global__ void __launch_bounds__(32 * RWPB, 4) k_eig_tri_r(EigArgs a, EigSplit 
   for (int i = lane; i < k; i += 32) { de[i] = dd[i]; de[k + i] = ee[i]; }
 }
 
+// k_eig_tri_t<K, NW>: k_eig_tri_r for 48 < k <= K <= 128 with a team of NW
+// warps per unit (one unit per CTA, 32 NW >= K): thread t holds row t of the
+// work matrix in registers; the reflector row VH[j] is written by thread j,
+// the sums over the rows run through the team in warp order, and Q is formed
+// with thread t holding column t.  Shared memory (dynamic): the reflectors
+// (K - 2) x K, then w, d, e, tau (K each).  Same arithmetic as k_eig_tri_r,
+// one row per thread instead of two per lane.
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * NW) k_eig_tri_t(EigArgs a, EigSplit sp, int u0, int nb) {
+  constexpr int NR = K - 2;
+  constexpr int K4 = K / 4;
+  static_assert(32 * NW >= K, "one row per thread");
+  extern __shared__ __align__(16) float tsm[];
+  __shared__ float red[NW];
+  float *VH = tsm;                 // reflector j in row j
+  float *ww = VH + NR * K;         // w of the current step
+  float *dd = ww + K, *ee = dd + K, *tau = ee + K;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int ub = blockIdx.x;
+  if (ub >= nb) return;
+  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
+  if (a.nkept[unit] <= 0) return;
+  const int k = a.k;
+  // the team's sum (butterfly in each warp, then the warps in order)
+  auto tsum = [&](float v) -> float {
+    v = wsum<float>(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float r = red[0];
+#pragma unroll
+    for (int q = 1; q < NW; q++) r += red[q];
+    __syncthreads();
+    return r;
+  };
+  // A = G + (k-1)/infl I (src/letkf_core.F90:101-104), row t
+  const float *Gin = a.G + (size_t)unit * packed_size(k);
+  const float shift = (float)(k - 1) * 1.0f / a.infl;
+  float A[K];
+#pragma unroll
+  for (int c = 0; c < K; c++) {
+    float v = 0.0f;
+    if (t < k && c < k) {
+      v = t <= c ? Gin[tri_idx(t, c, k)] : Gin[tri_idx(c, t, k)];
+      if (t == c) v += shift;
+    }
+    A[c] = v;
+  }
+  for (int j = 0; j < k - 2; j++) {
+    float *vj = VH + j * K;
+    __syncthreads();
+    if (t == j) {
+#pragma unroll
+      for (int c = 0; c < K; c++) {
+        const float x = A[c];
+        vj[c] = (c > j && c < k) ? x : 0.0f;
+        if (c == j) dd[j] = x;
+      }
+    }
+    __syncthreads();
+    const float xt = t < K ? vj[t] : 0.0f;
+    const float sig = tsum(xt * xt);
+    const float x0 = vj[j + 1];
+    const float s1 = sig - x0 * x0;
+    if (!(s1 > Lim<float>::tiny * sig) || sig == 0.0f) {
+      if (t == 0) { tau[j] = 0.0f; ee[j] = x0; }
+      continue;
+    }
+    const float alpha = -copysignf(sqrtf(sig), x0);
+    const float v0 = x0 - alpha;
+    const float tt = 2.0f / (v0 * v0 + s1);
+    __syncthreads();
+    if (t == 0) { vj[j + 1] = v0; tau[j] = tt; ee[j] = alpha; }
+    __syncthreads();
+    // p = t A v
+    float acc = 0.0f;
+#pragma unroll
+    for (int c4 = 0; c4 < K4; c4++) {
+      if (4 * c4 + 3 <= j) continue;
+      const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * c4);
+      acc = __fmaf_rn(A[4 * c4 + 0], v4.x, acc);
+      acc = __fmaf_rn(A[4 * c4 + 1], v4.y, acc);
+      acc = __fmaf_rn(A[4 * c4 + 2], v4.z, acc);
+      acc = __fmaf_rn(A[4 * c4 + 3], v4.w, acc);
+    }
+    const float p = tt * acc;
+    const float vt = t < K ? vj[t] : 0.0f;
+    const float beta = 0.5f * tt * tsum(t < K ? __fmaf_rn(p, vt, 0.0f) : 0.0f);
+    const float w = (t > j && t < k) ? p - beta * vt : 0.0f;
+    if (t < K) ww[t] = w;
+    __syncthreads();
+    // A -= v w^T + w v^T
+#pragma unroll
+    for (int c4 = 0; c4 < K4; c4++) {
+      if (4 * c4 + 3 <= j) continue;
+      const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * c4);
+      const float4 w4 = *reinterpret_cast<const float4 *>(ww + 4 * c4);
+      A[4 * c4 + 0] = A[4 * c4 + 0] - __fmaf_rn(vt, w4.x, w * v4.x);
+      A[4 * c4 + 1] = A[4 * c4 + 1] - __fmaf_rn(vt, w4.y, w * v4.y);
+      A[4 * c4 + 2] = A[4 * c4 + 2] - __fmaf_rn(vt, w4.z, w * v4.z);
+      A[4 * c4 + 3] = A[4 * c4 + 3] - __fmaf_rn(vt, w4.w, w * v4.w);
+    }
+  }
+  __syncthreads();
+  // the last 2 x 2 block: d[k-2], d[k-1], e[k-2]
+  if (t == k - 2 || t == k - 1) {
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+      if (c == t) dd[t] = A[c];
+      if (t == k - 1 && c == k - 2) ee[k - 2] = A[c];
+    }
+  }
+  if (t == 0) ee[k - 1] = 0.0f;
+  __syncthreads();
+  // Q = H_0 H_1 ... H_{k-3} I, reflectors from the last to the first; thread
+  // t holds column t
+#pragma unroll
+  for (int r = 0; r < K; r++) A[r] = (r == t && t < k) ? 1.0f : 0.0f;
+  for (int j = k - 3; j >= 0; j--) {
+    const float tj = tau[j];
+    if (tj == 0.0f) continue;
+    const float *vj = VH + j * K;
+    float s = 0.0f;
+#pragma unroll
+    for (int r4 = 0; r4 < K4; r4++) {
+      if (4 * r4 + 3 <= j) continue;
+      const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * r4);
+      s = __fmaf_rn(v4.x, A[4 * r4 + 0], s);
+      s = __fmaf_rn(v4.y, A[4 * r4 + 1], s);
+      s = __fmaf_rn(v4.z, A[4 * r4 + 2], s);
+      s = __fmaf_rn(v4.w, A[4 * r4 + 3], s);
+    }
+    s *= tj;
+#pragma unroll
+    for (int r4 = 0; r4 < K4; r4++) {
+      if (4 * r4 + 3 <= j) continue;
+      const float4 v4 = *reinterpret_cast<const float4 *>(vj + 4 * r4);
+      A[4 * r4 + 0] -= v4.x * s;
+      A[4 * r4 + 1] -= v4.y * s;
+      A[4 * r4 + 2] -= v4.z * s;
+      A[4 * r4 + 3] -= v4.w * s;
+    }
+  }
+  float *Q = sp.Q + (size_t)ub * k * k;
+  if (t < k) {
+#pragma unroll
+    for (int r = 0; r < K; r++)
+      if (r < k) Q[(size_t)r * k + t] = A[r];
+  }
+  float *de = sp.DE + (size_t)ub * 2 * k;
+  for (int i = t; i < k; i += 32 * NW) { de[i] = dd[i]; de[k + i] = ee[i]; }
+}
+
+template <int K, int NW>
+static size_t tri_t_smem() { return ((size_t)(K - 2) * K + 4 * K) * sizeof(float); }
+
 constexpr int QLT = 64;   // threads (units) per block of k_eig_ql
 
 __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, int nb) {
@@ -1207,7 +1362,7 @@ static int eig_team(int k) { return k <= 64 ? 1 : 2; }
 // k_eig_vec (above k = 48), or on the full matrix, forming Q: measured on
 // GB300 (206k units per analysis, eigensolve ms full -> packed): k = 40
 // 25.8 -> 26.6, k = 64 57.2 -> 53.8; C4 (824k units) k = 100 1057 -> 974
-static bool eig_packed(int k) { return k > 48; }
+static bool eig_packed(int k) { return k > 128; }
 
 // the register-resident first stage (k <= 48)
 static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
@@ -1222,6 +1377,32 @@ static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSpli
   default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+// the register-resident first stage with a team per unit (48 < k <= 128)
+template <int K, int NW>
+static cudaError_t launch_tri_t_k(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
+  const size_t smem = tri_t_smem<K, NW>();
+  cudaError_t e = cudaFuncSetAttribute(k_eig_tri_t<K, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_eig_tri_t<K, NW><<<nb, 32 * NW, smem, st>>>(a, sp, u0, nb);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_tri_t(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
+  switch ((a.k + 7) & ~7) {
+  case 56: return launch_tri_t_k<56, 2>(st, a, sp, u0, nb);
+  case 64: return launch_tri_t_k<64, 2>(st, a, sp, u0, nb);
+  case 72: return launch_tri_t_k<72, 4>(st, a, sp, u0, nb);
+  case 80: return launch_tri_t_k<80, 4>(st, a, sp, u0, nb);
+  case 88: return launch_tri_t_k<88, 4>(st, a, sp, u0, nb);
+  case 96: return launch_tri_t_k<96, 4>(st, a, sp, u0, nb);
+  case 104: return launch_tri_t_k<104, 4>(st, a, sp, u0, nb);
+  case 112: return launch_tri_t_k<112, 4>(st, a, sp, u0, nb);
+  case 120: return launch_tri_t_k<120, 4>(st, a, sp, u0, nb);
+  case 128: return launch_tri_t_k<128, 4>(st, a, sp, u0, nb);
+  default: return cudaErrorInvalidValue;
+  }
 }
 
 template <int NQ, int NW, bool kPackedTri>
@@ -1251,7 +1432,8 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
   for (int u0 = ustart; u0 < uend; u0 += batch) {
     const int nb = uend - u0 < batch ? uend - u0 : batch;
     if (kPackedTri) k_eig_trip<NW><<<(nb + wpt - 1) / wpt, tht, smt, st>>>(a, sp, wpt, u0, nb);
-    else if ((e = launch_tri_r(st, a, sp, u0, nb)) != cudaSuccess) return e;
+    else if ((e = a.k <= 48 ? launch_tri_r(st, a, sp, u0, nb) : launch_tri_t(st, a, sp, u0, nb)) != cudaSuccess)
+      return e;
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
     k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
     (*launches) += 3;
