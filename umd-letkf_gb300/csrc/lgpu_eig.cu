@@ -302,12 +302,17 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
 
 // Deflation test of the QL iteration: e_m is negligible when it is below
 // eps32 of its two diagonal neighbours (the local test of LAPACK's ssteqr /
-// EISPACK's tql2 family) or below eps32 times the norm of the whole
-// tridiagonal matrix (tql2's absolute test).  The second test ends the
-// iteration where rounding at the eps32 ||T|| level (already present in T
-// from the Householder reduction) keeps a strongly graded block from
-// meeting the local test; it leaves the eigenvalues within the backward
-// error the reduction has already made.
+// EISPACK's tql2 family) or, from the kQlAbsIter-th iteration on the current
+// eigenvalue, below eps32 times the norm of the whole tridiagonal matrix
+// (tql2's absolute test).  The second test ends the iteration where rounding
+// at the eps32 ||T|| level keeps a strongly graded block from meeting the
+// local test.  Applied from the first iteration it also deflated, at the
+// ||T|| level, off-diagonals between near-equal small eigenvalues that the
+// local test resolves in a few more sweeps (a rank-one update with k = 100
+// and condition ~1e5: those eigenvalues off by ~eps32 ||T||); the delay
+// keeps them.
+constexpr int kQlAbsIter = 6;
+
 template <class R>
 __device__ __forceinline__ bool ql_negligible(R em, R dm, R dm1, R tabs) {
   const R ae = fabs(em);
@@ -352,7 +357,7 @@ __device__ __forceinline__ void eig_ql_warp(int k, EigWork<R> &W, int lane, int 
         for (int base = l; base < k - 1; base += 32) {
           const int mm = base + lane;
           bool small = false;
-          if (mm < k - 1) small = ql_negligible(e[mm], d[mm], d[mm + 1], tabs);
+          if (mm < k - 1) small = ql_negligible(e[mm], d[mm], d[mm + 1], iter >= kQlAbsIter ? tabs : R(0));
           const unsigned bal = __ballot_sync(0xffffffffu, small);
           if (bal) { m = base + __ffs(bal) - 1; break; }
         }
@@ -961,7 +966,8 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
     int iter = 0;
     for (;;) {
       int m = l;
-      while (m < k - 1 && !ql_negligible(E(m), D(m), D(m + 1), tabs)) m++;
+      const float tab = iter >= kQlAbsIter ? tabs : 0.0f;
+      while (m < k - 1 && !ql_negligible(E(m), D(m), D(m + 1), tab)) m++;
       if (m == l) break;
       if (++iter > 60) { bad |= 1; break; }
       const float dl = D(l), el = E(l);
@@ -1178,7 +1184,7 @@ __device__ __forceinline__ void eig_ql_team(int k, EigWork<R> &W, const Team<NW,
         for (int base = l; base < k - 1; base += 32) {
           const int mm = base + lane;
           bool small = false;
-          if (mm < k - 1) small = ql_negligible(e[mm], d[mm], d[mm + 1], tabs);
+          if (mm < k - 1) small = ql_negligible(e[mm], d[mm], d[mm + 1], iter >= kQlAbsIter ? tabs : R(0));
           const unsigned bal = __ballot_sync(0xffffffffu, small);
           if (bal) { m = base + __ffs(bal) - 1; break; }
         }
