@@ -790,7 +790,7 @@ __global__ void __launch_bounds__(32 * RWPB, 4) k_eig_tri_r(EigArgs a, EigSplit 
   for (int i = lane; i < k; i += 32) { de[i] = dd[i]; de[k + i] = ee[i]; }
 }
 
-// k_eig_tri_t<K, NW>: k_eig_tri_r for 48 < k <= K <= 128 with a team of NW
+// k_eig_tri_t<K, NW>: k_eig_tri_r for 48 < k <= K <= 64 with a team of NW
 // warps per unit (one unit per CTA, 32 NW >= K): thread t holds row t of the
 // work matrix in registers; the reflector row VH[j] is written by thread j,
 // the sums over the rows run through the team in warp order, and Q is formed
@@ -1364,11 +1364,13 @@ static int eig_wpb(int k) { return eig_wpb_floats(eig_floats_per_warp(k)); }
 // against 414 with one warp and 308 / 359 with four / eight)
 static int eig_team(int k) { return k <= 64 ? 1 : 2; }
 
-// the split pipeline's first stage on the packed lower triangle, Q formed in
-// k_eig_vec (above k = 48), or on the full matrix, forming Q: measured on
-// GB300 (206k units per analysis, eigensolve ms full -> packed): k = 40
-// 25.8 -> 26.6, k = 64 57.2 -> 53.8; C4 (824k units) k = 100 1057 -> 974
-static bool eig_packed(int k) { return k > 128; }
+// the split pipeline's first stage: in registers, forming Q (k <= 48 one
+// warp, k <= 64 a two-warp team), or on the packed lower triangle with Q
+// formed in k_eig_vec (above k = 64).  Measured on GB300 (eigensolve ms):
+// k = 40 shared-memory full matrix 25.8, packed 26.6, registers 23.7; k = 64
+// full 57.2, packed 53.8, team registers 49.3; C4 (k = 100) full 1057, packed
+// 974, four-warp team registers 1018
+static bool eig_packed(int k) { return k > 64; }
 
 // the register-resident first stage (k <= 48)
 static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
@@ -1385,7 +1387,7 @@ static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSpli
   return cudaGetLastError();
 }
 
-// the register-resident first stage with a team per unit (48 < k <= 128)
+// the register-resident first stage with a two-warp team per unit (48 < k <= 64)
 template <int K, int NW>
 static cudaError_t launch_tri_t_k(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
   const size_t smem = tri_t_smem<K, NW>();
@@ -1399,14 +1401,6 @@ static cudaError_t launch_tri_t(cudaStream_t st, const EigArgs &a, const EigSpli
   switch ((a.k + 7) & ~7) {
   case 56: return launch_tri_t_k<56, 2>(st, a, sp, u0, nb);
   case 64: return launch_tri_t_k<64, 2>(st, a, sp, u0, nb);
-  case 72: return launch_tri_t_k<72, 4>(st, a, sp, u0, nb);
-  case 80: return launch_tri_t_k<80, 4>(st, a, sp, u0, nb);
-  case 88: return launch_tri_t_k<88, 4>(st, a, sp, u0, nb);
-  case 96: return launch_tri_t_k<96, 4>(st, a, sp, u0, nb);
-  case 104: return launch_tri_t_k<104, 4>(st, a, sp, u0, nb);
-  case 112: return launch_tri_t_k<112, 4>(st, a, sp, u0, nb);
-  case 120: return launch_tri_t_k<120, 4>(st, a, sp, u0, nb);
-  case 128: return launch_tri_t_k<128, 4>(st, a, sp, u0, nb);
   default: return cudaErrorInvalidValue;
   }
 }
