@@ -1045,7 +1045,6 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   const float *lam = sp.lam + (size_t)ub * k;
   for (int t = tt; t < k; t += TS) W.d[t] = lam[t];
   const float *G = a.G + (size_t)unit * packed_size(k);
-  for (int i = tt; i < k; i += TS) W.bv[i] = G[k * (k + 1) / 2 + i];
   T.sync();
   int bad = 0;
   if (total < 0) {
@@ -1057,10 +1056,15 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
     constexpr int NQW = 32 * NW * NQ <= 64 ? 2 : 4;
     if (warp == 0 || NW == 1) eig_ql_warp<NQW>(k, W, lane, bad);
   } else {
-    // replay the rotations on the thread's rows (tt + TS q); the log is
-    // read 32 entries at a time (lane j holds entry base + j) and broadcast
-    // within each warp
+    // replay the rotations on the thread's rows (tt + TS q).  The log passes
+    // through a window in the scratch vectors e .. gl (free until the
+    // transform; 8-byte aligned), refilled by the team at a sweep boundary
+    // whenever the next sweep (header + cnt <= k entries) would not fit, so
+    // that a sweep's rotations are read with one broadcast load each
     const float2 *lg = sp.log + (size_t)ub * sp.cap;
+    const int wofs = (k * (k + 2)) & 1;   // e sits k (k + 2) floats into the unit's scratch
+    float2 *win = reinterpret_cast<float2 *>(W.e + wofs);
+    const int WN = (7 * k + 8 - wofs) / 2;   // e, tau, bv, p, w, fl, gl and the 8 spare floats
     bool own[NQ];
     float *qr[NQ];
 #pragma unroll
@@ -1069,29 +1073,28 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
       qr[q] = A + (own[q] ? tt + TS * q : 0) * ld;
     }
     int base = 0;
-    float2 cur = lane < total ? lg[lane] : make_float2(0.f, 0.f);
-    float2 nxt = lane + 32 < total ? lg[32 + lane] : make_float2(0.f, 0.f);
-    auto get = [&](int idx) -> float2 {
-      if (idx >= base + 32) {   // warp-uniform
-        base += 32;
-        cur = nxt;
-        nxt = base + 32 + lane < total ? lg[base + 32 + lane] : make_float2(0.f, 0.f);
-      }
-      float2 v;
-      v.x = __shfl_sync(0xffffffffu, cur.x, idx - base);
-      v.y = __shfl_sync(0xffffffffu, cur.y, idx - base);
-      return v;
+    auto refill = [&](int from) {   // team-uniform
+      T.sync();
+      base = from;
+      const int n = total - from < WN ? total - from : WN;
+      for (int t = tt; t < n; t += TS) win[t] = lg[from + t];
+      T.sync();
     };
+    refill(0);
     int pidx = 0;
     while (pidx < total) {
-      const float2 h = get(pidx++);
+      if (pidx >= base + WN) refill(pidx);
+      const float2 h = win[pidx - base];
       const int m = __float_as_int(h.x), cnt = __float_as_int(h.y);
-      if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + cnt > total) { bad |= 32; break; }   // malformed log
+      if (m < 1 || m >= k || cnt < 0 || cnt > m || pidx + 1 + cnt > total) { bad |= 32; break; }   // malformed log
+      if (pidx + 1 + cnt > base + WN) refill(pidx);
+      const float2 *rot = win + (pidx + 1 - base);
+      pidx += 1 + cnt;
       float z[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : 0.0f;
       for (int r = 0; r < cnt; r++) {
-        const float2 cs = get(pidx++);
+        const float2 cs = rot[r];
         const float c = cs.x, s = cs.y;
         const int i = m - 1 - r;
 #pragma unroll
@@ -1105,6 +1108,9 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
         if (own[q]) qr[q][m - cnt] = z[q];
     }
   }
+  // b after the replay: its slot is part of the log window
+  T.sync();
+  for (int i = tt; i < k; i += TS) W.bv[i] = G[k * (k + 1) / 2 + i];
   T.sync();
   eig_transform<NQ>(a, unit, W, T, bad);
   bad = __reduce_or_sync(0xffffffffu, bad);

@@ -559,7 +559,9 @@ __global__ void __launch_bounds__(NT, 1) k_gram_tc(TcArgs a) {
           const float4 B = RA[16 + e];
           const float de = dist_from_chord2(chord2_exact(cp.ux, cp.uy, cp.uz, A.x, A.y, A.z));
           const bool in = de <= cp.rmax;
-          float rl = in ? localize(a.loc, cp, g, de, B.y, B.z, B.w) : 0.0f;
+          // the class's exact localizer with the column's parameters from
+          // global memory (keeps them out of the producers' registers)
+          float rl = in ? localize_cls<LOC>(a.loc, a.cp[col], g, de, B.y, B.z, B.w) : 0.0f;
           w[u] = (in && rl > kKeep) ? rl : 0.0f;
           inr = (inr & ~(1u << u)) | ((in ? 1u : 0u) << u);
         }

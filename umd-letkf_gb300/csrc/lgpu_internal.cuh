@@ -284,39 +284,44 @@ struct ColPar {
 
 // Localisation weight of one (column, group, observation) with exact keep
 // decisions: fast float evaluation, exact REAL(8) re-evaluation in the guard
-// band around the keep threshold.
-__device__ __forceinline__ float localize(const DevLoc &L, const ColPar &c, int gid, float dist,
-                                          float otime, float oz, float surf) {
-  switch (L.cls) {
-  case LOC_OCEAN: {
+// band around the keep threshold.  localize_cls is one class; the column's
+// parameters are read where the class needs them, so a caller holding c in
+// global memory keeps the unused ones out of its registers.
+template <int CLS>
+__device__ __forceinline__ float localize_cls(const DevLoc &L, const ColPar &c, int gid, float dist, float otime,
+                                              float oz, float surf) {
+  if (CLS == LOC_OCEAN) {
     // src/subclass.letkf_localizer/letkf_loc_ocean.F90:483-504
-    bool s = surf != 0.0f;
+    const bool s = surf != 0.0f;
     if (s && gid == 1) return 0.0f;
-    float Lh = s ? c.L2 : c.L1, ic = s ? c.ic2 : c.ic1, tl = s ? L.tloc_sat : L.tloc_prof;
+    const float Lh = s ? c.L2 : c.L1, ic = s ? c.ic2 : c.ic1, tl = s ? L.tloc_sat : L.tloc_prof;
     float r = gc_fast(dist, ic);
     if (tl > 0.0f) {
-      float rt = gc_fast(otime, inv_c_of(tl));
-      float p = r * rt;
+      float p = r * gc_fast(otime, inv_c_of(tl));
       if (fabsf(p - kKeep) <= kGuard2) p = gc_exact(dist, Lh) * gc_exact(otime, tl);
       return p;
     }
     if (fabsf(r - kKeep) <= kGuard1) r = gc_exact(dist, Lh);
     return r;
-  }
-  case LOC_VTGC: {
-    float rh = gc_fast(dist, c.ic1);
-    float dz = fabsf(oz - L.lev_depth[gid]);
-    float rv = gc_fast(dz, inv_c_of(L.vloc));
-    float p = rh * rv;
+  } else if (CLS == LOC_VTGC) {
+    const float dz = fabsf(oz - L.lev_depth[gid]);
+    float p = gc_fast(dist, c.ic1) * gc_fast(dz, inv_c_of(L.vloc));
     if (fabsf(p - kKeep) <= kGuard2) p = gc_exact(dist, c.L1) * gc_exact(dz, L.vloc);
     return p;
-  }
-  default: {
+  } else {
     // src/subclass.letkf_localizer/letkf_loc_novrt.F90:181
     float r = gc_fast(dist, c.ic1);
     if (fabsf(r - kKeep) <= kGuard1) r = gc_exact(dist, c.L1);
     return r;
   }
+}
+
+__device__ __forceinline__ float localize(const DevLoc &L, const ColPar &c, int gid, float dist,
+                                          float otime, float oz, float surf) {
+  switch (L.cls) {
+  case LOC_OCEAN: return localize_cls<LOC_OCEAN>(L, c, gid, dist, otime, oz, surf);
+  case LOC_VTGC: return localize_cls<LOC_VTGC>(L, c, gid, dist, otime, oz, surf);
+  default: return localize_cls<LOC_NOVRT>(L, c, gid, dist, otime, oz, surf);
   }
 }
 
