@@ -279,23 +279,38 @@ __device__ __forceinline__ void eig_transform(const EigArgs &a, int unit, EigWor
   // T_ij = sum_l U[i][l] U[j][l] + wbar_i ; thread owns columns tt + TS q
   // (a column past k repeats the thread's first column and is not stored)
   float *Tout = a.T + (size_t)unit * k * k;
+  // rows in blocks of TRB (a row past k repeats row 0 and is not stored);
+  // every sum runs over l in ascending order
   if (tt < k) {
+    constexpr int TRB = 4;
     const R *u[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; q++) u[q] = A + (tt + TS * q < k ? tt + TS * q : tt) * ld;
-    for (int i = 0; i < k; i++) {
-      const R *ur = A + i * ld;
-      R acc[NQ];
+    for (int i0 = 0; i0 < k; i0 += TRB) {
+      const R *ur[TRB];
 #pragma unroll
-      for (int q = 0; q < NQ; q++) acc[q] = R(0);
+      for (int b = 0; b < TRB; b++) ur[b] = A + (i0 + b < k ? i0 + b : 0) * ld;
+      R acc[TRB][NQ];
+#pragma unroll
+      for (int b = 0; b < TRB; b++)
+#pragma unroll
+        for (int q = 0; q < NQ; q++) acc[b][q] = R(0);
       for (int l = 0; l < k; l++) {
-        const R y = ur[l];
+        R uq[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; q++) acc[q] = fmar(y, u[q][l], acc[q]);
+        for (int q = 0; q < NQ; q++) uq[q] = u[q][l];
+#pragma unroll
+        for (int b = 0; b < TRB; b++) {
+          const R y = ur[b][l];
+#pragma unroll
+          for (int q = 0; q < NQ; q++) acc[b][q] = fmar(y, uq[q], acc[b][q]);
+        }
       }
 #pragma unroll
-      for (int q = 0; q < NQ; q++)
-        if (tt + TS * q < k) Tout[i * k + tt + TS * q] = (R)(acc[q] + w[i]);
+      for (int b = 0; b < TRB; b++)
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+          if (i0 + b < k && tt + TS * q < k) Tout[(i0 + b) * k + tt + TS * q] = (R)(acc[b][q] + w[i0 + b]);
     }
   }
 }
@@ -648,13 +663,28 @@ __global__ void __launch_bounds__(32 * RWPB, 4) k_eig_tri_r(EigArgs a, EigSplit 
   for (int j = 0; j < k - 2; j++) {
     float *vj = VH + j * K;
     __syncwarp();
+    // the owner of row j stores it whole (columns past k are zero in A);
+    // then d_j is taken and columns 0..j are cleared, one per lane
     if (lane == (j & 31)) {
-      const int oq = j >> 5;
+      if (NQ == 1 || (j >> 5) == 0) {
 #pragma unroll
-      for (int c = 0; c < K; c++) {
-        const float x = (NQ == 1 || oq == 0) ? A[0][c] : A[NQ - 1][c];
-        vj[c] = (c > j && c < k) ? x : 0.0f;
-        if (c == j) dd[j] = x;
+        for (int c4 = 0; c4 < K4; c4++)
+          *reinterpret_cast<float4 *>(vj + 4 * c4) =
+              make_float4(A[0][4 * c4], A[0][4 * c4 + 1], A[0][4 * c4 + 2], A[0][4 * c4 + 3]);
+      } else {
+#pragma unroll
+        for (int c4 = 0; c4 < K4; c4++)
+          *reinterpret_cast<float4 *>(vj + 4 * c4) = make_float4(A[NQ - 1][4 * c4], A[NQ - 1][4 * c4 + 1],
+                                                                 A[NQ - 1][4 * c4 + 2], A[NQ - 1][4 * c4 + 3]);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int c = lane + 32 * q;
+      if (c <= j) {
+        if (c == j) dd[j] = vj[j];
+        vj[c] = 0.0f;
       }
     }
     __syncwarp();
@@ -840,13 +870,17 @@ __global__ void __launch_bounds__(32 * NW) k_eig_tri_t(EigArgs a, EigSplit sp, i
   for (int j = 0; j < k - 2; j++) {
     float *vj = VH + j * K;
     __syncthreads();
+    // thread j stores its row whole (columns past k are zero in A); then d_j
+    // is taken and columns 0..j are cleared, one per thread
     if (t == j) {
 #pragma unroll
-      for (int c = 0; c < K; c++) {
-        const float x = A[c];
-        vj[c] = (c > j && c < k) ? x : 0.0f;
-        if (c == j) dd[j] = x;
-      }
+      for (int c4 = 0; c4 < K4; c4++)
+        *reinterpret_cast<float4 *>(vj + 4 * c4) = make_float4(A[4 * c4], A[4 * c4 + 1], A[4 * c4 + 2], A[4 * c4 + 3]);
+    }
+    __syncthreads();
+    if (t <= j) {
+      if (t == j) dd[j] = vj[j];
+      vj[t] = 0.0f;
     }
     __syncthreads();
     const float xt = t < K ? vj[t] : 0.0f;
@@ -1093,6 +1127,7 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
       float z[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; q++) z[q] = own[q] ? qr[q][m] : 0.0f;
+#pragma unroll 2
       for (int r = 0; r < cnt; r++) {
         const float2 cs = rot[r];
         const float c = cs.x, s = cs.y;
