@@ -476,14 +476,18 @@ __global__ void k_eig(EigArgs a, int wpb) {
 // is conflict-free.
 __host__ __device__ __forceinline__ int ptri(int i) { return i * (i + 1) / 2; }
 
-__host__ __device__ __forceinline__ int eig_pk_floats(int k) { return ((ptri(k) + 3) & ~3) + 6 * k + 8; }
+// the vectors d .. vv each start on a 16-byte boundary (k rounded up to 4)
+__host__ __device__ __forceinline__ int eig_pk_floats(int k) {
+  return ((ptri(k) + 3) & ~3) + 6 * ((k + 3) & ~3) + 8;
+}
 
 struct EigPk {
   float *L, *d, *e, *tau, *p, *w, *vv;
   __device__ EigPk(float *base, int k) {
+    const int k4 = (k + 3) & ~3;
     L = base;
     d = L + ((ptri(k) + 3) & ~3);
-    e = d + k; tau = e + k; p = tau + k; w = p + k; vv = w + k;
+    e = d + k4; tau = e + k4; p = tau + k4; w = p + k4; vv = w + k4;
   }
 };
 
@@ -514,15 +518,24 @@ __device__ __forceinline__ void eig_householder_pk(int k, EigPk &P, const Team<N
     if (tt == 0) { L[ptri(j + 1) + j] = v0; tau[j] = t; e[j] = alpha; d[j] = L[ptri(j) + j]; }
     for (int r = tt; r < m; r += TS) vv[r] = r == 0 ? v0 : L[ptri(j + 1 + r) + j];
     T.sync();
-    // p = t * A22 v: row r's own segment for c <= r, its column below for c > r
+    // p = t * A22 v: row r's own segment for c <= r, its column below for
+    // c > r (ascending c; v read four at a time in the segment)
     for (int r = tt; r < m; r += TS) {
       const int R = j + 1 + r;
       const float *rowR = L + ptri(R) + (j + 1);
-      int ci = ptri(j + 1) + R;              // L[j+1+c][R], c > r
       float acc = 0.0f;
-      for (int c = 0; c < m; c++) {
-        const float av = c <= r ? rowR[c] : L[ci];
-        acc = fmar(av, vv[c], acc);
+      int c = 0;
+      for (; c + 3 <= r; c += 4) {
+        const float4 v4 = *reinterpret_cast<const float4 *>(vv + c);
+        acc = fmar(rowR[c], v4.x, acc);
+        acc = fmar(rowR[c + 1], v4.y, acc);
+        acc = fmar(rowR[c + 2], v4.z, acc);
+        acc = fmar(rowR[c + 3], v4.w, acc);
+      }
+      for (; c <= r; c++) acc = fmar(rowR[c], vv[c], acc);
+      int ci = ptri(R + 1) + R;              // L[j+1+c][R] at c = r + 1
+      for (c = r + 1; c < m; c++) {
+        acc = fmar(L[ci], vv[c], acc);
         ci += j + 2 + c;
       }
       p[r] = t * acc;
@@ -537,7 +550,15 @@ __device__ __forceinline__ void eig_householder_pk(int k, EigPk &P, const Team<N
     for (int r = tt; r < m; r += TS) {
       float *rowR = L + ptri(j + 1 + r) + (j + 1);
       const float vr = vv[r], wr = w[r];
-      for (int c = 0; c <= r; c++) rowR[c] = rowR[c] - fmar(vr, w[c], wr * vv[c]);
+      int c = 0;
+      for (; c + 3 <= r; c += 4) {
+        const float4 w4 = *reinterpret_cast<const float4 *>(w + c), v4 = *reinterpret_cast<const float4 *>(vv + c);
+        rowR[c] = rowR[c] - fmar(vr, w4.x, wr * v4.x);
+        rowR[c + 1] = rowR[c + 1] - fmar(vr, w4.y, wr * v4.y);
+        rowR[c + 2] = rowR[c + 2] - fmar(vr, w4.z, wr * v4.z);
+        rowR[c + 3] = rowR[c + 3] - fmar(vr, w4.w, wr * v4.w);
+      }
+      for (; c <= r; c++) rowR[c] = rowR[c] - fmar(vr, w[c], wr * vv[c]);
     }
     T.sync();
   }

@@ -231,14 +231,22 @@ __device__ __forceinline__ void put_record(unsigned char *rec0, int cb, int k, i
   reinterpret_cast<float4 *>(r + 256)[e] = B;
   float *yT = reinterpret_cast<float *>(r + 512);
   if (hx) {
+    // the member row through the read-only path, four 16-byte loads in
+    // flight before their stores
     const float4 *h4 = reinterpret_cast<const float4 *>(hx);
-    for (int qq = 0; qq < (kp >> 2); qq++) {
-      const float4 v = h4[qq];
-      const int i = 4 * qq;
-      if (i + 0 < k) yT[(i + 0) * YS + e] = v.x;
-      if (i + 1 < k) yT[(i + 1) * YS + e] = v.y;
-      if (i + 2 < k) yT[(i + 2) * YS + e] = v.z;
-      if (i + 3 < k) yT[(i + 3) * YS + e] = v.w;
+    const int n4 = kp >> 2;
+    for (int q0 = 0; q0 < n4; q0 += 4) {
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) v[u] = q0 + u < n4 ? __ldg(h4 + q0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int i = 4 * (q0 + u);
+        if (i + 0 < k) yT[(i + 0) * YS + e] = v[u].x;
+        if (i + 1 < k) yT[(i + 1) * YS + e] = v[u].y;
+        if (i + 2 < k) yT[(i + 2) * YS + e] = v[u].z;
+        if (i + 3 < k) yT[(i + 3) * YS + e] = v[u].w;
+      }
     }
     yT[k * YS + e] = B.x;
   } else {
