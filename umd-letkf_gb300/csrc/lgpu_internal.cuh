@@ -477,7 +477,7 @@ struct TcArgs {
   // segments (one CTA each), and each CTA moves its tensor-core accumulator
   // out every `drain` chunks (the FP32 accumulation error of the tensor core
   // grows with the MMAs summed into one accumulator); launch_gram_segsum sums
-  // a tile's drained partials in FP64, in stream order
+  // a tile's drained partials in stream order, compensated (doubled precision)
   const TcWork *work;     // [nwork] work items (tile order, then segment)
   int nwork;
   int drain;              // chunks per drain interval
