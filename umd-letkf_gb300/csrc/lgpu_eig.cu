@@ -455,184 +455,18 @@ __global__ void k_eig(EigArgs a, int wpb) {
 }
 
 // ---------------------------------------------------------------------------
-// Split pipeline (same arithmetic as k_eig, bit-identical results up to
-// k = 48):
-//   k_eig_tri  team per unit: Householder + Q (to global), d and e; above
-//              k = 48 k_eig_trip: the reduction on the packed lower triangle,
-//              reflectors and tau to global
+// Split pipeline (the arithmetic of k_eig):
+//   k_eig_tri_r / k_eig_tri_t  the Householder reduction and Q with the work
+//              matrix in registers (a warp per unit up to k = 48, a team of
+//              ceil(k / 32) warps with one row per thread above); Q, d and e
+//              to global
 //   k_eig_ql   thread per unit: the QL recurrence on (d, e) alone, logging
 //              every sweep (start index, rotation count) and rotation (c, s)
-//   k_eig_vec  team per unit: (above k = 48) Q formed from the reflectors,
-//              the logged rotations applied to Q's columns (V = Q Z), then
-//              the spectral functions and T
+//   k_eig_vec  team per unit: the logged rotations applied to Q's columns
+//              (V = Q Z), then the spectral functions and T
 //   k_eig_flag (FP32_RESOLVE) warp per unit: units for the FP64 re-solve
 // The scalar recurrence, which the fused kernel evaluates redundantly on all
 // 32 lanes, runs once per unit.
-
-// ---- packed reduction: the symmetric work matrix as its lower triangle,
-// L[i][j] (j <= i) at i(i+1)/2 + j, half the shared memory of the full
-// matrix (twice the units per SM).  Triangular numbers of 32 consecutive rows
-// are distinct modulo 32, so a warp reading one element of each of its rows
-// is conflict-free.
-__host__ __device__ __forceinline__ int ptri(int i) { return i * (i + 1) / 2; }
-
-// the vectors d .. vv each start on a 16-byte boundary (k rounded up to 4)
-__host__ __device__ __forceinline__ int eig_pk_floats(int k) {
-  return ((ptri(k) + 3) & ~3) + 6 * ((k + 3) & ~3) + 8;
-}
-
-struct EigPk {
-  float *L, *d, *e, *tau, *p, *w, *vv;
-  __device__ EigPk(float *base, int k) {
-    const int k4 = (k + 3) & ~3;
-    L = base;
-    d = L + ((ptri(k) + 3) & ~3);
-    e = d + k4; tau = e + k4; p = tau + k4; w = p + k4; vv = w + k4;
-  }
-};
-
-// The Householder reduction of eig_tridiag_q on the packed lower triangle:
-// the same steps, with the trailing block read as A22[r][c] = L[max][min]
-// and its rank-two update applied to the lower triangle only (v_j stays in
-// column j below the diagonal, tau[j] and d, e as in eig_tridiag_q).
-template <int NW>
-__device__ __forceinline__ void eig_householder_pk(int k, EigPk &P, const Team<NW> &T) {
-  const int tt = T.tt, TS = T.TS;
-  float *L = P.L, *d = P.d, *e = P.e, *tau = P.tau, *p = P.p, *w = P.w, *vv = P.vv;
-  for (int j = 0; j < k - 2; j++) {
-    const int m = k - j - 1;                 // length of x = A[j+1:, j]
-    float s = 0.0f;
-    for (int r = tt; r < m; r += TS) { const float x = L[ptri(j + 1 + r) + j]; s += x * x; }
-    const float sig = T.sum(s);
-    const float x0 = L[ptri(j + 1) + j];
-    const float s1 = sig - x0 * x0;
-    if (!(s1 > Lim<float>::tiny * sig) || sig == 0.0f) {
-      if (tt == 0) { tau[j] = 0.0f; e[j] = x0; d[j] = L[ptri(j) + j]; }
-      T.sync();
-      continue;
-    }
-    const float alpha = -copysign(sqrt(sig), x0);
-    const float v0 = x0 - alpha;
-    const float t = 2.0f / (v0 * v0 + s1);
-    T.sync();
-    if (tt == 0) { L[ptri(j + 1) + j] = v0; tau[j] = t; e[j] = alpha; d[j] = L[ptri(j) + j]; }
-    for (int r = tt; r < m; r += TS) vv[r] = r == 0 ? v0 : L[ptri(j + 1 + r) + j];
-    T.sync();
-    // p = t * A22 v: row r's own segment for c <= r, its column below for
-    // c > r (ascending c; v read four at a time in the segment)
-    for (int r = tt; r < m; r += TS) {
-      const int R = j + 1 + r;
-      const float *rowR = L + ptri(R) + (j + 1);
-      float acc = 0.0f;
-      int c = 0;
-      for (; c + 3 <= r; c += 4) {
-        const float4 v4 = *reinterpret_cast<const float4 *>(vv + c);
-        acc = fmar(rowR[c], v4.x, acc);
-        acc = fmar(rowR[c + 1], v4.y, acc);
-        acc = fmar(rowR[c + 2], v4.z, acc);
-        acc = fmar(rowR[c + 3], v4.w, acc);
-      }
-      for (; c <= r; c++) acc = fmar(rowR[c], vv[c], acc);
-      int ci = ptri(R + 1) + R;              // L[j+1+c][R] at c = r + 1
-      for (c = r + 1; c < m; c++) {
-        acc = fmar(L[ci], vv[c], acc);
-        ci += j + 2 + c;
-      }
-      p[r] = t * acc;
-    }
-    T.sync();
-    float pv = 0.0f;
-    for (int r = tt; r < m; r += TS) pv = fmar(p[r], vv[r], pv);
-    const float beta = 0.5f * t * T.sum(pv);
-    for (int r = tt; r < m; r += TS) w[r] = p[r] - beta * vv[r];
-    T.sync();
-    // A22 -= v w^T + w v^T on the lower triangle
-    for (int r = tt; r < m; r += TS) {
-      float *rowR = L + ptri(j + 1 + r) + (j + 1);
-      const float vr = vv[r], wr = w[r];
-      int c = 0;
-      for (; c + 3 <= r; c += 4) {
-        const float4 w4 = *reinterpret_cast<const float4 *>(w + c), v4 = *reinterpret_cast<const float4 *>(vv + c);
-        rowR[c] = rowR[c] - fmar(vr, w4.x, wr * v4.x);
-        rowR[c + 1] = rowR[c + 1] - fmar(vr, w4.y, wr * v4.y);
-        rowR[c + 2] = rowR[c + 2] - fmar(vr, w4.z, wr * v4.z);
-        rowR[c + 3] = rowR[c + 3] - fmar(vr, w4.w, wr * v4.w);
-      }
-      for (; c <= r; c++) rowR[c] = rowR[c] - fmar(vr, w[c], wr * vv[c]);
-    }
-    T.sync();
-  }
-  if (tt == 0) {
-    if (k >= 2) {
-      d[k - 2] = L[ptri(k - 2) + (k - 2)];
-      e[k - 2] = L[ptri(k - 1) + (k - 2)];
-    }
-    d[k - 1] = L[ptri(k - 1) + (k - 1)];
-    e[k - 1] = 0.0f;
-  }
-  T.sync();
-}
-
-// Split pipeline, packed first stage: A from the packed Gram block into the
-// lower triangle, the reduction, then the reflectors (strictly lower part,
-// row-major k x k) with tau on the diagonal to the scratch Q, and d, e;
-// k_eig_vec<.., true> forms Q from them
-template <int NW>
-__global__ void k_eig_trip(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
-  extern __shared__ __align__(16) float sm[];
-  __shared__ float tred[NW];
-  const int k = a.k;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int slot = NW == 1 ? warp : 0;
-  const int ub = blockIdx.x * wpb + slot;
-  if (ub >= nb) return;
-  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
-  if (a.nkept[unit] <= 0) return;
-  EigPk P(sm + (size_t)slot * eig_pk_floats(k), k);
-  const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
-  const int tt = T.tt, TS = T.TS;
-  const float *Gin = a.G + (size_t)unit * packed_size(k);
-  // (k-1)/infl on the diagonal, src/letkf_core.F90:101-104
-  const float shift = (float)(k - 1) * 1.0f / a.infl;
-  for (int i = 0; i < k; i++)
-    for (int j = tt; j <= i; j += TS) {
-      float v = Gin[tri_idx(j, i, k)];
-      if (i == j) v += shift;
-      P.L[ptri(i) + j] = v;
-    }
-  T.sync();
-  eig_householder_pk(k, P, T);
-  float *Q = sp.Q + (size_t)ub * k * k;
-  for (int i = 0; i < k; i++)
-    for (int j = tt; j < k; j += TS)
-      Q[i * k + j] = j < i ? P.L[ptri(i) + j] : ((j == i && i < k - 2) ? P.tau[i] : 0.0f);
-  float *de = sp.DE + (size_t)ub * 2 * k;
-  for (int t = tt; t < k; t += TS) { de[t] = P.d[t]; de[k + t] = P.e[t]; }
-}
-
-// NW = 1: wpb units per CTA, one warp each; NW > 1: one unit per CTA of NW
-// warps (wpb = 1)
-template <int NQ, int NW>
-__global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
-  extern __shared__ __align__(16) float sm[];
-  __shared__ float tred[NW];
-  const int k = a.k;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int slot = NW == 1 ? warp : 0;
-  const int ub = blockIdx.x * wpb + slot;
-  if (ub >= nb) return;
-  const int unit = a.ulist ? a.ulist[u0 + ub] : u0 + ub;
-  if (a.nkept[unit] <= 0) return;
-  EigWork W(sm + (size_t)slot * eig_floats_per_warp(k), k);
-  const Team<NW> T{NW == 1 ? lane : (int)threadIdx.x, lane, warp, tred};
-  eig_load(a, unit, W, T);
-  eig_tridiag_q<NQ>(k, W, T);
-  const int ld = k + 1;
-  float *Q = sp.Q + (size_t)ub * k * k;
-  for (int t = T.tt; t < k * k; t += T.TS) Q[t] = W.A[(t / k) * ld + (t % k)];
-  float *de = sp.DE + (size_t)ub * 2 * k;
-  for (int t = T.tt; t < k; t += T.TS) { de[t] = W.d[t]; de[k + t] = W.e[t]; }
-}
 
 // The first stage for k <= 48 with the work matrix in registers: one warp
 // per unit, lane l holds rows l and l + 32 of A (K = k rounded up to 8
@@ -645,7 +479,7 @@ __global__ void k_eig_tri(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
 // they lie left of the block.  The dot products run over the columns in
 // ascending order as the shared-memory form does.  Q = H_0 ... H_{k-3} is
 // then formed with lane l holding columns l and l + 32 in the same registers
-// (reflectors applied from the last to the first).  Output as k_eig_tri: Q
+// (reflectors applied from the last to the first).  Output: Q
 // row-major and (d, e) to the scratch.
 constexpr int RWPB = 4;   // warps (units) per block
 
@@ -1072,7 +906,7 @@ __global__ void __launch_bounds__(QLT) k_eig_ql(EigArgs a, EigSplit sp, int u0, 
   if (bad && !a.flag_list) atomicOr(a.status, bad);   // with flagging, the FP64 re-solve takes the unit
 }
 
-template <int NQ, int NW, bool PK>
+template <int NQ, int NW>
 __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   extern __shared__ __align__(16) float sm[];
   __shared__ float tred[NW];
@@ -1091,12 +925,6 @@ __global__ void k_eig_vec(EigArgs a, EigSplit sp, int wpb, int u0, int nb) {
   float *A = W.A;
   const float *Q = sp.Q + (size_t)ub * k * k;
   for (int t = tt; t < k * k; t += TS) A[(t / k) * ld + (t % k)] = Q[t];
-  if constexpr (PK) {
-    // the scratch holds the reflectors (below the diagonal) and tau (on it): form Q
-    for (int j = tt; j < k; j += TS) W.tau[j] = Q[j * k + j];
-    T.sync();
-    eig_form_q<NQ>(k, W, T);
-  }
   const float *lam = sp.lam + (size_t)ub * k;
   for (int t = tt; t < k; t += TS) W.d[t] = lam[t];
   const float *G = a.G + (size_t)unit * packed_size(k);
@@ -1420,19 +1248,20 @@ static int eig_wpb_floats(int floats) {
 
 static int eig_wpb(int k) { return eig_wpb_floats(eig_floats_per_warp(k)); }
 
-// warps per unit of the split kernels, measured on GB300 (206k units per
-// analysis): k <= 64 one warp (two rows per lane; k = 40: 26 ms, against 33
-// with two warps), k > 64 two warps (two rows per thread; k = 100: 273 ms,
-// against 414 with one warp and 308 / 359 with four / eight)
-static int eig_team(int k) { return k <= 64 ? 1 : 2; }
+// warps per unit of k_eig_vec, measured on GB300: k <= 64 one warp (two
+// rows per lane; C2, k = 40: 26 ms against 33 with two warps), k > 64 four
+// warps (one row per thread; C4, k = 100: eigensolve 693 ms against 717 with
+// two warps of two rows per thread, whose 64-thread teams left 15% of the
+// warp slots filled)
+static int eig_team(int k) { return k <= 64 ? 1 : 4; }
 
-// the split pipeline's first stage: in registers, forming Q (k <= 48 one
-// warp, k <= 64 a two-warp team), or on the packed lower triangle with Q
-// formed in k_eig_vec (above k = 64).  Measured on GB300 (eigensolve ms):
-// k = 40 shared-memory full matrix 25.8, packed 26.6, registers 23.7; k = 64
-// full 57.2, packed 53.8, team registers 49.3; C4 (k = 100) full 1057, packed
-// 974, four-warp team registers 1018
-static bool eig_packed(int k) { return k > 64; }
+// The first stage, in registers with Q formed there: one warp up to k = 48
+// (k_eig_tri_r), above a team of ceil(k / 32) warps with one row per thread
+// (k_eig_tri_t).  Measured on GB300 (eigensolve ms): k = 40 shared-memory
+// full matrix 25.8, packed lower triangle 26.6, registers 23.7; k = 64 full
+// 57.2, packed 53.8, team registers 38.4; C4 (k = 100) full 1057, packed
+// (Q formed in k_eig_vec) 855, four-warp team registers 718.  The shared-memory
+// and packed forms are not built.
 
 // the register-resident first stage (k <= 48)
 static cudaError_t launch_tri_r(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int u0, int nb) {
@@ -1463,29 +1292,28 @@ static cudaError_t launch_tri_t(cudaStream_t st, const EigArgs &a, const EigSpli
   switch ((a.k + 7) & ~7) {
   case 56: return launch_tri_t_k<56, 2>(st, a, sp, u0, nb);
   case 64: return launch_tri_t_k<64, 2>(st, a, sp, u0, nb);
+  case 72: return launch_tri_t_k<72, 3>(st, a, sp, u0, nb);
+  case 80: return launch_tri_t_k<80, 3>(st, a, sp, u0, nb);
+  case 88: return launch_tri_t_k<88, 3>(st, a, sp, u0, nb);
+  case 96: return launch_tri_t_k<96, 3>(st, a, sp, u0, nb);
+  case 104: return launch_tri_t_k<104, 4>(st, a, sp, u0, nb);
+  case 112: return launch_tri_t_k<112, 4>(st, a, sp, u0, nb);
+  case 120: return launch_tri_t_k<120, 4>(st, a, sp, u0, nb);
+  case 128: return launch_tri_t_k<128, 4>(st, a, sp, u0, nb);
   default: return cudaErrorInvalidValue;
   }
 }
 
-template <int NQ, int NW, bool kPackedTri>
+template <int NQ, int NW>
 static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart,
                                   int ucount, int *launches) {
-  // first stage: the packed reduction (kPackedTri) or the full-matrix
-  // reduction + Q; its own warps per block from its shared memory
+  // k_eig_vec: its own warps per block from its shared memory
   const int wpb = NW == 1 ? eig_wpb(a.k) : 1;
   const size_t smem = (size_t)wpb * eig_floats_per_warp(a.k) * sizeof(float);
   const int threads = NW == 1 ? 32 * wpb : 32 * NW;
-  const int wpt = !kPackedTri ? wpb : (NW == 1 ? eig_wpb_floats(eig_pk_floats(a.k)) : 1);
-  const size_t smt = !kPackedTri ? smem : (size_t)wpt * eig_pk_floats(a.k) * sizeof(float);
-  const int tht = NW == 1 ? 32 * wpt : 32 * NW;
   cudaError_t e;
-  if (kPackedTri) {
-    if ((e = cudaFuncSetAttribute(k_eig_trip<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt)) !=
-        cudaSuccess)
-      return e;
-  }
-  if ((e = cudaFuncSetAttribute(k_eig_vec<NQ, NW, kPackedTri>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(k_eig_vec<NQ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+      cudaSuccess)
     return e;
   const size_t qsm = (size_t)2 * a.k * QLT * sizeof(float);
   if ((e = cudaFuncSetAttribute(k_eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm)) != cudaSuccess)
@@ -1493,11 +1321,9 @@ static cudaError_t launch_split_t(cudaStream_t st, const EigArgs &a, const EigSp
   const int uend = ustart + ucount;
   for (int u0 = ustart; u0 < uend; u0 += batch) {
     const int nb = uend - u0 < batch ? uend - u0 : batch;
-    if (kPackedTri) k_eig_trip<NW><<<(nb + wpt - 1) / wpt, tht, smt, st>>>(a, sp, wpt, u0, nb);
-    else if ((e = a.k <= 48 ? launch_tri_r(st, a, sp, u0, nb) : launch_tri_t(st, a, sp, u0, nb)) != cudaSuccess)
-      return e;
+    if ((e = a.k <= 48 ? launch_tri_r(st, a, sp, u0, nb) : launch_tri_t(st, a, sp, u0, nb)) != cudaSuccess) return e;
     k_eig_ql<<<(nb + QLT - 1) / QLT, QLT, qsm, st>>>(a, sp, u0, nb);
-    k_eig_vec<NQ, NW, kPackedTri><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
+    k_eig_vec<NQ, NW><<<(nb + wpb - 1) / wpb, threads, smem, st>>>(a, sp, wpb, u0, nb);
     (*launches) += 3;
     if (a.flag_list) {
       k_eig_flag<<<(nb + 7) / 8, 256, 0, st>>>(a, sp, u0, nb);
@@ -1517,13 +1343,8 @@ size_t eig_split_bytes_per_unit(int k) {
 cudaError_t launch_eig_split(cudaStream_t st, const EigArgs &a, const EigSplit &sp, int batch, int ustart, int ucount,
                              int *launches) {
   if (ucount <= 0) return cudaSuccess;
-  const int k = a.k, nw = eig_team(k);
-  if (nw == 1) {   // k <= 64
-    return eig_packed(k) ? launch_split_t<2, 1, true>(st, a, sp, batch, ustart, ucount, launches)
-                         : launch_split_t<2, 1, false>(st, a, sp, batch, ustart, ucount, launches);
-  }
-  return eig_packed(k) ? launch_split_t<2, 2, true>(st, a, sp, batch, ustart, ucount, launches)   // k <= 128
-                       : launch_split_t<2, 2, false>(st, a, sp, batch, ustart, ucount, launches);
+  if (eig_team(a.k) == 1) return launch_split_t<2, 1>(st, a, sp, batch, ustart, ucount, launches);   // k <= 64
+  return launch_split_t<1, 4>(st, a, sp, batch, ustart, ucount, launches);                            // k <= 128
 }
 
 cudaError_t launch_eig_debug(cudaStream_t st, int nunits, int k, const float *G, const int *nkept, float *T,
