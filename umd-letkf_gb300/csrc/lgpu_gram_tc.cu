@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(WT) k_tile_count(int ntiles, const TilePar *tp
   const TilePar tp = tps[tile];
   build_window(W, tp, geom, cell_start);
   int cnt = 0;
-  for (int j = threadIdx.x; j < W.total; j += WT) cnt += in_cap(tp, obsA[window_pos(W, j)]);
+#pragma unroll 4
+  for (int j = threadIdx.x; j < W.total; j += WT) cnt += in_cap(tp, __ldg(obsA + window_pos(W, j)));
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
   __syncthreads();
@@ -284,13 +285,21 @@ __global__ void __launch_bounds__(WT) k_tile_fill(int ntiles, const TilePar *tps
     }
   };
   int base = 0, pend = 0;
+  // the thread's next window candidate (position and record) is loaded one
+  // iteration ahead, so that its latency overlaps the current compaction
+  int p_nx = 0;
+  float4 a_nx = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (tid < W.total) {
+    p_nx = window_pos(W, tid);
+    a_nx = __ldg(obs.A + p_nx);
+  }
   for (int jb = 0; jb < W.total; jb += WT) {
     const int j = jb + tid;
-    int p = 0;
-    bool ok = false;
-    if (j < W.total) {
-      p = window_pos(W, j);
-      ok = in_cap(tp, obs.A[p]);
+    const int p = p_nx;
+    const bool ok = j < W.total && in_cap(tp, a_nx);
+    if (j + WT < W.total) {
+      p_nx = window_pos(W, j + WT);
+      a_nx = __ldg(obs.A + p_nx);
     }
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     if (lane == 0) wsc[wid] = __popc(m);
