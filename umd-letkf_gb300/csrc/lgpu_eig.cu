@@ -13,13 +13,17 @@
 // QL iteration with Wilkinson shifts on the tridiagonal matrix (the
 // tql2 scheme of Bowdler, Martin, Reinsch & Wilkinson, Numer. Math. 11,
 // 1968), accumulating the rotations into Z, and back-transformation
-// V = Q Z.  A unit is worked on by a team: one warp for k <= 64, two warps
-// (one unit per CTA) for k <= 128; rows of the k x k work matrices are
-// spread over the team's threads (tt + TS q, two per thread).  The fused
-// kernel evaluates the QL scalar recurrence redundantly on every lane of its
-// warp (shared memory broadcasts) with lane 0 as the only writer; the split
-// pipeline runs it once per unit and replays the logged rotations.  The FP64
-// form (k_eig64) runs the same phases in double on a team of 2 or 4 warps.
+// V = Q Z.  The split pipeline (used whenever its scratch fits) reduces in
+// registers (k_eig_tri_r: a warp per unit up to k = 48; k_eig_tri_t: a team
+// of ceil(k / 32) warps, one row per thread, above), runs the QL scalar
+// recurrence once per unit (k_eig_ql) and replays the logged rotations on Q's
+// rows in shared memory (k_eig_vec: one warp, two rows per lane, up to
+// k = 64; four warps, one row per thread, above).  The fused kernel (k_eig,
+// the fallback) works on the matrices in shared memory with the rows spread
+// over a warp's or team's threads (tt + TS q) and evaluates the QL recurrence
+// redundantly on every lane (shared memory broadcasts) with lane 0 as the
+// only writer.  The FP64 form (k_eig64) runs the fused phases in double on a
+// team of 2 or 4 warps.
 #include "lgpu_internal.cuh"
 #include <algorithm>
 
