@@ -59,7 +59,9 @@ def cases(k, rng):
     return out
 
 
-@pytest.mark.parametrize("k", [5, 20, 40, 64, 65, 100, 128])
+# every width of the register-resident first stage (k rounded up to 8: one
+# warp up to 48, a team of ceil(k / 32) warps above) and both replay teams
+@pytest.mark.parametrize("k", [5, 12, 20, 28, 33, 40, 47, 56, 64, 65, 77, 88, 96, 100, 105, 117, 128])
 def test_transform_against_float64(k):
     from letkf_gb300 import Solver
     rng = np.random.default_rng(k)
